@@ -1,0 +1,393 @@
+"""Throughput of the DBSCAN clone-collapsing path on GB300.
+
+Default workload: 64 synthetic amino-acid repertoires of log-uniform size
+5k-500k (~6M sequences), Hamming eps=1, minPts=2 -- the batched workload the
+throughput target is quoted on.  A step clusters all 64 repertoires.
+
+Metric: Gpair-distances/s = admissible unique pairs (V and J overlap, admissible
+length gap, counted once; a property of the workload, not of the schedule) per
+second of device time; sequences/s alongside.
+
+  value   batched path: one CUDA-graph replay per step (idb_batch_run) with the
+          inputs resident in HBM; device time from CUDA events on the library's
+          stream.  Inputs (~0.7 GB) and working set exceed the 129 MB L2.
+  e2e     idb_cluster (the InterlinkClass replacement) with pinned host buffers:
+          H2D of the columns, the whole path, D2H of clone_id/core/copies.
+  plain   the same workload as 64 per-repertoire idb_cluster_device calls.
+
+`--impl reference` times the CPU restatement of the reference path (the
+all-pairs oracle, OpenMP on all host cores) on a bounded sample of the same
+workload; the reference's CUDA code has no CPU backend.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = ("Gpair-distances/s and sequences clustered/s, batched+learned vs plain "
+          "(identical partitions)")
+UNIT = "Gpair-distances/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", type=int, default=2)
+    ap.add_argument("--scale", type=float, default=1.0)
+    ap.add_argument("--schedule", type=int, default=0)
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-rows", type=int, default=60000)
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allreduce_max(world, x: float) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_sample(w, rows: int):
+    """The smallest prefix of repertoires (in order of size) holding about `rows` rows."""
+    sizes = np.diff(w.rep_off)
+    order = np.argsort(sizes, kind="stable")
+    pick, total = [], 0
+    for r in order:
+        if total >= rows:
+            break
+        pick.append(int(r))
+        total += int(sizes[r])
+    pick.sort()
+    return w.subset_repertoires(pick), pick
+
+
+def run_cpu(w, rows: int, threads: int):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    sub, pick = cpu_sample(w, rows)
+    oracle.lib()
+    t0 = time.perf_counter()
+    r = oracle.cluster(sub, n_threads=threads, max_candidates=0)
+    dt = time.perf_counter() - t0
+    return dict(value=r.admissible_pairs / dt / 1e9, seq_per_s=sub.n / dt, seconds=dt,
+                rows=sub.n, reps=len(pick), pairs=r.admissible_pairs)
+
+
+def reference_arm(args, world, rank, w):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rows = max(args.cpu_rows // 2, 5000)
+    for _ in range(max(args.warmup, 0) and 1):
+        run_cpu(w, min(rows, 5000), threads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        res = run_cpu(w, rows, threads)
+        vals.append(res["value"])
+        secs.append(res["seconds"])
+    value = float(np.median(vals))
+    sample = (f"{res['reps']} smallest repertoires of the workload ({res['rows']} rows, "
+              f"{res['pairs']} admissible pairs) per step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": f"{w.name}: {w.n_rep} aa repertoires, {w.n} rows",
+                   "global_batch": w.n, "seq_len": int(w.lengths().max()),
+                   "parallelism": "replicas only"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_init(args)
+    from immunodbscan_gb300 import synth
+    t0 = time.time()
+    w = synth.workload(args.workload, scale=args.scale)
+    gen_s = time.time() - t0
+    if args.impl == "reference":
+        reference_arm(args, world, rank, w)
+        return
+    import torch
+    from immunodbscan_gb300 import Context, DeviceBatch, _lib
+    from immunodbscan_gb300.interlink import Interlink, _as_blob, _p, make_params
+    torch.cuda.set_device(local)
+    L = _lib.lib()
+    ctx = Context(local)
+    n = w.n
+
+    # numerator: admissible unique pairs (setup, untimed)
+    inp, keep = build_host_input(w, pinned=False)
+    prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, args.schedule)
+    adm = C.c_uint64()
+    _lib.check(L.idb_count_admissible(ctx.handle, C.byref(inp), C.byref(prm), C.byref(adm)))
+    admissible = int(adm.value)
+
+    # batched graph path (value)
+    batch = DeviceBatch(w, ctx, schedule=args.schedule)
+    batch.plan()
+    for _ in range(args.warmup):
+        batch.run()
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ms, ms_dist, phases, launches = [], [], [], 0
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        st = batch.run()
+        ms.append(st.ms_total)
+        ms_dist.append(st.ms_distance)
+        phases.append([st.ms_phase[k] for k in range(5)])
+        launches += st.kernel_launches
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier(world)
+    clk = clocks.stop()
+    step_ms = allreduce_max(world, float(np.mean(ms)))
+    value = world * admissible / (step_ms * 1e-3) / 1e9
+    seq_per_s = world * n / (step_ms * 1e-3)
+    last = st
+    clone_b, core_b, copies_b = batch.results()
+
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "u8",
+           "data": "synthetic (seeded generator, no public dataset)",
+           "config": {"workload": f"{w.name}: {w.n_rep} aa repertoires, {n} rows, "
+                                  f"{'Hamming' if w.use_hamming else 'Levenshtein'} "
+                                  f"eps={w.abs_eps}, minPts={w.min_pts}",
+                      "global_batch": n * world, "seq_len": int(w.lengths().max()),
+                      "parallelism": "replicas only" if world > 1 else "single GPU",
+                      "l2": "inputs and working set larger than L2 (129 MB)",
+                      "schedule": "learned" if args.schedule == 1 else "static heavy-first"},
+           "seq_per_s": seq_per_s, "admissible_pairs": admissible,
+           "pairs_evaluated": int(last.pairs_evaluated),
+           "neighbour_pairs": int(last.neighbour_pairs), "n_uniques": int(last.n_uniques),
+           "n_clusters": int(last.n_clusters), "gpu_launches": int(launches),
+           "phase_ms": {k: float(np.mean([p[i] for p in phases])) for i, k in
+                        enumerate(["front_dedupe", "buckets_schedule", "distance", "graph",
+                                   "outputs"])},
+           "wall_ms_per_step": 1e3 * wall / args.steps, "gen_seconds": gen_s,
+           "clocks": clk}
+
+    # roofline of the distance kernel: integer logic against the measured int peak
+    gops = C.c_double()
+    pms = C.c_double()
+    L.idb_diag_int_peak(local, C.byref(gops), C.byref(pms))
+    ops_pair = ops_per_pair(w, batch)
+    t_dist = float(np.mean(ms_dist)) * 1e-3
+    achieved = ops_pair * last.pairs_evaluated / t_dist / 1e9 if t_dist > 0 else 0.0
+    out["roofline"] = {"bound": "int", "achieved": achieved, "peak": gops.value,
+                       "unit": "Gop/s (32-bit integer logic)",
+                       "frac": achieved / gops.value if gops.value else None,
+                       "traffic": None, "kernel": "k_hamming" if w.use_hamming else "k_levenshtein",
+                       "ops_per_pair": ops_pair, "kernel_ms": t_dist * 1e3,
+                       "peak_source": "measured: idb_diag_int_peak (lop3/add chains, all SMs)"}
+
+    # e2e through idb_cluster with pinned host buffers
+    if not args.no_e2e:
+        hin, hkeep = build_host_input(w, pinned=True)
+        clone = torch.empty(n, dtype=torch.int32).pin_memory()
+        core = torch.empty(n, dtype=torch.int32).pin_memory()
+        copies = torch.empty(n, dtype=torch.int32).pin_memory()
+        o = _lib.Output(clone.data_ptr(), core.data_ptr(), copies.data_ptr(), None, None, None,
+                        None)
+        for _ in range(max(1, args.warmup)):
+            _lib.check(L.idb_cluster(ctx.handle, C.byref(hin), C.byref(prm), C.byref(o)))
+        barrier(world)
+        times = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            _lib.check(L.idb_cluster(ctx.handle, C.byref(hin), C.byref(prm), C.byref(o)))
+            times.append(time.perf_counter() - t0)
+        barrier(world)
+        e2e_s = allreduce_max(world, float(np.mean(times)))
+        h2d = sum(int(a.numel() * a.element_size()) for a in hkeep if isinstance(a, torch.Tensor))
+        out["e2e"] = {"value": world * admissible / e2e_s / 1e9, "unit": UNIT,
+                      "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * n,
+                      "ms_per_step": e2e_s * 1e3, "seq_per_s": world * n / e2e_s,
+                      "api": "idb_cluster (host buffers)"}
+        same = (np.array_equal(clone.numpy().view(np.uint32), clone_b) and
+                np.array_equal(core.numpy(), core_b))
+        out["e2e"]["identical_partitions_vs_batched"] = bool(same)
+
+    # plain per-repertoire path
+    if not args.no_plain:
+        plain_ms = []
+        subs = [DeviceBatch(w.subset_repertoires([r]), ctx, schedule=args.schedule)
+                for r in range(w.n_rep)]
+        for sb in subs:
+            sb.cluster_once()
+        for _ in range(max(1, min(args.steps, 3))):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for sb in subs:
+                sb.cluster_once()
+            torch.cuda.synchronize()
+            plain_ms.append(1e3 * (time.perf_counter() - t0))
+        pm = float(np.mean(plain_ms))
+        same = True
+        for r, sb in enumerate(subs):
+            c_, k_, p_ = sb.results()
+            lo, hi = int(w.rep_off[r]), int(w.rep_off[r + 1])
+            same &= np.array_equal(c_, clone_b[lo:hi]) and np.array_equal(k_, core_b[lo:hi])
+        out["plain"] = {"value": admissible / (pm * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pm,
+                        "api": "64 x idb_cluster_device (eager, per repertoire)",
+                        "batched_speedup": pm / step_ms, "identical_partitions": bool(same)}
+
+    if rank == 0 and not args.no_cpu:
+        res = run_cpu(w, args.cpu_rows, os.cpu_count() or 1)
+        out["cpu_baseline"] = {"value": res["value"], "unit": UNIT, "cores": os.cpu_count(),
+                               "kind": "port",
+                               "sample": f"{res['reps']} smallest repertoires ({res['rows']} rows, "
+                                         f"{res['pairs']} admissible pairs), "
+                                         f"{res['seconds']:.1f} s"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    ctx.close()
+
+
+def ops_per_pair(w, batch) -> int:
+    """Algorithmic 32-bit integer ops per evaluated pair of the distance kernel.
+
+    Hamming (bit planes): one LOP3 per plane word folds XOR and OR, then the
+    population test (eps==1: x & (x-1) == 0 -> 2 ops + 1 compare; otherwise
+    popc + add per word + 1 compare).  Levenshtein: ~16 ops per text column.
+    """
+    L = int(w.lengths().max())
+    Wd = max(1, (L + 31) // 32)
+    planes = 2 if len(set(w.seq_blob.tolist()[:200000])) <= 4 else 5
+    if w.use_hamming:
+        if Wd == 1 and w.abs_eps == 1 and math.isnan(w.threshold):
+            return planes + 3
+        return planes * Wd + 2 * Wd + 1
+    return 16 * int(np.mean(w.lengths()))
+
+
+def build_host_input(w, pinned: bool):
+    """idb_input over host copies of the workload columns (pinned if asked)."""
+    import torch
+    from immunodbscan_gb300 import _lib
+    from immunodbscan_gb300.interlink import _as_blob
+    keep = []
+
+    def host(a):
+        t = torch.from_numpy(np.ascontiguousarray(a))
+        if pinned:
+            t = t.pin_memory()
+        keep.append(t)
+        return t.data_ptr()
+
+    inp = _lib.Input()
+    inp.n_rows = w.n
+    inp.seqs, inp.seq_offsets = host(w.seq_blob if w.seq_blob.size else np.zeros(1, np.uint8)), host(w.seq_off)
+    inp.v_calls, inp.v_offsets = host(w.v_blob), host(w.v_off)
+    inp.j_calls, inp.j_offsets = host(w.j_blob), host(w.j_off)
+    vb, vo = _as_blob(w.v_genes)
+    jb, jo = _as_blob(w.j_genes)
+    roff = np.ascontiguousarray(w.rep_off, np.uint32)
+    keep += [vb, vo, jb, jo, roff]
+    inp.v_genes, inp.v_gene_offsets, inp.n_v_genes = vb.ctypes.data, vo.ctypes.data, len(w.v_genes)
+    inp.j_genes, inp.j_gene_offsets, inp.n_j_genes = jb.ctypes.data, jo.ctypes.data, len(w.j_genes)
+    inp.n_repertoires = w.n_rep
+    inp.rep_offsets = roff.ctypes.data
+    return inp, keep
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,870 @@
+// idb_api.cu -- C ABI, contexts, workspace, plan and pipeline orchestration.
+//
+// The reference's boundary is InterlinkClass (cuda/Interlink.cu:34-95): build
+// the V and J bitset containers, the string set, run DBSCAN::doScan
+// (cuda/PSDBSCAN.hcu:1300-1356, nine phases each followed by
+// cudaDeviceSynchronize) and copy clusters, cores, uniques and copies back.
+// idb_cluster is that boundary with plain C types.  The pipeline here is
+// device-driven: every kernel reads its work counts from device memory, so the
+// same launch sequence runs eagerly (with a few size read-backs that grow the
+// workspace) or replays from a captured CUDA graph (idb_batch_run).
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/immunodbscan_gb300.h"
+#include "../../include/immunodbscan_gb300_diag.h"
+#include "idb_internal.cuh"
+
+namespace idb {
+void launch_const_strings(uint8_t *blob, int64_t *off, uint32_t N, cudaStream_t s);
+void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s);
+}
+
+namespace {
+
+using namespace idb;
+
+thread_local std::string g_err;
+
+idb_status fail(idb_status st, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return st;
+}
+
+#define CU(call)                                                                        \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess) {                                                        \
+            if (e_ == cudaErrorMemoryAllocation)                                        \
+                return fail(IDB_ERR_OUT_OF_MEMORY, "%s: %s", #call, cudaGetErrorString(e_)); \
+            return fail(IDB_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_));         \
+        }                                                                               \
+    } while (0)
+
+#define TRY(expr)                                 \
+    do {                                          \
+        idb_status st_ = (expr);                  \
+        if (st_ != IDB_OK) return st_;            \
+    } while (0)
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+};
+
+enum BufId {
+    bSeq, bSeqOff, bV, bVOff, bJ, bJOff, bVGenes, bVGOff, bJGenes, bJGOff, bRepOff, bEps, bCode,
+    bVBits, bJBits, bSlot, bRepRow, bFlag, bUidOfRow, bRow2Uid, bTable, bTCount,
+    bURow, bUCopies, bULen, bURep, bBinHist, bBinCursor, bEntUid, bEntRec, bBpCount, bBp,
+    bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bDeg, bGOff, bGCur, bAdj, bCnt, bUCore,
+    bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
+    bCtr, bNumBufs
+};
+
+}  // namespace
+
+struct idb_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    DevBuf buf[bNumBufs];
+    Counters *h_ctr = nullptr;        // pinned mirror of the counters
+    cudaEvent_t ev[16] = {};
+    // batch (graph) state
+    bool planned = false;
+    Plan plan;
+    Buffers bufs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    idb_output out_dev{};
+    bool trees = false;
+    uint32_t graph_kernels = 0;
+};
+
+namespace {
+
+idb_status ensure(idb_context *c, BufId id, size_t bytes, bool exact = false) {
+    DevBuf &b = c->buf[id];
+    if (bytes == 0) bytes = 16;
+    if (b.cap >= bytes) return IDB_OK;
+    if (b.p) CU(cudaFree(b.p));
+    b.p = nullptr;
+    b.cap = 0;
+    size_t want = exact ? bytes : bytes + bytes / 8 + 256;
+    want = (want + 255) & ~(size_t)255;
+    cudaError_t e = cudaMalloc(&b.p, want);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return fail(IDB_ERR_OUT_OF_MEMORY, "device allocation of %zu bytes failed", want);
+    }
+    b.cap = want;
+    return IDB_OK;
+}
+
+template <typename T>
+T *ptr(idb_context *c, BufId id) { return reinterpret_cast<T *>(c->buf[id].p); }
+
+idb_status check_launch() {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(IDB_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e));
+    return IDB_OK;
+}
+
+uint64_t next_pow2(uint64_t x) {
+    uint64_t p = 1;
+    while (p < x) p <<= 1;
+    return p;
+}
+
+// eps(Lx,Ly) exactly as the reference computes it in single precision:
+// (int)truncf((float)max(Lx,Ly) * threshold) (cuda/SpecialFunctors.hcu:257-261),
+// capped by the absolute eps when that key is set.
+int eps_value(uint32_t lx, uint32_t ly, float threshold, int32_t abs_eps) {
+    int64_t e = INT32_MAX;
+    if (!std::isnan(threshold)) {
+        volatile float m = (float)(lx > ly ? lx : ly);
+        volatile float prod = m * threshold;
+        float t = truncf(prod);
+        if (t >= 2147483647.0f) e = INT32_MAX;
+        else if (t <= -2147483648.0f) e = INT32_MIN;
+        else e = (int64_t)t;
+    }
+    if (abs_eps >= 0 && abs_eps < e) e = abs_eps;
+    return (int)e;
+}
+
+idb_status get_ctx(idb_context **pc);
+
+struct HostInputs {
+    // staged or caller device pointers
+    const uint8_t *seq; const int64_t *seq_off;
+    const uint8_t *v; const int64_t *v_off;
+    const uint8_t *j; const int64_t *j_off;
+};
+
+idb_status validate(const idb_input *in, const idb_params *prm, const idb_output *out) {
+    if (!in || !prm || !out) return fail(IDB_ERR_INVALID_ARG, "NULL argument");
+    if (in->n_rows > 0 && (!out->clone_id || !out->core || !out->copies))
+        return fail(IDB_ERR_INVALID_ARG, "clone_id, core and copies outputs are required");
+    if ((in->v_calls == nullptr) != (in->v_offsets == nullptr))
+        return fail(IDB_ERR_INVALID_ARG, "v_calls and v_offsets must both be set or both NULL");
+    if ((in->j_calls == nullptr) != (in->j_offsets == nullptr))
+        return fail(IDB_ERR_INVALID_ARG, "j_calls and j_offsets must both be set or both NULL");
+    if ((in->seqs == nullptr) != (in->seq_offsets == nullptr))
+        return fail(IDB_ERR_INVALID_ARG, "seqs and seq_offsets must both be set or both NULL");
+    if (in->v_calls && in->n_v_genes && (!in->v_genes || !in->v_gene_offsets))
+        return fail(IDB_ERR_INVALID_ARG, "V reference gene list missing");
+    if (in->j_calls && in->n_j_genes && (!in->j_genes || !in->j_gene_offsets))
+        return fail(IDB_ERR_INVALID_ARG, "J reference gene list missing");
+    if (in->v_calls && in->n_v_genes > 64u * kMaxGeneWords)
+        return fail(IDB_ERR_UNSUPPORTED, "at most %d V reference genes", 64 * kMaxGeneWords);
+    if (in->j_calls && in->n_j_genes > 64u * kMaxGeneWords)
+        return fail(IDB_ERR_UNSUPPORTED, "at most %d J reference genes", 64 * kMaxGeneWords);
+    if (std::isnan(prm->threshold) && prm->abs_eps < 0)
+        return fail(IDB_ERR_INVALID_ARG, "neither threshold nor abs_eps is set");
+    if (in->n_repertoires > 0 && in->rep_offsets) {
+        if (in->rep_offsets[0] != 0 || in->rep_offsets[in->n_repertoires] != in->n_rows)
+            return fail(IDB_ERR_INVALID_ARG, "rep_offsets must start at 0 and end at n_rows");
+        for (uint32_t r = 0; r < in->n_repertoires; ++r)
+            if (in->rep_offsets[r] > in->rep_offsets[r + 1])
+                return fail(IDB_ERR_INVALID_ARG, "rep_offsets must be non-decreasing");
+    }
+    if (in->n_rows >= 0x7FFFFFFFu) return fail(IDB_ERR_UNSUPPORTED, "at most 2^31-2 rows");
+    return IDB_OK;
+}
+
+// Gene name lists -> device (host memory always).
+idb_status upload_genes(idb_context *c, const char *names, const int64_t *off, uint32_t G,
+                        BufId blob_id, BufId off_id, uint32_t *bytes_out) {
+    std::vector<int32_t> o(G + 1);
+    const int64_t base = G ? off[0] : 0;
+    for (uint32_t g = 0; g <= G; ++g) o[g] = (int32_t)(off[g] - base);
+    const size_t nb = G ? (size_t)(off[G] - base) : 0;
+    TRY(ensure(c, blob_id, nb + 16));
+    TRY(ensure(c, off_id, sizeof(int32_t) * (G + 1)));
+    if (nb) CU(cudaMemcpyAsync(c->buf[blob_id].p, names + base, nb, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->buf[off_id].p, o.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));   // o is a local
+    *bytes_out = (uint32_t)nb;
+    return IDB_OK;
+}
+
+struct Pipeline {
+    idb_context *c;
+    Plan P;
+    Buffers B;
+    bool trees = false;
+    bool timing = false;
+    std::vector<int16_t> eps_host;
+};
+
+void record(Pipeline &pl, int k) {
+    if (pl.timing) cudaEventRecord(pl.c->ev[k], pl.c->stream);
+}
+
+// Stage 0: inputs in place, counters zeroed, survey run and read back.
+idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_inputs) {
+    idb_context *c = pl.c;
+    Plan &P = pl.P;
+    Buffers &B = pl.B;
+    cudaStream_t s = c->stream;
+    P.N = in->n_rows;
+    P.R = (in->n_repertoires > 0 && in->rep_offsets) ? in->n_repertoires : 1;
+    P.no_v = in->v_calls == nullptr;
+    P.no_j = in->j_calls == nullptr;
+    P.no_seq = in->seqs == nullptr;
+    TRY(ensure(c, bCtr, sizeof(Counters)));
+    B.ctr = ptr<Counters>(c, bCtr);
+    CU(cudaMemsetAsync(B.ctr, 0, sizeof(Counters), s));
+    CU(cudaMemsetAsync(&B.ctr->lmin, 0xFF, sizeof(uint32_t), s));   // min starts at max
+    auto stage = [&](const char *src, const int64_t *off, BufId bid, BufId oid,
+                     const uint8_t **dst, const int64_t **doff) -> idb_status {
+        if (!host_inputs) {
+            *dst = reinterpret_cast<const uint8_t *>(src);
+            *doff = off;
+            return IDB_OK;
+        }
+        const size_t nbytes = (size_t)(P.N ? off[P.N] : 0);
+        TRY(ensure(c, bid, nbytes + 16));
+        TRY(ensure(c, oid, sizeof(int64_t) * ((size_t)P.N + 1)));
+        if (nbytes) CU(cudaMemcpyAsync(c->buf[bid].p, src, nbytes, cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(c->buf[oid].p, off, sizeof(int64_t) * ((size_t)P.N + 1),
+                           cudaMemcpyHostToDevice, s));
+        *dst = ptr<uint8_t>(c, bid);
+        *doff = ptr<int64_t>(c, oid);
+        return IDB_OK;
+    };
+    if (P.no_seq) {
+        TRY(ensure(c, bSeq, 4 * (size_t)P.N + 16));
+        TRY(ensure(c, bSeqOff, sizeof(int64_t) * ((size_t)P.N + 1)));
+        launch_const_strings(ptr<uint8_t>(c, bSeq), ptr<int64_t>(c, bSeqOff), P.N, s);
+        B.seq = ptr<uint8_t>(c, bSeq);
+        B.seq_off = ptr<int64_t>(c, bSeqOff);
+    } else {
+        TRY(stage(in->seqs, in->seq_offsets, bSeq, bSeqOff, &B.seq, &B.seq_off));
+    }
+    if (!P.no_v) TRY(stage(in->v_calls, in->v_offsets, bV, bVOff, &B.vcall, &B.v_off));
+    if (!P.no_j) TRY(stage(in->j_calls, in->j_offsets, bJ, bJOff, &B.jcall, &B.j_off));
+    // repertoire offsets
+    std::vector<uint32_t> roff(P.R + 1);
+    if (in->n_repertoires > 0 && in->rep_offsets) {
+        for (uint32_t r = 0; r <= P.R; ++r) roff[r] = in->rep_offsets[r];
+    } else {
+        roff[0] = 0;
+        roff[1] = P.N;
+    }
+    TRY(ensure(c, bRepOff, sizeof(uint32_t) * (P.R + 1)));
+    CU(cudaMemcpyAsync(c->buf[bRepOff].p, roff.data(), sizeof(uint32_t) * (P.R + 1),
+                       cudaMemcpyHostToDevice, s));
+    B.rep_off = ptr<uint32_t>(c, bRepOff);
+    // gene lists
+    P.Gv = P.no_v ? 1 : in->n_v_genes;
+    P.Gj = P.no_j ? 1 : in->n_j_genes;
+    if (!P.no_v) TRY(upload_genes(c, in->v_genes, in->v_gene_offsets, P.Gv, bVGenes, bVGOff, &P.gene_bytes_v));
+    if (!P.no_j) TRY(upload_genes(c, in->j_genes, in->j_gene_offsets, P.Gj, bJGenes, bJGOff, &P.gene_bytes_j));
+    B.vgenes = ptr<uint8_t>(c, bVGenes); B.vg_off = ptr<int32_t>(c, bVGOff);
+    B.jgenes = ptr<uint8_t>(c, bJGenes); B.jg_off = ptr<int32_t>(c, bJGOff);
+    P.VW = P.Gv > 64 ? (P.Gv + 63) / 64 : 1;
+    P.JW = P.Gj > 64 ? (P.Gj + 63) / 64 : 1;
+    if (P.Gv == 0) P.Gv = 1;   // a V column with an empty reference list: all bitsets 0
+    if (P.Gj == 0) P.Gj = 1;
+    record(pl, 0);
+    launch_survey(P, B, s);
+    TRY(check_launch());
+    CU(cudaMemcpyAsync(c->h_ctr, B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    return IDB_OK;
+}
+
+// Plan constants from the survey.
+idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
+    Plan &P = pl.P;
+    const Counters &h = *pl.c->h_ctr;
+    P.hamming = prm->use_hamming != 0;
+    P.min_pts = prm->min_pts;
+    P.schedule = prm->schedule;
+    P.Lmin = P.N ? h.lmin : 0;
+    P.Lmax = P.N ? h.lmax : 0;
+    if (P.Lmin > P.Lmax) P.Lmin = P.Lmax;
+    if (P.Lmax > 65535) return fail(IDB_ERR_UNSUPPORTED, "sequences longer than 65535 bytes");
+    P.NL = P.Lmax - P.Lmin + 1;
+    // alphabet: codes = ranks of the byte values present
+    std::memset(P.codemap, 0, sizeof P.codemap);
+    uint32_t A = 0;
+    P.first_byte = -1;
+    for (int b = 0; b < 256; ++b)
+        if ((h.used[b >> 5] >> (b & 31)) & 1u) {
+            if (A == 0) P.first_byte = b;
+            P.codemap[b] = (uint8_t)A++;
+        }
+    P.A = A ? A : 1;
+    P.W = P.Lmax > 32 ? (P.Lmax + 31) / 32 : 1;
+    P.fast = P.A <= (uint32_t)kFastMaxCodes && P.Lmax <= 32u * kFastMaxWords;
+    if (!P.hamming && !P.fast && P.Lmax > (uint32_t)kGenericMaxLen)
+        return fail(IDB_ERR_UNSUPPORTED, "Levenshtein mode supports sequences up to %d bytes",
+                    kGenericMaxLen);
+    if (P.fast && P.hamming) {
+        P.B = P.A <= 4 ? 2 : 5;
+        P.RS = ((P.B * P.W * 4) + 15) & ~15u;
+    } else {
+        P.B = 8;
+        P.RS = ((P.Lmax > 0 ? P.Lmax : 1) + 15) & ~15u;
+    }
+    // unit shape
+    if (P.fast && P.hamming) {
+        P.RX = P.W == 1 ? 8 : 4;
+        P.TX = 32 * P.RX;
+        P.TY = 256;
+    } else if (P.fast) {
+        P.RX = 1;
+        P.TX = 32;
+        P.TY = 256;
+    } else {
+        P.RX = 1;
+        P.TX = 32;
+        P.TY = 256;
+    }
+    if (prm->reserved[0] > 0 && P.fast) {   // tuned shape: reserved[0] = RX, reserved[1] = TY
+        const int rx = prm->reserved[0];
+        if (P.hamming && (rx == 4 || (rx == 8 && P.W == 1))) P.RX = rx;
+        if (!P.hamming && (rx == 1 || (rx == 2 && P.W == 1))) P.RX = rx;
+        P.TX = 32 * P.RX;
+        const int ty = prm->reserved[1];
+        if (ty >= (int)P.TX && ty % (int)P.TX == 0 && ty <= 4096) P.TY = ty;
+    }
+    // eps table over the length range, and the largest admissible gap
+    pl.eps_host.assign((size_t)P.NL * P.NL, 0);
+    int dl = 0;
+    int emin_same = INT32_MAX, emax_same = INT32_MIN;
+    for (uint32_t a = 0; a < P.NL; ++a)
+        for (uint32_t b = 0; b < P.NL; ++b) {
+            int e = eps_value(P.Lmin + a, P.Lmin + b, prm->threshold, prm->abs_eps);
+            if (e > 32767) e = 32767;
+            if (e < -1) e = -1;
+            pl.eps_host[(size_t)a * P.NL + b] = (int16_t)e;
+            if (b >= a && e >= (int)(b - a) && (int)(b - a) > dl) dl = (int)(b - a);
+            if (a == b) { emin_same = std::min(emin_same, e); emax_same = std::max(emax_same, e); }
+        }
+    P.dLmax = P.hamming ? 0 : dl;
+    P.hamming_eps_mode = 0;
+    if (P.hamming && emin_same == emax_same && emin_same == 1) P.hamming_eps_mode = 1;
+    if (P.hamming && emin_same == emax_same && emin_same == 0) P.hamming_eps_mode = 2;
+    P.nbins = (uint64_t)P.R * P.Gv * P.Gj * P.NL;
+    if (P.nbins >= (1ull << 31))
+        return fail(IDB_ERR_UNSUPPORTED, "too many buckets (repertoires x V genes x J genes x lengths = %llu)",
+                    (unsigned long long)P.nbins);
+    return IDB_OK;
+}
+
+// Workspace for everything sized by N and the plan.
+idb_status alloc_fixed(Pipeline &pl) {
+    idb_context *c = pl.c;
+    Plan &P = pl.P;
+    Buffers &B = pl.B;
+    const size_t N = P.N, N1 = N + 1;
+    TRY(ensure(c, bEps, sizeof(int16_t) * pl.eps_host.size()));
+    TRY(ensure(c, bCode, 256));
+    CU(cudaMemcpyAsync(c->buf[bEps].p, pl.eps_host.data(), sizeof(int16_t) * pl.eps_host.size(),
+                       cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->buf[bCode].p, P.codemap, 256, cudaMemcpyHostToDevice, c->stream));
+    B.eps_tab = ptr<int16_t>(c, bEps);
+    B.codemap = ptr<uint8_t>(c, bCode);
+    TRY(ensure(c, bVBits, sizeof(uint64_t) * N * P.VW));
+    TRY(ensure(c, bJBits, sizeof(uint64_t) * N * P.JW));
+    TRY(ensure(c, bSlot, 4 * N));
+    TRY(ensure(c, bRepRow, 4 * N));
+    TRY(ensure(c, bFlag, 4 * N1));
+    TRY(ensure(c, bUidOfRow, 4 * N1));
+    TRY(ensure(c, bRow2Uid, 4 * N));
+    const uint64_t tcap = next_pow2(std::max<uint64_t>(2 * N, 1024));
+    TRY(ensure(c, bTable, 4 * tcap));
+    TRY(ensure(c, bTCount, 4 * tcap));
+    TRY(ensure(c, bURow, 4 * N1));
+    TRY(ensure(c, bUCopies, 4 * N1));
+    TRY(ensure(c, bULen, 4 * N1));
+    TRY(ensure(c, bURep, 4 * N1));
+    TRY(ensure(c, bBinHist, 4 * (P.nbins + 1)));
+    TRY(ensure(c, bBinCursor, 4 * (P.nbins + 1)));
+    TRY(ensure(c, bBpCount, 4 * (P.nbins + 1)));
+    TRY(ensure(c, bClsHist, 4 * 130));
+    TRY(ensure(c, bDeg, 4 * N1));
+    TRY(ensure(c, bGOff, 4 * N1));
+    TRY(ensure(c, bGCur, 4 * N1));
+    TRY(ensure(c, bCnt, 4 * N1));
+    TRY(ensure(c, bUCore, 4 * N1));
+    TRY(ensure(c, bParent, 4 * N1));
+    TRY(ensure(c, bBMin, 4 * N1));
+    TRY(ensure(c, bRootFlag, 4 * N1));
+    TRY(ensure(c, bUidFirst, 4 * (P.R + 1)));
+    TRY(ensure(c, bDepth, 4 * (kDepthMax + 1)));
+    const uint64_t scan_n = std::max<uint64_t>(N1, P.nbins + 1);
+    B.scan_part_cap = scan_part_needed(std::max<uint64_t>(scan_n, 1u << 20));
+    TRY(ensure(c, bScanPart, 4 * (size_t)B.scan_part_cap));
+    B.vbits = ptr<uint64_t>(c, bVBits); B.jbits = ptr<uint64_t>(c, bJBits);
+    B.slot = ptr<uint32_t>(c, bSlot); B.rep_row = ptr<uint32_t>(c, bRepRow);
+    B.flag = ptr<uint32_t>(c, bFlag); B.uid_of_row = ptr<uint32_t>(c, bUidOfRow);
+    B.row2uid = ptr<uint32_t>(c, bRow2Uid);
+    B.table = ptr<uint32_t>(c, bTable); B.tcount = ptr<uint32_t>(c, bTCount);
+    B.table_mask = tcap - 1;
+    B.urow = ptr<uint32_t>(c, bURow); B.ucopies = ptr<uint32_t>(c, bUCopies);
+    B.ulen = ptr<uint32_t>(c, bULen); B.urep = ptr<uint32_t>(c, bURep);
+    B.bin_hist = ptr<uint32_t>(c, bBinHist); B.bin_cursor = ptr<uint32_t>(c, bBinCursor);
+    B.bp_count = ptr<uint32_t>(c, bBpCount); B.cls_hist = ptr<uint32_t>(c, bClsHist);
+    B.deg = ptr<uint32_t>(c, bDeg); B.goff = ptr<uint32_t>(c, bGOff); B.gcur = ptr<uint32_t>(c, bGCur);
+    B.cnt = ptr<uint32_t>(c, bCnt); B.ucore = ptr<uint32_t>(c, bUCore);
+    B.parent = ptr<uint32_t>(c, bParent); B.bmin = ptr<uint32_t>(c, bBMin);
+    B.rootflag = ptr<uint32_t>(c, bRootFlag); B.uid_first = ptr<uint32_t>(c, bUidFirst);
+    B.depth_hist = ptr<uint32_t>(c, bDepth);
+    B.scan_part = ptr<uint32_t>(c, bScanPart);
+    return IDB_OK;
+}
+
+idb_status alloc_entries(Pipeline &pl, uint64_t n_entries) {
+    idb_context *c = pl.c;
+    pl.P.cap_entries = std::max<uint64_t>(n_entries, 1);
+    TRY(ensure(c, bEntUid, 4 * pl.P.cap_entries));
+    TRY(ensure(c, bEntRec, (size_t)pl.P.RS * pl.P.cap_entries));
+    pl.B.ent_uid = ptr<uint32_t>(c, bEntUid);
+    pl.B.ent_rec = ptr<uint4>(c, bEntRec);
+    return IDB_OK;
+}
+
+idb_status alloc_binpairs(Pipeline &pl, uint64_t n_bp) {
+    idb_context *c = pl.c;
+    pl.P.cap_binpairs = std::max<uint64_t>(n_bp, 1);
+    TRY(ensure(c, bBp, sizeof(BinPair) * pl.P.cap_binpairs));
+    TRY(ensure(c, bBpSorted, sizeof(BinPair) * pl.P.cap_binpairs));
+    TRY(ensure(c, bBpUnits, 4 * (pl.P.cap_binpairs + 1)));
+    TRY(ensure(c, bPred, 4 * (pl.P.cap_binpairs + 1)));
+    const uint64_t need = scan_part_needed(pl.P.cap_binpairs + 1);
+    if (need > pl.B.scan_part_cap) {
+        pl.B.scan_part_cap = (uint32_t)need;
+        TRY(ensure(c, bScanPart, 4 * (size_t)need));
+        pl.B.scan_part = ptr<uint32_t>(c, bScanPart);
+    }
+    pl.B.bp = ptr<BinPair>(c, bBp);
+    pl.B.bp_sorted = ptr<BinPair>(c, bBpSorted);
+    pl.B.bp_units = ptr<uint32_t>(c, bBpUnits);
+    pl.B.pred = ptr<float>(c, bPred);
+    return IDB_OK;
+}
+
+idb_status alloc_edges(Pipeline &pl, uint64_t cap) {
+    idb_context *c = pl.c;
+    cap = std::max<uint64_t>(cap, 4096);
+    if (cap > 0xFFFFFFF0ull) return fail(IDB_ERR_UNSUPPORTED, "more than 2^32 neighbour pairs");
+    pl.P.cap_edges = cap;
+    TRY(ensure(c, bEdges, sizeof(uint2) * cap, true));
+    TRY(ensure(c, bAdj, 2 * sizeof(uint32_t) * cap, true));
+    pl.B.edges = ptr<uint2>(c, bEdges);
+    pl.B.adj = ptr<uint32_t>(c, bAdj);
+    return IDB_OK;
+}
+
+idb_status read_counters(Pipeline &pl) {
+    CU(cudaMemcpyAsync(pl.c->h_ctr, pl.B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, pl.c->stream));
+    CU(cudaStreamSynchronize(pl.c->stream));
+    return IDB_OK;
+}
+
+idb_status device_errors(const Counters &h) {
+    if (h.error & kErrHashStall) return fail(IDB_ERR_DEVICE_STALL, "duplicate table probe gave up");
+    if (h.error & kErrUnionStall) return fail(IDB_ERR_DEVICE_STALL, "union-find retry bound reached");
+    if (h.error & (kErrAlphabet | kErrLength))
+        return fail(IDB_ERR_REPLAN, "inputs no longer match the captured plan");
+    if (h.error & (kErrEdgeOverflow | kErrUnitOverflow | kErrBinPairOverflow | kErrEntryOverflow))
+        return fail(IDB_ERR_CAPACITY, "a plan capacity was exceeded (error bits 0x%x)", h.error);
+    return IDB_OK;
+}
+
+// Phases after the survey.  With `eager`, sizes are read back and buffers grown
+// between phases; otherwise (graph capture) the capacities in P are used as-is.
+idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false) {
+    idb_context *c = pl.c;
+    Plan &P = pl.P;
+    Buffers &B = pl.B;
+    cudaStream_t s = c->stream;
+    if (!eager) launch_check_plan(P, B, s);
+    launch_gene_bits(P, B, true, s);
+    launch_gene_bits(P, B, false, s);
+    launch_dedupe(P, B, s);
+    launch_uniques(P, B, s);
+    TRY(check_launch());
+    record(pl, 1);
+    launch_buckets(P, B, s);
+    if (eager) {
+        TRY(read_counters(pl));
+        TRY(alloc_entries(pl, c->h_ctr->n_entries));
+    }
+    launch_fill(P, B, s);
+    launch_binpairs(P, B, s);
+    TRY(check_launch());
+    if (eager) {
+        TRY(read_counters(pl));
+        TRY(alloc_binpairs(pl, c->h_ctr->n_binpairs));
+    }
+    launch_binpairs_fill(P, B, s);
+    launch_schedule(P, B, s);
+    TRY(check_launch());
+    record(pl, 2);
+    if (stop_after_schedule) return IDB_OK;
+    if (eager && P.cap_edges == 0) TRY(alloc_edges(pl, std::max<uint64_t>(4ull * P.N, 1ull << 16)));
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        launch_distance(P, B, 0, s);
+        TRY(check_launch());
+        if (!eager) break;
+        TRY(read_counters(pl));
+        const Counters &h = *c->h_ctr;
+        if (!(h.error & kErrEdgeOverflow)) break;
+        // grow to the exact requirement and sweep again
+        TRY(alloc_edges(pl, (uint64_t)h.edge_reserved + 64ull * kEdgeChunk * 1024));
+        const uint32_t clear_err = h.error & ~kErrEdgeOverflow;
+        CU(cudaMemsetAsync(&B.ctr->unit_cursor, 0, 4, s));
+        CU(cudaMemsetAsync(&B.ctr->edge_reserved, 0, 4, s));
+        CU(cudaMemsetAsync(&B.ctr->n_edges, 0, 4, s));
+        CU(cudaMemsetAsync(&B.ctr->pairs_evaluated, 0, 8, s));
+        CU(cudaMemcpyAsync(&B.ctr->error, &clear_err, 4, cudaMemcpyHostToDevice, s));
+        CU(cudaStreamSynchronize(s));
+    }
+    record(pl, 3);
+    launch_graph(P, B, pl.trees, s);
+    record(pl, 4);
+    launch_outputs(P, B, s);
+    TRY(check_launch());
+    record(pl, 5);
+    return IDB_OK;
+}
+
+idb_status fill_stats(Pipeline &pl, idb_stats *st) {
+    if (!st) return IDB_OK;
+    const Counters &h = *pl.c->h_ctr;
+    std::memset(st, 0, sizeof *st);
+    st->n_uniques = h.n_uniques;
+    st->n_cores = h.n_cores;
+    st->n_clusters = h.n_clusters;
+    st->n_noise_rows = h.n_noise_rows;
+    st->pairs_evaluated = h.pairs_evaluated;
+    st->neighbour_pairs = h.n_edges;
+    st->n_entries = h.n_entries;
+    st->n_units = h.n_units;
+    if (pl.timing) {
+        float ms = 0;
+        for (int k = 0; k < 5; ++k) {
+            cudaEventElapsedTime(&ms, pl.c->ev[k], pl.c->ev[k + 1]);
+            st->ms_phase[k] = ms;
+        }
+        cudaEventElapsedTime(&ms, pl.c->ev[0], pl.c->ev[5]);
+        st->ms_total = ms;
+        st->ms_distance = st->ms_phase[2];
+    }
+    return IDB_OK;
+}
+
+idb_status cluster_impl(idb_context *c, const idb_input *in, const idb_params *prm,
+                        idb_output *out, bool host_io) {
+    TRY(validate(in, prm, out));
+    CU(cudaSetDevice(c->device));
+    Pipeline pl;
+    pl.c = c;
+    pl.trees = prm->eval_trees != 0 && out->tree_depth_hist != nullptr;
+    pl.timing = out->stats != nullptr;
+    if (in->n_rows == 0) {
+        if (out->n_uniques) *out->n_uniques = 0;
+        if (out->stats) std::memset(out->stats, 0, sizeof *out->stats);
+        return IDB_OK;
+    }
+    TRY(stage_inputs_and_survey(pl, in, host_io));
+    TRY(derive_plan(pl, prm));
+    TRY(alloc_fixed(pl));
+    Buffers &B = pl.B;
+    const size_t N = pl.P.N;
+    if (host_io) {
+        TRY(ensure(c, bClone, 4 * N));
+        TRY(ensure(c, bCore, 4 * N));
+        TRY(ensure(c, bCopies, 4 * N));
+        B.clone_id = ptr<uint32_t>(c, bClone);
+        B.core = ptr<int32_t>(c, bCore);
+        B.copies = ptr<uint32_t>(c, bCopies);
+        if (out->uniques) {
+            TRY(ensure(c, bUniques, 4 * N));
+            B.uniques = ptr<uint32_t>(c, bUniques);
+        }
+    } else {
+        B.clone_id = out->clone_id;
+        B.core = out->core;
+        B.copies = out->copies;
+        B.uniques = out->uniques;
+    }
+    TRY(run_phases(pl, true));
+    cudaStream_t s = c->stream;
+    if (host_io) {
+        CU(cudaMemcpyAsync(out->clone_id, B.clone_id, 4 * N, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(out->core, B.core, 4 * N, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(out->copies, B.copies, 4 * N, cudaMemcpyDeviceToHost, s));
+    }
+    CU(cudaMemcpyAsync(c->h_ctr, B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    std::vector<uint32_t> hist(kDepthMax + 1);
+    if (pl.trees)
+        CU(cudaMemcpyAsync(hist.data(), B.depth_hist, 4 * (kDepthMax + 1), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    TRY(device_errors(*c->h_ctr));
+    const uint32_t nu = c->h_ctr->n_uniques;
+    if (out->uniques) {
+        if (host_io)
+            CU(cudaMemcpy(out->uniques, B.uniques, 4 * (size_t)nu, cudaMemcpyDeviceToHost));
+    }
+    if (out->n_uniques) {
+        if (host_io) *out->n_uniques = nu;
+        else CU(cudaMemcpy(out->n_uniques, &nu, 4, cudaMemcpyHostToDevice));
+    }
+    if (pl.trees) std::memcpy(out->tree_depth_hist, hist.data(), 4 * (kDepthMax + 1));
+    TRY(fill_stats(pl, out->stats));
+    return IDB_OK;
+}
+
+thread_local idb_context *t_default_ctx = nullptr;
+
+idb_status get_ctx(idb_context **pc) {
+    if (*pc) return IDB_OK;
+    if (!t_default_ctx) TRY(idb_context_create(0, &t_default_ctx));
+    *pc = t_default_ctx;
+    return IDB_OK;
+}
+
+}  // namespace
+
+namespace idb {
+int sm_count() {
+    static thread_local int dev = -1, n = 0;
+    int d = 0;
+    cudaGetDevice(&d);
+    if (d != dev) {
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, d);
+        if (n <= 0) n = 1;
+        dev = d;
+    }
+    return n;
+}
+}  // namespace idb
+
+// ============================================================================
+// C ABI
+// ============================================================================
+extern "C" {
+
+int idb_abi_version(void) { return IDB_ABI_VERSION; }
+
+const char *idb_status_string(idb_status s) {
+    switch (s) {
+        case IDB_OK: return "ok";
+        case IDB_ERR_INVALID_ARG: return "invalid argument";
+        case IDB_ERR_CUDA: return "CUDA error";
+        case IDB_ERR_NO_DEVICE: return "no usable CUDA device";
+        case IDB_ERR_UNSUPPORTED: return "unsupported input";
+        case IDB_ERR_OUT_OF_MEMORY: return "out of device memory";
+        case IDB_ERR_CAPACITY: return "plan capacity exceeded";
+        case IDB_ERR_DEVICE_STALL: return "bounded device wait gave up";
+        case IDB_ERR_REPLAN: return "inputs no longer match the plan";
+    }
+    return "unknown status";
+}
+
+size_t idb_last_error(char *buf, size_t size) {
+    if (buf && size) {
+        std::snprintf(buf, size, "%s", g_err.c_str());
+    }
+    return g_err.size();
+}
+
+idb_status idb_context_create(int device, idb_context **out) {
+    if (!out) return fail(IDB_ERR_INVALID_ARG, "NULL context pointer");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(IDB_ERR_NO_DEVICE, "no CUDA device");
+    }
+    if (device < 0 || device >= n) return fail(IDB_ERR_NO_DEVICE, "device %d not present", device);
+    cudaDeviceProp prop;
+    CU(cudaGetDeviceProperties(&prop, device));
+    if (prop.major * 10 + prop.minor < 100)
+        return fail(IDB_ERR_NO_DEVICE, "device %d is sm_%d%d; this library targets sm_103", device,
+                    prop.major, prop.minor);
+    CU(cudaSetDevice(device));
+    idb_context *c = new idb_context();
+    c->device = device;
+    CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CU(cudaMallocHost(&c->h_ctr, sizeof(Counters)));
+    for (auto &e : c->ev) CU(cudaEventCreate(&e));
+    *out = c;
+    return IDB_OK;
+}
+
+idb_status idb_context_destroy(idb_context *c) {
+    if (!c) return IDB_OK;
+    cudaSetDevice(c->device);
+    if (c->exec) cudaGraphExecDestroy(c->exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    for (auto &b : c->buf)
+        if (b.p) cudaFree(b.p);
+    for (auto &e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->h_ctr) cudaFreeHost(c->h_ctr);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    if (c == t_default_ctx) t_default_ctx = nullptr;
+    delete c;
+    return IDB_OK;
+}
+
+idb_status idb_cluster(idb_context *ctx, const idb_input *in, const idb_params *prm,
+                       idb_output *out) {
+    TRY(get_ctx(&ctx));
+    return cluster_impl(ctx, in, prm, out, true);
+}
+
+idb_status idb_cluster_device(idb_context *ctx, const idb_input *in, const idb_params *prm,
+                              idb_output *out) {
+    TRY(get_ctx(&ctx));
+    return cluster_impl(ctx, in, prm, out, false);
+}
+
+idb_status idb_batch_plan(idb_context *c, const idb_input *in, const idb_params *prm,
+                          const idb_output *out) {
+    if (!c) return fail(IDB_ERR_INVALID_ARG, "idb_batch_plan needs an explicit context");
+    TRY(validate(in, prm, out));
+    if (in->n_rows == 0) return fail(IDB_ERR_INVALID_ARG, "empty input");
+    CU(cudaSetDevice(c->device));
+    if (c->exec) { cudaGraphExecDestroy(c->exec); c->exec = nullptr; }
+    if (c->graph) { cudaGraphDestroy(c->graph); c->graph = nullptr; }
+    c->planned = false;
+    // 1. discovery run (eager) to learn the sizes
+    idb_output o = *out;
+    o.stats = nullptr;
+    o.tree_depth_hist = nullptr;
+    o.n_uniques = nullptr;
+    Pipeline pl;
+    pl.c = c;
+    pl.trees = false;
+    TRY(stage_inputs_and_survey(pl, in, false));
+    TRY(derive_plan(pl, prm));
+    TRY(alloc_fixed(pl));
+    pl.B.clone_id = o.clone_id;
+    pl.B.core = o.core;
+    pl.B.copies = o.copies;
+    pl.B.uniques = o.uniques;
+    TRY(run_phases(pl, true));
+    TRY(read_counters(pl));
+    TRY(device_errors(*c->h_ctr));
+    // 2. capacities with headroom; the buffers keep their addresses from here on
+    const Counters h = *c->h_ctr;
+    TRY(alloc_entries(pl, (uint64_t)h.n_entries + h.n_entries / 16 + 1024));
+    TRY(alloc_binpairs(pl, (uint64_t)h.n_binpairs + h.n_binpairs / 16 + 1024));
+    TRY(alloc_edges(pl, (uint64_t)h.edge_reserved + h.edge_reserved / 8 + 64ull * kEdgeChunk * 1024));
+    // 3. capture the complete launch sequence
+    cudaStream_t s = c->stream;
+    CU(cudaStreamSynchronize(s));
+    CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(pl.B.ctr, 0, sizeof(Counters), s);
+    cudaMemsetAsync(&pl.B.ctr->lmin, 0xFF, sizeof(uint32_t), s);
+    launch_survey(pl.P, pl.B, s);
+    pl.timing = true;   // event-record nodes between the phases
+    idb_status st = run_phases(pl, false);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (st != IDB_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (ce != cudaSuccess) return fail(IDB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    c->graph = g;
+    CU(cudaGraphInstantiate(&c->exec, g, 0));
+    {
+        size_t nn = 0;
+        CU(cudaGraphGetNodes(g, nullptr, &nn));
+        std::vector<cudaGraphNode_t> nodes(nn);
+        CU(cudaGraphGetNodes(g, nodes.data(), &nn));
+        uint32_t k = 0;
+        for (auto nd : nodes) {
+            cudaGraphNodeType t;
+            CU(cudaGraphNodeGetType(nd, &t));
+            k += t == cudaGraphNodeTypeKernel;
+        }
+        c->graph_kernels = k;
+    }
+    c->plan = pl.P;
+    c->bufs = pl.B;
+    c->out_dev = o;
+    c->planned = true;
+    return IDB_OK;
+}
+
+idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
+    if (!c || !c->planned) return fail(IDB_ERR_INVALID_ARG, "no batch plan");
+    CU(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    CU(cudaEventRecord(c->ev[0], s));
+    CU(cudaGraphLaunch(c->exec, s));
+    CU(cudaEventRecord(c->ev[6], s));
+    CU(cudaMemcpyAsync(c->h_ctr, c->bufs.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    TRY(device_errors(*c->h_ctr));
+    if (stats) {
+        const Counters &h = *c->h_ctr;
+        std::memset(stats, 0, sizeof *stats);
+        stats->n_uniques = h.n_uniques;
+        stats->n_cores = h.n_cores;
+        stats->n_clusters = h.n_clusters;
+        stats->n_noise_rows = h.n_noise_rows;
+        stats->pairs_evaluated = h.pairs_evaluated;
+        stats->neighbour_pairs = h.n_edges;
+        stats->n_entries = h.n_entries;
+        stats->n_units = h.n_units;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev[0], c->ev[6]);
+        stats->ms_total = ms;
+        for (int k = 0; k < 5; ++k) {
+            cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]);
+            stats->ms_phase[k] = ms;
+        }
+        stats->ms_distance = stats->ms_phase[2];
+        stats->kernel_launches = c->graph_kernels;
+    }
+    return IDB_OK;
+}
+
+idb_status idb_count_admissible(idb_context *c, const idb_input *in, const idb_params *prm,
+                                uint64_t *pairs_out) {
+    TRY(get_ctx(&c));
+    if (!pairs_out) return fail(IDB_ERR_INVALID_ARG, "NULL output");
+    uint32_t dummy = 0;
+    idb_output o{};
+    o.clone_id = &dummy; o.core = reinterpret_cast<int32_t *>(&dummy); o.copies = &dummy;
+    TRY(validate(in, prm, &o));
+    *pairs_out = 0;
+    if (in->n_rows == 0) return IDB_OK;
+    CU(cudaSetDevice(c->device));
+    Pipeline pl;
+    pl.c = c;
+    TRY(stage_inputs_and_survey(pl, in, true));
+    TRY(derive_plan(pl, prm));
+    TRY(alloc_fixed(pl));
+    TRY(run_phases(pl, true, true));
+    launch_count_admissible(pl.P, pl.B, c->stream);
+    TRY(check_launch());
+    TRY(read_counters(pl));
+    TRY(device_errors(*c->h_ctr));
+    *pairs_out = c->h_ctr->admissible_pairs;
+    return IDB_OK;
+}
+
+}  // extern "C"

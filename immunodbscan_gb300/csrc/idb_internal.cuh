@@ -1,0 +1,176 @@
+// idb_internal.cuh -- device data layout, plan constants and kernel launchers
+// shared by the translation units of libimmunodbscan_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bitops.cuh"
+
+namespace idb {
+
+constexpr uint32_t kNone = 0xFFFFFFFFu;
+constexpr int kMaxGeneWords = 8;        // 512 reference genes per gene column
+constexpr int kFastMaxCodes = 32;       // alphabet of the fast (bit-plane) path
+constexpr int kFastMaxWords = 4;        // 128 residues on the fast path
+constexpr int kGenericMaxLen = 1024;    // Levenshtein on the generic path
+constexpr int kDepthMax = 50;           // tree-depth histogram cap (cuda/PSDBSCAN.hcu:1029)
+constexpr uint32_t kEdgeChunk = 256;    // edge slots reserved per warp at a time
+constexpr uint32_t kSpinCap = 1u << 22; // bound of every device-side retry loop
+
+// error bits raised by kernels (Counters::error)
+enum : uint32_t {
+    kErrHashStall = 1u,       // duplicate-table probe exceeded its bound
+    kErrUnionStall = 2u,      // union-find retry exceeded its bound
+    kErrEdgeOverflow = 4u,    // edge buffer too small (count still exact)
+    kErrUnitOverflow = 8u,    // work-unit list exceeded its capacity
+    kErrAlphabet = 16u,       // a byte outside the plan's code map
+    kErrLength = 32u,         // a length outside the plan's range
+    kErrBinPairOverflow = 64u,
+    kErrEntryOverflow = 128u,
+};
+
+// Device-resident counters of one clustering call (one struct, zeroed first).
+struct Counters {
+    uint32_t lmax, lmin;
+    uint32_t used[8];            // 256-bit byte-presence map of the sequences
+    uint32_t n_uniques;
+    uint32_t n_entries;
+    uint32_t n_binpairs;
+    uint32_t n_units;
+    uint32_t unit_cursor;        // persistent work queue head
+    uint32_t edge_reserved;      // edge slots handed out (chunks)
+    uint32_t n_edges;            // real edges written
+    uint32_t n_cores;
+    uint32_t n_clusters;
+    uint32_t n_noise_rows;
+    uint32_t error;
+    uint32_t heavy_count;
+    unsigned long long pairs_evaluated;
+    unsigned long long admissible_pairs;
+    uint32_t pad[4];
+};
+
+// One bucket ("bin") holds the uniques of one (repertoire, V gene, J gene,
+// length); a unique with V/J ambiguity sets sits in |V|*|J| bins.  Two uniques
+// are V- and J-compatible iff they share a bin, and each compatible pair is
+// evaluated in exactly one bin: its lowest common V gene and lowest common J
+// gene (checked when a pair is a neighbour).
+struct BinPair {
+    uint32_t a_start, a_n;      // x entries [a_start, a_start+a_n)
+    uint32_t b_start, b_n;      // y entries
+    uint32_t unit_base;         // first work unit (exclusive scan, schedule order)
+    uint32_t ncx;               // x chunks
+    uint16_t la, lb;            // lengths of the two bins
+    uint16_t v, j;              // the bins' V gene and J gene
+    int16_t eps;                // neighbour threshold of the length pair
+    uint8_t same;               // 1: a and b are the same bin (triangular units)
+    uint8_t cls;                // schedule class
+    uint32_t cost_lo;           // predicted cost (pairs or learned), low 32 bits
+};
+static_assert(sizeof(BinPair) == 40, "BinPair layout");
+
+// Host-side plan of one call (everything the kernels need as constants).
+struct Plan {
+    uint32_t N = 0, R = 1;
+    uint32_t Gv = 1, Gj = 1, VW = 1, JW = 1;     // genes and uint64 words per column
+    uint32_t gene_bytes_v = 0, gene_bytes_j = 0; // bytes of the reference name lists
+    bool no_v = true, no_j = true, no_seq = false;
+    bool hamming = false;
+    uint32_t min_pts = 2;
+    uint32_t Lmin = 0, Lmax = 0, NL = 1;
+    uint32_t A = 1, B = 1, W = 1;                 // codes, bit planes, 32-bit words
+    bool fast = true;
+    uint32_t RS = 16;                             // record bytes per entry
+    int dLmax = 0;                                // largest admissible length gap
+    uint64_t nbins = 0;
+    uint32_t TX = 256, TY = 256, RX = 8;          // unit shape (entries)
+    int schedule = 0;
+    int hamming_eps_mode = 0;                     // 0 popcount, 1 eps==1, 2 eps==0
+    uint8_t codemap[256];
+    int first_byte = -1;                          // byte value with code 0
+    // capacities
+    uint64_t cap_entries = 0, cap_binpairs = 0, cap_units = 0, cap_edges = 0;
+};
+
+// Device buffers of one call (all carved from the context arena).
+struct Buffers {
+    // inputs (device)
+    const uint8_t *seq = nullptr;  const int64_t *seq_off = nullptr;
+    const uint8_t *vcall = nullptr; const int64_t *v_off = nullptr;
+    const uint8_t *jcall = nullptr; const int64_t *j_off = nullptr;
+    const uint8_t *vgenes = nullptr; const int32_t *vg_off = nullptr;
+    const uint8_t *jgenes = nullptr; const int32_t *jg_off = nullptr;
+    const uint32_t *rep_off = nullptr;              // [R+1]
+    const int16_t *eps_tab = nullptr;               // [NL*NL]
+    const uint8_t *codemap = nullptr;               // [256]
+    // row level [N]
+    uint64_t *vbits = nullptr, *jbits = nullptr;    // [N*VW], [N*JW]
+    uint64_t *rhash = nullptr;
+    uint32_t *slot = nullptr, *rep_row = nullptr, *flag = nullptr, *uid_of_row = nullptr;
+    uint32_t *row2uid = nullptr;
+    // duplicate table
+    uint32_t *table = nullptr, *tcount = nullptr;
+    uint64_t table_mask = 0;
+    // uniques [N]
+    uint32_t *urow = nullptr, *ucopies = nullptr, *ulen = nullptr, *urep = nullptr;
+    // bins
+    uint32_t *bin_hist = nullptr;                   // [nbins+1] -> bin_start
+    uint32_t *bin_cursor = nullptr;                 // [nbins]
+    uint32_t *ent_uid = nullptr;                    // [cap_entries]
+    uint4 *ent_rec = nullptr;                       // [cap_entries * RS/16]
+    uint32_t *bp_count = nullptr;                   // [nbins+1]
+    BinPair *bp = nullptr, *bp_sorted = nullptr;    // [cap_binpairs]
+    uint32_t *bp_units = nullptr;                   // [cap_binpairs+1]
+    uint32_t *cls_hist = nullptr;                   // [65]
+    float *pred = nullptr;                          // learned cost per bin pair
+    // graph
+    uint2 *edges = nullptr;                         // [cap_edges]
+    uint32_t *deg = nullptr;                        // [N+1] degrees
+    uint32_t *goff = nullptr;                       // [N+1] CSR offsets
+    uint32_t *gcur = nullptr;                       // [N+1] fill cursors
+    uint32_t *adj = nullptr;                        // [2*cap_edges]
+    uint32_t *cnt = nullptr;                        // [N] neighbour copies count
+    uint32_t *ucore = nullptr;                      // [N]
+    uint32_t *parent = nullptr;                     // [N]
+    uint32_t *bmin = nullptr;                       // [N]
+    uint32_t *rootflag = nullptr;                   // [N+1] -> rank
+    uint32_t *uid_first = nullptr;                  // [R+1]
+    uint32_t *depth_hist = nullptr;                 // [kDepthMax+1]
+    // scan scratch
+    uint32_t *scan_part = nullptr;                  // [scan_part_cap]
+    uint32_t scan_part_cap = 0;
+    // outputs (device)
+    uint32_t *clone_id = nullptr;
+    int32_t *core = nullptr;
+    uint32_t *copies = nullptr;
+    uint32_t *uniques = nullptr;
+    Counters *ctr = nullptr;
+    // per bin-pair timing log (optional)
+    unsigned long long *bp_cycles = nullptr;
+    uint32_t *bp_hits = nullptr;
+};
+
+// ---- launchers (each enqueues on `s`, never synchronises) ----
+void launch_survey(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_check_plan(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream_t s);
+void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_schedule(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s);
+void launch_count_admissible(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s);
+void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s);
+
+// exclusive scan of n (host) or *n_dev (device, capacity n) uint32 values;
+// out may alias in; *total (device) receives the sum when non-null.
+void scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, const uint32_t *n_dev,
+              uint32_t *total, uint32_t *part, uint32_t part_cap, cudaStream_t s);
+uint32_t scan_part_needed(uint64_t n);
+
+int sm_count();
+const char *distance_variant_name(const Plan &P);
+
+}  // namespace idb

@@ -1,0 +1,331 @@
+// k_buckets.cu -- bucketing of the uniques and the work list of the distance
+// kernel.
+//
+// The reference compares every pair of uniques (an n_u x n_u block grid,
+// cuda/PSDBSCAN.hcu:1115-1178, and n_cores x n_u at :1200-1257) and tests V/J
+// compatibility and the length gap inside each pair (:785-788).  Here the
+// uniques are first placed in bins keyed by (repertoire, V gene, J gene,
+// length); a unique with ambiguous calls sits in |V|*|J| bins.  Two uniques are
+// V- and J-compatible (both bitset intersections non-empty,
+// cuda/BitsetVector.inl:214-237) iff they share a bin, so only pairs inside a
+// bin, or between the bins of one (repertoire, V, J) whose lengths are within
+// the threshold, are ever evaluated.  Bins are laid out densely with the length
+// fastest, so the partner bin of length L+g is the bin index + g.
+#include "idb_internal.cuh"
+
+namespace idb {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int grid_for(uint64_t n, int threads = kThreads) {
+    uint64_t g = (n + threads - 1) / threads;
+    uint64_t cap = (uint64_t)sm_count() * 8;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+struct BinGeom {
+    uint32_t Gv, Gj, NL, Lmin, VW, JW;
+    __device__ __forceinline__ bool in_range(uint32_t L) const { return L >= Lmin && L - Lmin < NL; }
+    __device__ __forceinline__ uint32_t bin(uint32_t r, uint32_t v, uint32_t j, uint32_t L) const {
+        return ((r * Gv + v) * Gj + j) * NL + (L - Lmin);
+    }
+};
+
+// Entries per unique: |V bits| * |J bits|, one histogram increment per entry.
+__global__ void k_bin_hist(BinGeom g, const Counters *__restrict__ ctr,
+                           const uint32_t *__restrict__ urow, const uint32_t *__restrict__ ulen,
+                           const uint32_t *__restrict__ urep, const uint64_t *__restrict__ vbits,
+                           const uint64_t *__restrict__ jbits, uint32_t *__restrict__ hist) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t row = urow[u], L = ulen[u], r = urep[u];
+        if (!g.in_range(L)) continue;   // only after a replay on changed data (flagged)
+        for (uint32_t vw = 0; vw < g.VW; ++vw) {
+            uint64_t vb = vbits[(size_t)row * g.VW + vw];
+            while (vb) {
+                const uint32_t v = vw * 64 + lowest_bit64(vb);
+                vb &= vb - 1;
+                if (v >= g.Gv) break;
+                for (uint32_t jw = 0; jw < g.JW; ++jw) {
+                    uint64_t jb = jbits[(size_t)row * g.JW + jw];
+                    while (jb) {
+                        const uint32_t j = jw * 64 + lowest_bit64(jb);
+                        jb &= jb - 1;
+                        if (j >= g.Gj) break;
+                        atomicAdd(&hist[g.bin(r, v, j, L)], 1u);
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Record of one unique.
+//  planes (Hamming, fast path): Bp bit planes x W words; bit i of word
+//    p*W + i/32 is bit p of the code of residue i.  Hamming distance of two
+//    records = sum over words of popc(OR_p (x_p ^ y_p)).
+//  codes (Levenshtein and generic path): one code byte per residue.
+// Codes are a bijection of the byte values present, so equality of codes is
+// equality of bytes.
+__global__ void k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
+                           const uint32_t *__restrict__ urow, const uint32_t *__restrict__ ulen,
+                           const uint32_t *__restrict__ urep, const uint64_t *__restrict__ vbits,
+                           const uint64_t *__restrict__ jbits, const uint8_t *__restrict__ seq,
+                           const int64_t *__restrict__ seq_off, const uint8_t *__restrict__ codemap,
+                           const uint32_t *__restrict__ bin_start, uint32_t *__restrict__ cursor,
+                           uint32_t *__restrict__ ent_uid, uint4 *__restrict__ ent_rec,
+                           uint32_t rs16, int planes, uint32_t W, uint64_t cap_entries,
+                           uint32_t *err) {
+    __shared__ uint8_t cm[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
+    __syncthreads();
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t row = urow[u], L = ulen[u], r = urep[u];
+        if (!g.in_range(L)) continue;
+        const uint8_t *s = seq + seq_off[row];
+        for (uint32_t vw = 0; vw < g.VW; ++vw) {
+            uint64_t vb = vbits[(size_t)row * g.VW + vw];
+            while (vb) {
+                const uint32_t v = vw * 64 + lowest_bit64(vb);
+                vb &= vb - 1;
+                if (v >= g.Gv) break;
+                for (uint32_t jw = 0; jw < g.JW; ++jw) {
+                    uint64_t jb = jbits[(size_t)row * g.JW + jw];
+                    while (jb) {
+                        const uint32_t j = jw * 64 + lowest_bit64(jb);
+                        jb &= jb - 1;
+                        if (j >= g.Gj) break;
+                        const uint32_t b = g.bin(r, v, j, L);
+                        const uint64_t pos = (uint64_t)bin_start[b] + atomicAdd(&cursor[b], 1u);
+                        if (pos >= cap_entries) { atomicOr(err, kErrEntryOverflow); continue; }
+                        ent_uid[pos] = u;
+                        uint4 *dst = ent_rec + pos * rs16;
+                        if (planes > 0) {
+                            // bit planes, written word by word (16 bytes at a time)
+                            for (uint32_t q = 0; q < rs16; ++q) {
+                                uint32_t wv[4];
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) {
+                                    const uint32_t widx = q * 4 + e;
+                                    const uint32_t p = widx / W, w = widx % W;
+                                    uint32_t acc = 0;
+                                    if (p < (uint32_t)planes) {
+                                        const uint32_t i0 = w * 32;
+                                        const uint32_t i1 = min(L, i0 + 32);
+                                        for (uint32_t i = i0; i < i1; ++i)
+                                            acc |= ((uint32_t)(cm[s[i]] >> p) & 1u) << (i - i0);
+                                    }
+                                    wv[e] = acc;
+                                }
+                                dst[q] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+                            }
+                        } else {
+                            for (uint32_t q = 0; q < rs16; ++q) {
+                                uint32_t wv[4];
+#pragma unroll
+                                for (int e = 0; e < 4; ++e) {
+                                    uint32_t acc = 0;
+#pragma unroll
+                                    for (int t = 0; t < 4; ++t) {
+                                        const uint32_t i = q * 16 + e * 4 + t;
+                                        const uint32_t c = i < L ? cm[s[i]] : 0u;
+                                        acc |= c << (8 * t);
+                                    }
+                                    wv[e] = acc;
+                                }
+                                dst[q] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+    }
+}
+
+// Bin pairs: (bin, bin+g) for every admissible length gap g (eps(L,L+g) >= g;
+// Hamming compares equal lengths only, cuda/PSDBSCAN.hcu:615).
+struct PairGeom {
+    uint32_t NL, Lmin, Gv, Gj;
+    int dLmax;
+    bool hamming;
+    uint32_t TX, TY, q;
+};
+
+__device__ __forceinline__ bool pair_ok(const PairGeom &pg, const int16_t *eps_tab, uint32_t li,
+                                        int gap) {
+    if (li + gap >= pg.NL) return false;
+    if (pg.hamming && gap != 0) return false;
+    const int e = eps_tab[(size_t)li * pg.NL + li + gap];
+    return e >= gap;
+}
+
+__global__ void k_binpairs_count(uint32_t nbins, PairGeom pg, const int16_t *__restrict__ eps_tab,
+                                 const uint32_t *__restrict__ bin_start, uint32_t *__restrict__ cnt) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += stride) {
+        const uint32_t nA = bin_start[b + 1] - bin_start[b];
+        uint32_t c = 0;
+        if (nA > 0) {
+            const uint32_t li = b % pg.NL;
+            for (int g = 0; g <= pg.dLmax; ++g) {
+                if (!pair_ok(pg, eps_tab, li, g)) continue;
+                const uint32_t nB = bin_start[b + g + 1] - bin_start[b + g];
+                if (nB == 0) continue;
+                if (g == 0 && nA < 2) continue;
+                ++c;
+            }
+        }
+        cnt[b] = c;
+    }
+}
+
+__global__ void k_binpairs_fill(uint32_t nbins, PairGeom pg, const int16_t *__restrict__ eps_tab,
+                                const uint32_t *__restrict__ bin_start,
+                                const uint32_t *__restrict__ bp_off, uint64_t cap_bp,
+                                BinPair *__restrict__ out, uint32_t *err) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += stride) {
+        const uint32_t a0 = bin_start[b], nA = bin_start[b + 1] - a0;
+        if (nA == 0) continue;
+        uint32_t k = bp_off[b];
+        const uint32_t li = b % pg.NL;
+        const uint32_t rest = b / pg.NL;
+        const uint32_t j = rest % pg.Gj, v = (rest / pg.Gj) % pg.Gv;
+        for (int g = 0; g <= pg.dLmax; ++g) {
+            if (!pair_ok(pg, eps_tab, li, g)) continue;
+            const uint32_t b0 = bin_start[b + g], nB = bin_start[b + g + 1] - b0;
+            if (nB == 0) continue;
+            if (g == 0 && nA < 2) continue;
+            if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); ++k; continue; }
+            BinPair P;
+            P.a_start = a0; P.a_n = nA; P.b_start = b0; P.b_n = nB;
+            P.unit_base = 0;
+            P.ncx = (nA + pg.TX - 1) / pg.TX;
+            P.la = (uint16_t)(pg.Lmin + li); P.lb = (uint16_t)(pg.Lmin + li + g);
+            P.v = (uint16_t)v; P.j = (uint16_t)j;
+            P.eps = eps_tab[(size_t)li * pg.NL + li + g];
+            P.same = g == 0;
+            const uint64_t cost = g == 0 ? (uint64_t)nA * (nA - 1) / 2 : (uint64_t)nA * nB;
+            P.cls = (uint8_t)(cost ? 63 - __clzll((long long)cost) : 0);
+            P.cost_lo = (uint32_t)min(cost, (uint64_t)0xFFFFFFFFu);
+            out[k++] = P;
+        }
+    }
+}
+
+// Schedule: heavy bin pairs first (counting sort on log2 of the cost, cost =
+// pairs for the static schedule or the predicted cost for the learned one).
+__global__ void k_cls_hist(const Counters *__restrict__ ctr, const BinPair *__restrict__ bp,
+                           const float *__restrict__ pred, uint32_t *__restrict__ hist) {
+    __shared__ uint32_t h[64];
+    if (threadIdx.x < 64) h[threadIdx.x] = 0;
+    __syncthreads();
+    const uint32_t n = ctr->n_binpairs;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        uint32_t cls = bp[i].cls;
+        if (pred) {
+            const float c = fmaxf(pred[i], 1.0f);
+            cls = min(63u, (uint32_t)(log2f(c) * 2.0f));
+        }
+        atomicAdd(&h[63 - cls], 1u);
+    }
+    __syncthreads();
+    if (threadIdx.x < 64 && h[threadIdx.x]) atomicAdd(&hist[threadIdx.x], h[threadIdx.x]);
+}
+
+__global__ void k_cls_scatter(const Counters *__restrict__ ctr, const BinPair *__restrict__ bp,
+                              const float *__restrict__ pred, const uint32_t *__restrict__ start,
+                              uint32_t *__restrict__ cursor, BinPair *__restrict__ out,
+                              uint32_t *__restrict__ units, uint32_t TX, uint32_t TY, uint32_t q) {
+    const uint32_t n = ctr->n_binpairs;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        BinPair P = bp[i];
+        uint32_t cls = P.cls;
+        if (pred) {
+            const float c = fmaxf(pred[i], 1.0f);
+            cls = min(63u, (uint32_t)(log2f(c) * 2.0f));
+        }
+        const uint32_t pos = start[63 - cls] + atomicAdd(&cursor[63 - cls], 1u);
+        P.cls = (uint8_t)cls;
+        out[pos] = P;
+        uint64_t nu;
+        if (P.same) {
+            const uint32_t ncy = (P.a_n + TY - 1) / TY;
+            nu = tri_units(P.ncx, ncy, q);
+        } else {
+            const uint32_t ncy = (P.b_n + TY - 1) / TY;
+            nu = (uint64_t)P.ncx * ncy;
+        }
+        units[pos] = (uint32_t)nu;
+    }
+}
+
+__global__ void k_set_unit_base(const Counters *__restrict__ ctr, BinPair *__restrict__ bp,
+                                const uint32_t *__restrict__ base) {
+    const uint32_t n = ctr->n_binpairs;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride)
+        bp[i].unit_base = base[i];
+}
+
+}  // namespace
+
+void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
+    BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW};
+    const uint32_t nb = (uint32_t)P.nbins;
+    cudaMemsetAsync(B.bin_hist, 0, sizeof(uint32_t) * (P.nbins + 1), s);
+    k_bin_hist<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.vbits,
+                                                    B.jbits, B.bin_hist);
+    scan_u32(B.bin_hist, B.bin_hist, nb + 1, nullptr, &B.ctr->n_entries, B.scan_part,
+             B.scan_part_cap, s);
+}
+
+void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
+    BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW};
+    cudaMemsetAsync(B.bin_cursor, 0, sizeof(uint32_t) * P.nbins, s);
+    const int planes = (P.fast && P.hamming) ? (int)P.B : 0;
+    k_bin_fill<<<grid_for(P.N), kThreads, 0, s>>>(
+        g, B.ctr, B.urow, B.ulen, B.urep, B.vbits, B.jbits, B.seq, B.seq_off, B.codemap,
+        B.bin_hist, B.bin_cursor, B.ent_uid, B.ent_rec, P.RS / 16, planes, P.W, P.cap_entries,
+        &B.ctr->error);
+}
+
+void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s) {
+    PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
+    const uint32_t nb = (uint32_t)P.nbins;
+    k_binpairs_count<<<grid_for(nb), kThreads, 0, s>>>(nb, pg, B.eps_tab, B.bin_hist, B.bp_count);
+    scan_u32(B.bp_count, B.bp_count, nb, nullptr, &B.ctr->n_binpairs, B.scan_part,
+             B.scan_part_cap, s);
+}
+
+void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
+    PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
+    const uint32_t nb = (uint32_t)P.nbins;
+    k_binpairs_fill<<<grid_for(nb), kThreads, 0, s>>>(nb, pg, B.eps_tab, B.bin_hist, B.bp_count,
+                                                       P.cap_binpairs, B.bp, &B.ctr->error);
+}
+
+void launch_schedule(const Plan &P, const Buffers &B, cudaStream_t s) {
+    const uint32_t q = P.TY / P.TX;
+    const float *pred = P.schedule == 1 ? B.pred : nullptr;
+    cudaMemsetAsync(B.cls_hist, 0, sizeof(uint32_t) * 130, s);
+    k_cls_hist<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(B.ctr, B.bp, pred, B.cls_hist);
+    scan_u32(B.cls_hist, B.cls_hist, 64, nullptr, nullptr, B.scan_part, B.scan_part_cap, s);
+    k_cls_scatter<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(
+        B.ctr, B.bp, pred, B.cls_hist, B.cls_hist + 64, B.bp_sorted, B.bp_units, P.TX, P.TY, q);
+    scan_u32(B.bp_units, B.bp_units, (uint32_t)P.cap_binpairs, &B.ctr->n_binpairs,
+             &B.ctr->n_units, B.scan_part, B.scan_part_cap, s);
+    k_set_unit_base<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(B.ctr, B.bp_sorted, B.bp_units);
+}
+
+}  // namespace idb

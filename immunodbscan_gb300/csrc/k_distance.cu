@@ -1,0 +1,602 @@
+// k_distance.cu -- the neighbour search (rule S4), one persistent launch.
+//
+// Reference: half_core_points / half_hamming_core_points
+// (cuda/PSDBSCAN.hcu:585-657, 751-833) and their second sweep fuse_clusters /
+// fuse_hamming_clusters (:664-742, 840-931).  The reference runs one block per
+// pair with an anti-diagonal DP and a __syncthreads per diagonal, twice.  Here
+// the distance work is done once: every neighbour pair becomes an edge of the
+// neighbour graph, and core marking and cluster growth run on that graph.
+//
+// Work decomposition
+//  * A work unit is an x-chunk of TX = 32*RX entries of bin A against a y-chunk
+//    of TY entries of bin B (B = A for a same-bin pair; then only pairs with
+//    y after x in the bin are kept).  Units are numbered in schedule order (heavy
+//    bin pairs first) and handed out by an atomic queue; each warp owns a unit.
+//  * Lane l holds x-entries l, l+32, ... of the chunk in registers.  The
+//    y-records are staged into the warp's shared memory with coalesced 128-bit
+//    loads and read back as broadcasts, so a y-record costs two shared loads
+//    per RX pairs.
+//  * Hamming (fast path): residues are bit-sliced (Bp planes of W 32-bit
+//    words); a pair costs Bp*W XOR/OR plus a population test.
+//  * Levenshtein (fast path): Myers/Hyyro bit-parallel recurrence with the
+//    x-pattern's match masks (Peq) in shared memory and the y-text broadcast;
+//    the value on the diagonal through (m, n) is checked every 4 columns and a
+//    warp leaves a y early once all its pairs exceed eps (the diagonal value
+//    never decreases, so the early exit is exact).
+//  * A neighbour pair is kept only in the bin of its lowest common V gene and
+//    lowest common J gene, so a pair that shares several bins counts once.
+#include "idb_internal.cuh"
+
+namespace idb {
+
+namespace {
+
+constexpr int kWarps = 4;            // warps per block
+constexpr int kYB = 64;              // y-records staged per batch
+
+struct DistArgs {
+    const BinPair *bp;
+    const uint32_t *unit_base;
+    const uint4 *rec;
+    const uint32_t *ent_uid;
+    const uint32_t *urow;
+    const uint64_t *vbits, *jbits;
+    uint32_t VW, JW;
+    uint32_t rs16;                   // record size in 16-byte words
+    uint32_t TX, TY, q;
+    uint32_t A;                      // number of codes (Levenshtein)
+    uint2 *edges;
+    uint64_t cap_edges;
+    Counters *ctr;
+    unsigned long long *bp_cycles;   // optional per bin-pair cycle log
+    uint32_t *bp_hits;
+};
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// Edge writer: each warp reserves kEdgeChunk slots at a time; slots a warp
+// does not fill are set to the sentinel (x = kNone) before it moves on.
+struct EdgeWriter {
+    uint64_t base;     // kNone64 = no chunk held
+    uint32_t fill;
+    uint32_t written;
+    static constexpr uint64_t kNoChunk = ~0ull;
+
+    __device__ void init() { base = kNoChunk; fill = 0; written = 0; }
+
+    __device__ void pad(const DistArgs &a, int lane) {
+        if (base == kNoChunk) return;
+        for (uint32_t t = fill + lane; t < kEdgeChunk; t += 32) {
+            const uint64_t slot = base + t;
+            if (slot < a.cap_edges) a.edges[slot] = make_uint2(kNone, kNone);
+        }
+    }
+
+    // warp-uniform call; lanes with ok=true append (lo, hi)
+    __device__ void append(const DistArgs &a, int lane, bool ok, uint32_t lo, uint32_t hi) {
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+        if (!m) return;
+        const uint32_t n = __popc(m);
+        if (base == kNoChunk || fill + n > kEdgeChunk) {
+            pad(a, lane);
+            uint32_t b = 0;
+            if (lane == 0) b = atomicAdd(&a.ctr->edge_reserved, kEdgeChunk);
+            b = __shfl_sync(0xFFFFFFFFu, b, 0);
+            base = b;
+            fill = 0;
+            if ((uint64_t)b + kEdgeChunk > a.cap_edges && lane == 0)
+                atomicOr(&a.ctr->error, kErrEdgeOverflow);
+        }
+        if (ok) {
+            const uint64_t slot = base + fill + __popc(m & lanemask_lt());
+            if (slot < a.cap_edges) a.edges[slot] = make_uint2(lo, hi);
+        }
+        fill += n;
+        written += n;
+    }
+};
+
+// lowest common gene of two uniques in one column, -1 if none
+__device__ __forceinline__ int lowest_common(const uint64_t *bits, uint32_t W, uint32_t rx,
+                                             uint32_t ry) {
+    for (uint32_t w = 0; w < W; ++w) {
+        const uint64_t c = bits[(size_t)rx * W + w] & bits[(size_t)ry * W + w];
+        if (c) return (int)(w * 64) + lowest_bit64(c);
+    }
+    return -1;
+}
+
+__device__ __forceinline__ bool canonical(const DistArgs &a, const BinPair &P, uint32_t ux,
+                                          uint32_t uy) {
+    const uint32_t rx = a.urow[ux], ry = a.urow[uy];
+    return lowest_common(a.vbits, a.VW, rx, ry) == (int)P.v &&
+           lowest_common(a.jbits, a.JW, rx, ry) == (int)P.j;
+}
+
+// Warp-cooperative lookup of the bin pair that owns unit u (largest i with
+// unit_base[i] <= u); 32-ary search.
+__device__ __forceinline__ uint32_t find_binpair(const uint32_t *base, uint32_t n, uint32_t u,
+                                                 int lane) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 32) {
+        const uint32_t step = (hi - lo + 31) / 32;
+        const uint32_t idx = lo + (uint32_t)lane * step;
+        const bool ok = idx < hi && __ldg(base + idx) <= u;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+        const uint32_t t = 31 - __clz(m);
+        lo = lo + t * step;
+        hi = min(hi, lo + step);
+    }
+    const uint32_t idx = lo + lane;
+    const bool ok = idx < hi && __ldg(base + idx) <= u;
+    const uint32_t m = __ballot_sync(0xFFFFFFFFu, ok);
+    return lo + (31 - __clz(m));
+}
+
+struct Unit {
+    BinPair P;
+    uint32_t xbase, nx, ybase, ny;
+};
+
+__device__ __forceinline__ bool next_unit(const DistArgs &a, uint32_t n_units, uint32_t n_bp,
+                                          int lane, Unit &U) {
+    uint32_t u = 0;
+    if (lane == 0) u = atomicAdd(&a.ctr->unit_cursor, 1u);
+    u = __shfl_sync(0xFFFFFFFFu, u, 0);
+    if (u >= n_units) return false;
+    const uint32_t i = find_binpair(a.unit_base, n_bp, u, lane);
+    U.P = a.bp[i];
+    const uint64_t k = u - a.unit_base[i];
+    uint32_t cx, cy;
+    if (U.P.same) {
+        tri_decode(k, U.P.ncx, a.q, cx, cy);
+    } else {
+        cy = (uint32_t)(k / U.P.ncx);
+        cx = (uint32_t)(k % U.P.ncx);
+    }
+    U.xbase = cx * a.TX;
+    U.nx = min(a.TX, U.P.a_n - U.xbase);
+    U.ybase = cy * a.TY;
+    const uint32_t bn = U.P.same ? U.P.a_n : U.P.b_n;
+    U.ny = min(a.TY, bn - U.ybase);
+    return true;
+}
+
+// pairs of the unit that the method evaluates (y after x for a same-bin pair)
+__device__ __forceinline__ uint64_t unit_pairs(const Unit &U, uint32_t xpos) {
+    if (!U.P.same) return U.ny;
+    const uint32_t lo = max(U.ybase, xpos + 1), hi = U.ybase + U.ny;
+    return hi > lo ? hi - lo : 0;
+}
+
+__device__ __forceinline__ void finish(const DistArgs &a, EdgeWriter &ew, uint64_t pairs,
+                                       int lane) {
+    ew.pad(a, lane);
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) pairs += __shfl_xor_sync(0xFFFFFFFFu, pairs, d);
+    if (lane == 0) {
+        if (pairs) atomicAdd(&a.ctr->pairs_evaluated, (unsigned long long)pairs);
+        if (ew.written) atomicAdd(&a.ctr->n_edges, ew.written);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Hamming, fast path.  BP planes x W words per record; RX x-entries per lane.
+// EM: 0 = popcount test, 1 = eps == 1 (d & (d-1)) == 0, 2 = eps == 0.
+// ---------------------------------------------------------------------------
+template <int BP, int W, int RX, int EM>
+__global__ void __launch_bounds__(kWarps * 32)
+k_hamming(DistArgs a) {
+    constexpr int NW = BP * W;                 // words per record used
+    constexpr int R16 = (NW + 3) / 4;          // 16-byte words per record
+    __shared__ uint4 sy[kWarps][kYB * R16];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
+    EdgeWriter ew;
+    ew.init();
+    uint64_t pairs = 0;
+    Unit U;
+    while (next_unit(a, n_units, n_bp, lane, U)) {
+        uint32_t x[RX][R16 * 4];
+        uint32_t xpos[RX];
+        bool xval[RX];
+#pragma unroll
+        for (int r = 0; r < RX; ++r) {
+            xpos[r] = U.xbase + r * 32 + lane;
+            xval[r] = xpos[r] < U.xbase + U.nx;
+            const uint4 *src = a.rec + (size_t)(U.P.a_start + (xval[r] ? xpos[r] : U.xbase)) * R16;
+#pragma unroll
+            for (int q = 0; q < R16; ++q) {
+                const uint4 v = __ldg(src + q);
+                x[r][4 * q + 0] = v.x; x[r][4 * q + 1] = v.y;
+                x[r][4 * q + 2] = v.z; x[r][4 * q + 3] = v.w;
+            }
+            if (xval[r]) pairs += unit_pairs(U, xpos[r]);
+        }
+        const int eps = U.P.eps;
+        const uint32_t yrow0 = (U.P.same ? U.P.a_start : U.P.b_start) + U.ybase;
+        for (uint32_t yb = 0; yb < U.ny; yb += kYB) {
+            const uint32_t nb = min((uint32_t)kYB, U.ny - yb);
+            const uint4 *src = a.rec + (size_t)(yrow0 + yb) * R16;
+            for (uint32_t t = lane; t < nb * R16; t += 32) sy[wid][t] = __ldg(src + t);
+            __syncwarp();
+            for (uint32_t t = 0; t < nb; ++t) {
+                // x-entries before this y (all of them unless the bin pairs with itself)
+                const uint32_t yp = U.ybase + yb + t;
+                uint32_t nact = U.nx;
+                if (U.P.same) nact = yp > U.xbase ? min(U.nx, yp - U.xbase) : 0u;
+                if (nact == 0) continue;
+                uint32_t y[R16 * 4];
+#pragma unroll
+                for (int q = 0; q < R16; ++q) {
+                    const uint4 v = sy[wid][t * R16 + q];
+                    y[4 * q + 0] = v.x; y[4 * q + 1] = v.y; y[4 * q + 2] = v.z; y[4 * q + 3] = v.w;
+                }
+                uint32_t hit = 0;
+#pragma unroll
+                for (int r = 0; r < RX; ++r) {
+                    if ((uint32_t)r * 32 >= nact) break;   // warp-uniform
+                    bool h;
+                    if (W == 1) {
+                        uint32_t d = x[r][0] ^ y[0];
+#pragma unroll
+                        for (int p = 1; p < BP; ++p) d |= x[r][p] ^ y[p];
+                        if (EM == 2) h = d == 0;
+                        else if (EM == 1) h = (d & (d - 1)) == 0;
+                        else h = __popc(d) <= eps;
+                    } else {
+                        int dist = 0;
+#pragma unroll
+                        for (int w = 0; w < W; ++w) {
+                            uint32_t d = x[r][w] ^ y[w];
+#pragma unroll
+                            for (int p = 1; p < BP; ++p) d |= x[r][p * W + w] ^ y[p * W + w];
+                            dist += __popc(d);
+                        }
+                        h = dist <= eps;
+                    }
+                    hit |= (uint32_t)(h && xval[r]) << r;
+                }
+                if (__any_sync(0xFFFFFFFFu, hit)) {
+                    const uint32_t ypos = U.ybase + yb + t;
+                    const uint32_t uy = a.ent_uid[yrow0 + yb + t];
+#pragma unroll
+                    for (int r = 0; r < RX; ++r) {
+                        bool ok = (hit >> r) & 1u;
+                        uint32_t ux = 0;
+                        if (ok && U.P.same && ypos <= xpos[r]) ok = false;
+                        if (ok) {
+                            ux = a.ent_uid[U.P.a_start + xpos[r]];
+                            ok = canonical(a, U.P, ux, uy);
+                        }
+                        ew.append(a, lane, ok, min(ux, uy), max(ux, uy));
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    finish(a, ew, pairs, lane);
+}
+
+// ---------------------------------------------------------------------------
+// Levenshtein, fast path.  Codes records (one byte per residue, RS bytes);
+// pattern <= 32*W residues; RX patterns per lane.
+// ---------------------------------------------------------------------------
+template <int W, int RX>
+__global__ void __launch_bounds__(kWarps * 32)
+k_levenshtein(DistArgs a) {
+    extern __shared__ uint32_t smem[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t A = a.A;
+    const uint32_t peq_words = RX * A * W * 32;          // per warp
+    const uint32_t ybuf_words = kYB * a.rs16 * 4;        // per warp
+    uint32_t *peq = smem + wid * (peq_words + ybuf_words);
+    uint4 *sy = reinterpret_cast<uint4 *>(peq + peq_words);
+    const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
+    EdgeWriter ew;
+    ew.init();
+    uint64_t pairs = 0;
+    Unit U;
+    while (next_unit(a, n_units, n_bp, lane, U)) {
+        const int m = U.P.la, n = U.P.lb, eps = U.P.eps;
+        const int dg = n - m;
+        uint32_t xpos[RX];
+        bool xval[RX];
+        // Peq[r][c][w][lane]
+        for (uint32_t k = 0; k < (uint32_t)RX * A * W; ++k) peq[k * 32 + lane] = 0u;
+        __syncwarp();
+#pragma unroll
+        for (int r = 0; r < RX; ++r) {
+            xpos[r] = U.xbase + r * 32 + lane;
+            xval[r] = xpos[r] < U.xbase + U.nx;
+            if (xval[r]) {
+                pairs += unit_pairs(U, xpos[r]);
+                const uint8_t *codes =
+                    reinterpret_cast<const uint8_t *>(a.rec + (size_t)(U.P.a_start + xpos[r]) * a.rs16);
+                for (int i = 0; i < m; ++i) {
+                    const uint32_t c = __ldg(codes + i);
+                    peq[((r * A + c) * W + (i >> 5)) * 32 + lane] |= 1u << (i & 31);
+                }
+            }
+        }
+        __syncwarp();
+        const uint32_t yrow0 = (U.P.same ? U.P.a_start : U.P.b_start) + U.ybase;
+        for (uint32_t yb = 0; yb < U.ny; yb += kYB) {
+            const uint32_t nb = min((uint32_t)kYB, U.ny - yb);
+            const uint4 *src = a.rec + (size_t)(yrow0 + yb) * a.rs16;
+            for (uint32_t t = lane; t < nb * a.rs16; t += 32) sy[t] = __ldg(src + t);
+            __syncwarp();
+            for (uint32_t t = 0; t < nb; ++t) {
+                const uint32_t ypos = U.ybase + yb + t;
+                const uint8_t *yc = reinterpret_cast<const uint8_t *>(sy + t * a.rs16);
+                uint32_t Pv[RX][W], Mv[RX][W];
+                bool alive[RX];
+#pragma unroll
+                for (int r = 0; r < RX; ++r) {
+                    alive[r] = xval[r] && !(U.P.same && ypos <= xpos[r]);
+#pragma unroll
+                    for (int w = 0; w < W; ++w) { Pv[r][w] = 0xFFFFFFFFu; Mv[r][w] = 0u; }
+                }
+                bool any = false;
+#pragma unroll
+                for (int r = 0; r < RX; ++r) any |= alive[r];
+                if (!__any_sync(0xFFFFFFFFu, any)) continue;
+                for (int j = 0; j < n; ++j) {
+                    const uint32_t c = yc[j];
+#pragma unroll
+                    for (int r = 0; r < RX; ++r) {
+                        const uint32_t *pe = peq + ((r * A + c) * W) * 32 + lane;
+                        if (W == 1) {
+                            myers_step1(Pv[r][0], Mv[r][0], pe[0]);
+                        } else {
+                            int h = 1;
+#pragma unroll
+                            for (int w = 0; w < W; ++w) h = myers_block(Pv[r][w], Mv[r][w], pe[w * 32], h);
+                        }
+                    }
+                    if ((j & 3) == 3) {
+                        const int col = j + 1;
+                        const int i = col - dg;
+                        if (i >= 0 && i <= m) {
+                            bool live = false;
+#pragma unroll
+                            for (int r = 0; r < RX; ++r) {
+                                if (alive[r] && myers_value<W>(Pv[r], Mv[r], i, col) > eps) alive[r] = false;
+                                live |= alive[r];
+                            }
+                            if (!__any_sync(0xFFFFFFFFu, live)) break;
+                        }
+                    }
+                }
+                uint32_t hit = 0;
+#pragma unroll
+                for (int r = 0; r < RX; ++r)
+                    if (alive[r] && myers_value<W>(Pv[r], Mv[r], m, n) <= eps) hit |= 1u << r;
+                if (__any_sync(0xFFFFFFFFu, hit)) {
+                    const uint32_t uy = a.ent_uid[yrow0 + yb + t];
+#pragma unroll
+                    for (int r = 0; r < RX; ++r) {
+                        bool ok = (hit >> r) & 1u;
+                        uint32_t ux = 0;
+                        if (ok) {
+                            ux = a.ent_uid[U.P.a_start + xpos[r]];
+                            ok = canonical(a, U.P, ux, uy);
+                        }
+                        ew.append(a, lane, ok, min(ux, uy), max(ux, uy));
+                    }
+                }
+            }
+            __syncwarp();
+        }
+    }
+    finish(a, ew, pairs, lane);
+}
+
+// ---------------------------------------------------------------------------
+// Generic path (more than 32 distinct residues, or longer than 128): one pair
+// per lane, code bytes read from global memory.  Hamming stops once the count
+// exceeds eps (cuda/PSDBSCAN.hcu:628-636); Levenshtein is a DP restricted to
+// the diagonals |j - i| <= eps with a cut-off once a row exceeds eps.
+// ---------------------------------------------------------------------------
+__device__ bool generic_lev_leq(const uint8_t *x, int m, const uint8_t *y, int n, int eps) {
+    if (eps < 0) return false;
+    if (m - n > eps || n - m > eps) return false;
+    // D restricted to the band; values above eps are clamped to eps+1
+    short row[2][kGenericMaxLen + 1];
+    const int big = eps + 1;
+    for (int j = 0; j <= n; ++j) row[0][j] = (short)min(j, big);
+    int cur = 0;
+    for (int i = 1; i <= m; ++i) {
+        const int nx = cur ^ 1;
+        const int jlo = max(1, i - eps), jhi = min(n, i + eps);
+        row[nx][0] = (short)min(i, big);
+        if (jlo > 1) row[nx][jlo - 1] = (short)big;
+        int rmin = row[nx][0];
+        for (int j = jlo; j <= jhi; ++j) {
+            int v = row[cur][j - 1] + (x[i - 1] != y[j - 1]);
+            const int up = (j <= i - 1 + eps) ? row[cur][j] + 1 : big;
+            const int left = row[nx][j - 1] + 1;
+            v = min(v, min(up, left));
+            v = min(v, big);
+            row[nx][j] = (short)v;
+            rmin = min(rmin, v);
+        }
+        if (jhi < n) row[nx][jhi + 1] = (short)big;
+        cur = nx;
+        if (rmin > eps) return false;
+    }
+    return row[cur][n] <= eps;
+}
+
+template <bool HAM>
+__global__ void __launch_bounds__(kWarps * 32)
+k_generic(DistArgs a) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
+    EdgeWriter ew;
+    ew.init();
+    uint64_t pairs = 0;
+    Unit U;
+    while (next_unit(a, n_units, n_bp, lane, U)) {
+        const int m = U.P.la, n = U.P.lb, eps = U.P.eps;
+        const uint32_t yrow0 = (U.P.same ? U.P.a_start : U.P.b_start) + U.ybase;
+        const uint32_t total = U.nx * U.ny;
+        for (uint32_t p0 = 0; p0 < total; p0 += 32) {
+            const uint32_t p = p0 + lane;
+            bool ok = false;
+            uint32_t ux = 0, uy = 0;
+            if (p < total) {
+                const uint32_t xi = p / U.ny, yi = p % U.ny;
+                const uint32_t xpos = U.xbase + xi, ypos = U.ybase + yi;
+                if (!(U.P.same && ypos <= xpos)) {
+                    ++pairs;
+                    const uint8_t *xc =
+                        reinterpret_cast<const uint8_t *>(a.rec + (size_t)(U.P.a_start + xpos) * a.rs16);
+                    const uint8_t *yc =
+                        reinterpret_cast<const uint8_t *>(a.rec + (size_t)(yrow0 + yi) * a.rs16);
+                    if (HAM) {
+                        int d = 0;
+                        ok = eps >= 0;
+                        for (int k = 0; k < m && ok; ++k)
+                            if (xc[k] != yc[k] && ++d > eps) ok = false;
+                    } else {
+                        ok = generic_lev_leq(xc, m, yc, n, eps);
+                    }
+                    if (ok) {
+                        ux = a.ent_uid[U.P.a_start + xpos];
+                        uy = a.ent_uid[yrow0 + yi];
+                        ok = canonical(a, U.P, ux, uy);
+                    }
+                }
+            }
+            ew.append(a, lane, ok, min(ux, uy), max(ux, uy));
+        }
+    }
+    finish(a, ew, pairs, lane);
+}
+
+// ---------------------------------------------------------------------------
+// Admissible-pair count (the throughput metric's numerator): unique pairs that
+// share a bin (V and J overlap) with an admissible length gap, each counted in
+// its canonical bin only.  One pair per lane; run once per workload.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kWarps * 32)
+k_count_admissible(DistArgs a) {
+    const int lane = threadIdx.x & 31;
+    const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
+    unsigned long long cnt = 0;
+    Unit U;
+    while (next_unit(a, n_units, n_bp, lane, U)) {
+        const uint32_t yrow0 = (U.P.same ? U.P.a_start : U.P.b_start) + U.ybase;
+        const uint32_t total = U.nx * U.ny;
+        for (uint32_t p = lane; p < total; p += 32) {
+            const uint32_t xi = p / U.ny, yi = p % U.ny;
+            const uint32_t xpos = U.xbase + xi, ypos = U.ybase + yi;
+            if (U.P.same && ypos <= xpos) continue;
+            if (U.P.eps < 0) continue;
+            const uint32_t ux = a.ent_uid[U.P.a_start + xpos], uy = a.ent_uid[yrow0 + yi];
+            cnt += canonical(a, U.P, ux, uy);
+        }
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, d);
+    if (lane == 0 && cnt) atomicAdd(&a.ctr->admissible_pairs, cnt);
+}
+
+template <typename K>
+int occupancy_grid(K kernel, size_t smem) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kWarps * 32, smem);
+    if (per_sm < 1) per_sm = 1;
+    return per_sm * sm_count();
+}
+
+template <typename K>
+void run(K kernel, const DistArgs &a, size_t smem, int grid, cudaStream_t s) {
+    if (smem > 48 * 1024)
+        cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (grid <= 0) grid = occupancy_grid(kernel, smem);
+    kernel<<<grid, kWarps * 32, smem, s>>>(a);
+}
+
+template <int BP, int W, int RX>
+void run_hamming(const Plan &P, const DistArgs &a, int grid, cudaStream_t s) {
+    if (P.hamming_eps_mode == 2) run(k_hamming<BP, W, RX, 2>, a, 0, grid, s);
+    else if (P.hamming_eps_mode == 1 && W == 1) run(k_hamming<BP, W, RX, 1>, a, 0, grid, s);
+    else run(k_hamming<BP, W, RX, 0>, a, 0, grid, s);
+}
+
+}  // namespace
+
+static DistArgs make_args(const Plan &P, const Buffers &B) {
+    DistArgs a;
+    a.bp = B.bp_sorted;
+    a.unit_base = B.bp_units;
+    a.rec = B.ent_rec;
+    a.ent_uid = B.ent_uid;
+    a.urow = B.urow;
+    a.vbits = B.vbits; a.jbits = B.jbits;
+    a.VW = P.VW; a.JW = P.JW;
+    a.rs16 = P.RS / 16;
+    a.TX = P.TX; a.TY = P.TY; a.q = P.TY / P.TX;
+    a.A = P.A;
+    a.edges = B.edges;
+    a.cap_edges = P.cap_edges;
+    a.ctr = B.ctr;
+    a.bp_cycles = nullptr;
+    a.bp_hits = nullptr;
+    return a;
+}
+
+void launch_count_admissible(const Plan &P, const Buffers &B, cudaStream_t s) {
+    DistArgs a = make_args(P, B);
+    cudaMemsetAsync(&B.ctr->unit_cursor, 0, sizeof(uint32_t), s);
+    run(k_count_admissible, a, 0, 0, s);
+}
+
+const char *distance_variant_name(const Plan &P) {
+    if (!P.fast) return P.hamming ? "k_generic<hamming>" : "k_generic<levenshtein>";
+    return P.hamming ? "k_hamming" : "k_levenshtein";
+}
+
+void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s) {
+    DistArgs a = make_args(P, B);
+    if (!P.fast) {
+        if (P.hamming) run(k_generic<true>, a, 0, grid, s);
+        else run(k_generic<false>, a, 0, grid, s);
+        return;
+    }
+    if (P.hamming) {
+        const int RX = (int)P.RX;
+        if (P.B <= 2) {
+            switch (P.W) {
+                case 1: if (RX == 4) run_hamming<2, 1, 4>(P, a, grid, s); else run_hamming<2, 1, 8>(P, a, grid, s); break;
+                case 2: run_hamming<2, 2, 4>(P, a, grid, s); break;
+                case 3: run_hamming<2, 3, 4>(P, a, grid, s); break;
+                default: run_hamming<2, 4, 4>(P, a, grid, s); break;
+            }
+        } else {
+            switch (P.W) {
+                case 1: if (RX == 4) run_hamming<5, 1, 4>(P, a, grid, s); else run_hamming<5, 1, 8>(P, a, grid, s); break;
+                case 2: run_hamming<5, 2, 4>(P, a, grid, s); break;
+                case 3: run_hamming<5, 3, 4>(P, a, grid, s); break;
+                default: run_hamming<5, 4, 4>(P, a, grid, s); break;
+            }
+        }
+        return;
+    }
+    const size_t smem = (size_t)kWarps * ((size_t)P.RX * P.A * P.W * 32 * 4 + (size_t)kYB * P.RS);
+    switch (P.W) {
+        case 1: if (P.RX == 2) run(k_levenshtein<1, 2>, a, smem, grid, s); else run(k_levenshtein<1, 1>, a, smem, grid, s); break;
+        case 2: run(k_levenshtein<2, 1>, a, smem, grid, s); break;
+        case 3: run(k_levenshtein<3, 1>, a, smem, grid, s); break;
+        default: run(k_levenshtein<4, 1>, a, smem, grid, s); break;
+    }
+}
+
+}  // namespace idb

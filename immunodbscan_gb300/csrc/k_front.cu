@@ -1,0 +1,455 @@
+// k_front.cu -- front of the clustering path: input survey, V/J gene bitsets,
+// exact-duplicate collapse, unique numbering, and the device-wide scan used by
+// every compaction of the pipeline.
+//
+// Reference counterparts:
+//  survey/lengths      cuda/StringOperations.hcu:77-116 (lengths, max_strlen)
+//  gene bitsets (S1)   cuda/BitsetVector.inl:28-45, 118-209 (110 serial launches,
+//                      one block per row); here one launch, one warp per row
+//  duplicates (S3)     cuda/PSDBSCAN.hcu:525-573 (an N^2 thread grid) + 1074-1085
+//                      (sort / reduce_by_key / scatter); here one hash-table pass
+//  uniques             cuda/PSDBSCAN.hcu:1102-1111 (remove_if over copies != 0)
+#include "idb_internal.cuh"
+
+namespace idb {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+__device__ __forceinline__ uint32_t rep_of_row(const uint32_t *rep_off, uint32_t R, uint32_t i) {
+    // largest r with rep_off[r] <= i
+    uint32_t lo = 0, hi = R;   // invariant: rep_off[lo] <= i < rep_off[hi]
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (rep_off[mid] <= i) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------------------
+// Survey: sequence length range and the set of byte values present.
+// ---------------------------------------------------------------------------
+__global__ void k_survey(const uint8_t *__restrict__ seq, const int64_t *__restrict__ off,
+                         uint32_t N, Counters *ctr) {
+    __shared__ uint32_t used[8];
+    __shared__ uint32_t smax, smin;
+    if (threadIdx.x < 8) used[threadIdx.x] = 0;
+    if (threadIdx.x == 0) { smax = 0; smin = 0xFFFFFFFFu; }
+    __syncthreads();
+    uint32_t lmax = 0, lmin = 0xFFFFFFFFu;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+        uint32_t L = (uint32_t)(off[i + 1] - off[i]);
+        lmax = max(lmax, L);
+        lmin = min(lmin, L);
+    }
+    const int64_t b0 = N ? off[0] : 0, b1 = N ? off[N] : 0;
+    for (int64_t p = b0 + blockIdx.x * blockDim.x + threadIdx.x; p < b1; p += stride) {
+        uint32_t b = seq[p];
+        uint32_t bit = 1u << (b & 31);
+        if (!(used[b >> 5] & bit)) atomicOr(&used[b >> 5], bit);
+    }
+    atomicMax(&smax, lmax);
+    atomicMin(&smin, lmin);
+    __syncthreads();
+    if (threadIdx.x < 8 && used[threadIdx.x]) atomicOr(&ctr->used[threadIdx.x], used[threadIdx.x]);
+    if (threadIdx.x == 0) {
+        atomicMax(&ctr->lmax, smax);
+        atomicMin(&ctr->lmin, smin);
+    }
+}
+
+// Every row carries the literal "Gene" (no sequence column configured).
+__global__ void k_const_strings(uint8_t *blob, int64_t *off, uint32_t N) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i <= N; i += stride) {
+        off[i] = 4 * (int64_t)i;
+        if (i < N) {
+            blob[4 * (size_t)i + 0] = 'G';
+            blob[4 * (size_t)i + 1] = 'e';
+            blob[4 * (size_t)i + 2] = 'n';
+            blob[4 * (size_t)i + 3] = 'e';
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// S1 -- gene bitsets.  Bit g of a row is set iff reference gene name g is a
+// byte-exact substring of the row's call (cuda/BitsetVector.inl:149-175).  One
+// warp per row; lane l tests genes l, l+32, ...; a ballot assembles 32 bits.
+// Names live in shared memory.  An empty name never matches (the reference
+// launches a zero-thread block for it).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads)
+k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, uint32_t N,
+            const uint8_t *__restrict__ genes, const int32_t *__restrict__ goff, uint32_t G,
+            uint32_t GW, uint32_t smem_genes, uint64_t *__restrict__ bits) {
+    extern __shared__ uint8_t sm[];
+    int32_t *s_goff = reinterpret_cast<int32_t *>(sm);
+    uint8_t *s_genes = sm + sizeof(int32_t) * (G + 1);
+    for (uint32_t k = threadIdx.x; k <= G; k += blockDim.x) s_goff[k] = goff[k];
+    for (uint32_t k = threadIdx.x; k < smem_genes; k += blockDim.x) s_genes[k] = genes[k];
+    __syncthreads();
+    const uint8_t *gsrc = (uint32_t)goff[G] <= smem_genes ? s_genes : genes;
+    const int lane = threadIdx.x & 31;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t i = warp; i < N; i += nwarps) {
+        const int64_t c0 = off[i];
+        const uint32_t cl = (uint32_t)(off[i + 1] - c0);
+        const uint8_t *c = calls + c0;
+        uint64_t acc[kMaxGeneWords];
+#pragma unroll
+        for (int w = 0; w < kMaxGeneWords; ++w) acc[w] = 0;
+        for (uint32_t gb = 0; gb * 32 < G; ++gb) {
+            const uint32_t g = gb * 32 + lane;
+            bool found = false;
+            if (g < G) {
+                const int32_t n0 = s_goff[g];
+                const uint32_t nl = (uint32_t)(s_goff[g + 1] - n0);
+                const uint8_t *name = gsrc + n0;
+                if (nl > 0 && nl <= cl) {
+                    const uint8_t first = name[0];
+                    for (uint32_t p = 0; p + nl <= cl && !found; ++p) {
+                        if (c[p] != first) continue;
+                        uint32_t k = 1;
+                        while (k < nl && c[p + k] == name[k]) ++k;
+                        found = (k == nl);
+                    }
+                }
+            }
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, found);
+#pragma unroll
+            for (int w = 0; w < kMaxGeneWords; ++w)
+                if ((int)(gb >> 1) == w) acc[w] |= (uint64_t)m << (32 * (gb & 1));
+        }
+#pragma unroll
+        for (int w = 0; w < kMaxGeneWords; ++w)
+            if (lane == w && (uint32_t)w < GW) bits[(size_t)i * GW + w] = acc[w];
+    }
+}
+
+// No gene column: every row carries bit 0 ("V" against ["V"]).
+__global__ void k_gene_bits_const(uint32_t N, uint64_t *bits) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) bits[i] = 1ull;
+}
+
+// ---------------------------------------------------------------------------
+// S3 -- exact duplicates.  Key = (repertoire, length, V bits, J bits, bytes).
+// Open addressing; a slot holds a row index, the class's minimum row wins via
+// atomicMin (the reference links larger indices to smaller ones,
+// cuda/PSDBSCAN.hcu:85-86, so its representative is the minimum index too).
+// Equality is checked on the full key; the hash only spreads the probes.
+// ---------------------------------------------------------------------------
+struct DedupArgs {
+    const uint8_t *seq; const int64_t *off;
+    const uint64_t *vbits, *jbits; uint32_t VW, JW;
+    const uint32_t *rep_off; uint32_t R;
+    uint32_t N;
+    uint32_t *table, *tcount, *slot;
+    uint64_t mask;
+    Counters *ctr;
+};
+
+__device__ bool rows_equal(const DedupArgs &a, uint32_t x, uint32_t y, uint32_t rx) {
+    const int64_t ox = a.off[x], oy = a.off[y];
+    const uint32_t lx = (uint32_t)(a.off[x + 1] - ox);
+    if ((uint32_t)(a.off[y + 1] - oy) != lx) return false;
+    if (rep_of_row(a.rep_off, a.R, y) != rx) return false;
+    for (uint32_t w = 0; w < a.VW; ++w)
+        if (a.vbits[(size_t)x * a.VW + w] != a.vbits[(size_t)y * a.VW + w]) return false;
+    for (uint32_t w = 0; w < a.JW; ++w)
+        if (a.jbits[(size_t)x * a.JW + w] != a.jbits[(size_t)y * a.JW + w]) return false;
+    const uint8_t *px = a.seq + ox, *py = a.seq + oy;
+    for (uint32_t k = 0; k < lx; ++k)
+        if (px[k] != py[k]) return false;
+    return true;
+}
+
+__global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += stride) {
+        const uint32_t r = rep_of_row(a.rep_off, a.R, i);
+        const int64_t o = a.off[i];
+        const uint32_t L = (uint32_t)(a.off[i + 1] - o);
+        uint64_t h = mix64(0x1234567ull + r, L);
+        for (uint32_t w = 0; w < a.VW; ++w) h = mix64(h, a.vbits[(size_t)i * a.VW + w]);
+        for (uint32_t w = 0; w < a.JW; ++w) h = mix64(h, a.jbits[(size_t)i * a.JW + w]);
+        const uint8_t *p = a.seq + o;
+        uint64_t word = 0;
+        for (uint32_t k = 0; k < L; ++k) {
+            word = (word << 8) | p[k];
+            if ((k & 7) == 7) { h = mix64(h, word); word = 0; }
+        }
+        h = mix64(h, word);
+        uint64_t s = h & a.mask;
+        uint32_t it = 0;
+        for (;; ++it) {
+            if (it > a.mask || it >= kSpinCap) {   // table full: cannot happen at load <= 1/2
+                atomicOr(&a.ctr->error, kErrHashStall);
+                s = kNone;
+                break;
+            }
+            uint32_t cur = *((volatile uint32_t *)&a.table[s]);
+            if (cur == kNone) {
+                uint32_t prev = atomicCAS(&a.table[s], kNone, i);
+                if (prev == kNone) break;
+                cur = prev;
+            }
+            if (rows_equal(a, i, cur, r)) {
+                atomicMin(&a.table[s], i);
+                break;
+            }
+            s = (s + 1) & a.mask;
+        }
+        a.slot[i] = (uint32_t)s;
+        if (s != kNone) atomicAdd(&a.tcount[s], 1u);
+    }
+}
+
+__global__ void k_dedupe_final(uint32_t N, const uint32_t *__restrict__ slot,
+                               const uint32_t *__restrict__ table, uint32_t *__restrict__ rep_row,
+                               uint32_t *__restrict__ flag) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+        const uint32_t s = slot[i];
+        const uint32_t r = s == kNone ? i : table[s];
+        rep_row[i] = r;
+        flag[i] = (r == i);
+    }
+}
+
+// Unique numbering: uid = rank of the representative row among representatives
+// (ascending row order, cuda/PSDBSCAN.hcu:1102-1111).  Also the per-unique
+// columns and the row -> uid map.
+__global__ void k_uniques(uint32_t N, const int64_t *__restrict__ off,
+                          const uint32_t *__restrict__ rep_off, uint32_t R,
+                          const uint32_t *__restrict__ slot, const uint32_t *__restrict__ tcount,
+                          const uint32_t *__restrict__ rep_row, const uint32_t *__restrict__ uid_of_row,
+                          uint32_t *__restrict__ urow, uint32_t *__restrict__ ucopies,
+                          uint32_t *__restrict__ ulen, uint32_t *__restrict__ urep,
+                          uint32_t *__restrict__ row2uid) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+        const uint32_t r = rep_row[i];
+        if (r == i) {
+            const uint32_t u = uid_of_row[i];
+            urow[u] = i;
+            ucopies[u] = slot[i] == kNone ? 1u : tcount[slot[i]];
+            ulen[u] = (uint32_t)(off[i + 1] - off[i]);
+            urep[u] = rep_of_row(rep_off, R, i);
+        }
+        row2uid[i] = uid_of_row[r];
+    }
+}
+
+__global__ void k_uid_first(uint32_t N, uint32_t R, const uint32_t *__restrict__ rep_off,
+                            const uint32_t *__restrict__ uid_of_row, const Counters *ctr,
+                            uint32_t *__restrict__ uid_first) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r <= R) {
+        const uint32_t row = rep_off[r];
+        uid_first[r] = row < N ? uid_of_row[row] : ctr->n_uniques;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Exclusive scan (reduce, scan of block sums, down-sweep).  4096 items per block.
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr uint32_t kScanTile = kScanThreads * kScanItems;
+
+__device__ __forceinline__ uint32_t warp_incl_scan(uint32_t v) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        uint32_t t = __shfl_up_sync(0xFFFFFFFFu, v, d);
+        if (lane >= d) v += t;
+    }
+    return v;
+}
+
+// exclusive block scan of one value per thread; returns prefix, *sum = total
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *sum) {
+    __shared__ uint32_t wsum[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int nw = blockDim.x >> 5;
+    uint32_t inc = warp_incl_scan(v);
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        uint32_t w = lane < nw ? wsum[lane] : 0u;
+        uint32_t wi = warp_incl_scan(w);
+        if (lane < nw) wsum[lane] = wi - w;
+        if (lane == nw - 1) wsum[31] = wi;
+    }
+    __syncthreads();
+    uint32_t res = inc - v + wsum[wid];
+    *sum = wsum[31];
+    __syncthreads();
+    return res;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_reduce(const uint32_t *__restrict__ in, uint32_t n_host, const uint32_t *n_dev,
+              uint32_t *__restrict__ part) {
+    const uint32_t n = n_dev ? min(*n_dev, n_host) : n_host;
+    const uint64_t base = (uint64_t)blockIdx.x * kScanTile;
+    uint32_t s = 0;
+    for (int k = 0; k < kScanItems; ++k) {
+        uint64_t i = base + (uint64_t)k * kScanThreads + threadIdx.x;
+        if (i < n) s += in[i];
+    }
+    uint32_t total;
+    block_excl_scan(s, &total);
+    if (threadIdx.x == 0) part[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024)
+k_scan_parts(uint32_t *__restrict__ part, uint32_t nb, uint32_t *total_out) {
+    const uint32_t per = (nb + blockDim.x - 1) / blockDim.x;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t s = 0;
+    for (uint32_t k = 0; k < per; ++k)
+        if (b0 + k < nb) s += part[b0 + k];
+    uint32_t total;
+    uint32_t pre = block_excl_scan(s, &total);
+    for (uint32_t k = 0; k < per; ++k)
+        if (b0 + k < nb) {
+            uint32_t v = part[b0 + k];
+            part[b0 + k] = pre;
+            pre += v;
+        }
+    if (threadIdx.x == 0 && total_out) *total_out = total;
+}
+
+__global__ void __launch_bounds__(kScanThreads)
+k_scan_down(const uint32_t *in, uint32_t *out, uint32_t n_host, const uint32_t *n_dev,
+            const uint32_t *__restrict__ part) {
+    const uint32_t n = n_dev ? min(*n_dev, n_host) : n_host;
+    const uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        uint64_t i = base + k;
+        v[k] = i < n ? in[i] : 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t pre = block_excl_scan(s, &total) + part[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) {
+        uint64_t i = base + k;
+        if (i < n) out[i] = pre;
+        pre += v[k];
+    }
+}
+
+// A replayed plan is only valid while lengths and byte values stay inside the
+// ones it was built for.
+struct PlanShape {
+    uint32_t lmin, lmax;
+    uint32_t used[8];
+};
+
+__global__ void k_check_plan(PlanShape ps, Counters *ctr) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    uint32_t err = 0;
+    if (ctr->lmax > ps.lmax || ctr->lmin < ps.lmin) err |= kErrLength;
+    for (int k = 0; k < 8; ++k)
+        if (ctr->used[k] & ~ps.used[k]) err |= kErrAlphabet;
+    if (err) atomicOr(&ctr->error, err);
+}
+
+inline int grid_for(uint64_t n, int threads = kThreads) {
+    uint64_t g = (n + threads - 1) / threads;
+    uint64_t cap = (uint64_t)sm_count() * 8;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+uint32_t scan_part_needed(uint64_t n) { return (uint32_t)((n + kScanTile - 1) / kScanTile + 1); }
+
+void scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, const uint32_t *n_dev,
+              uint32_t *total, uint32_t *part, uint32_t part_cap, cudaStream_t s) {
+    const uint32_t nb = (uint32_t)((n + kScanTile - 1) / kScanTile);
+    if (nb == 0) {
+        if (total) cudaMemsetAsync(total, 0, sizeof(uint32_t), s);
+        return;
+    }
+    (void)part_cap;
+    k_scan_reduce<<<nb, kScanThreads, 0, s>>>(in, n, n_dev, part);
+    k_scan_parts<<<1, 1024, 0, s>>>(part, nb, total);
+    k_scan_down<<<nb, kScanThreads, 0, s>>>(in, out, n, n_dev, part);
+}
+
+void launch_check_plan(const Plan &P, const Buffers &B, cudaStream_t s) {
+    PlanShape ps;
+    ps.lmin = P.Lmin;
+    ps.lmax = P.Lmax;
+    for (int k = 0; k < 8; ++k) ps.used[k] = 0;
+    for (int b = 0; b < 256; ++b)
+        if (P.codemap[b] != 0 || b == P.first_byte) ps.used[b >> 5] |= 1u << (b & 31);
+    k_check_plan<<<1, 32, 0, s>>>(ps, B.ctr);
+}
+
+void launch_survey(const Plan &P, const Buffers &B, cudaStream_t s) {
+    k_survey<<<grid_for(P.N), kThreads, 0, s>>>(B.seq, B.seq_off, P.N, B.ctr);
+}
+
+void launch_const_strings(uint8_t *blob, int64_t *off, uint32_t N, cudaStream_t s) {
+    k_const_strings<<<grid_for((uint64_t)N + 1), kThreads, 0, s>>>(blob, off, N);
+}
+
+void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream_t s) {
+    const bool absent = v_column ? P.no_v : P.no_j;
+    uint64_t *bits = v_column ? B.vbits : B.jbits;
+    if (absent) {
+        k_gene_bits_const<<<grid_for(P.N), kThreads, 0, s>>>(P.N, bits);
+        return;
+    }
+    const uint32_t G = v_column ? P.Gv : P.Gj;
+    const uint32_t GW = v_column ? P.VW : P.JW;
+    const uint8_t *calls = v_column ? B.vcall : B.jcall;
+    const int64_t *off = v_column ? B.v_off : B.j_off;
+    const uint8_t *genes = v_column ? B.vgenes : B.jgenes;
+    const int32_t *goff = v_column ? B.vg_off : B.jg_off;
+    const uint32_t gene_bytes = v_column ? P.gene_bytes_v : P.gene_bytes_j;
+    const uint32_t smem_genes = gene_bytes <= 40000u ? gene_bytes : 0u;
+    const size_t smem = sizeof(int32_t) * (G + 1) + smem_genes;
+    const int grid = grid_for((uint64_t)P.N * 32);
+    k_gene_bits<<<grid, kThreads, smem, s>>>(calls, off, P.N, genes, goff, G, GW, smem_genes, bits);
+}
+
+void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s) {
+    DedupArgs a;
+    a.seq = B.seq; a.off = B.seq_off;
+    a.vbits = B.vbits; a.jbits = B.jbits; a.VW = P.VW; a.JW = P.JW;
+    a.rep_off = B.rep_off; a.R = P.R; a.N = P.N;
+    a.table = B.table; a.tcount = B.tcount; a.slot = B.slot;
+    a.mask = B.table_mask; a.ctr = B.ctr;
+    cudaMemsetAsync(B.table, 0xFF, sizeof(uint32_t) * (B.table_mask + 1), s);
+    cudaMemsetAsync(B.tcount, 0, sizeof(uint32_t) * (B.table_mask + 1), s);
+    k_dedupe_insert<<<grid_for(P.N), kThreads, 0, s>>>(a);
+    k_dedupe_final<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.slot, B.table, B.rep_row, B.flag);
+}
+
+void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s) {
+    scan_u32(B.flag, B.uid_of_row, P.N, nullptr, &B.ctr->n_uniques, B.scan_part,
+             B.scan_part_cap, s);
+    k_uniques<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.seq_off, B.rep_off, P.R, B.slot, B.tcount,
+                                                   B.rep_row, B.uid_of_row, B.urow, B.ucopies,
+                                                   B.ulen, B.urep, B.row2uid);
+    k_uid_first<<<(P.R + 1 + 255) / 256, 256, 0, s>>>(P.N, P.R, B.rep_off, B.uid_of_row, B.ctr,
+                                                     B.uid_first);
+}
+
+}  // namespace idb

@@ -1,0 +1,276 @@
+// k_graph.cu -- neighbour graph, core points, cluster growth and labels
+// (rules S5-S7).
+//
+// Reference counterparts:
+//  core counts (S5)  cuda/PSDBSCAN.hcu:1099 (count starts at copies), :824-826 /
+//                    :648-650 (each neighbour pair adds the other side's copies),
+//                    :1180 (core = count >= minPts)
+//  growth (S6)       cuda/PSDBSCAN.hcu:866-926: core-core neighbours are merged by
+//                    union_a_and_b (:76-107, link towards the smaller index), a
+//                    non-core neighbour is claimed by the first core to win an
+//                    atomicCAS (:113-122)
+//  labels (S7)       cuda/PSDBSCAN.hcu:1263-1294 (+ tree_reduction_kernel :129-149)
+//  tree depths       cuda/PSDBSCAN.hcu:154-177, 1020-1040
+//
+// Here the neighbour pairs found by the distance kernel form an edge list that
+// is turned into a CSR graph by count / scan / fill.  Counts are accumulated
+// per edge, unions hook the larger root under the smaller one with atomicCAS
+// and find() halves paths, so every component's root is its minimum core
+// index, as in the reference.  A border unique joins the cluster of its
+// minimum-index core neighbour (deterministic; one of the outcomes the
+// reference's race allows).  Labels are 1 + the rank of the root among the
+// repertoire's core roots, found with one exclusive scan over root flags.
+#include "idb_internal.cuh"
+
+namespace idb {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline int grid_for(uint64_t n, int threads = kThreads) {
+    uint64_t g = (n + threads - 1) / threads;
+    uint64_t cap = (uint64_t)sm_count() * 8;
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
+
+__device__ __forceinline__ uint32_t edge_slots(const Counters *ctr, uint64_t cap) {
+    const uint64_t r = ctr->edge_reserved;
+    return (uint32_t)(r < cap ? r : cap);
+}
+
+__global__ void k_graph_init(const Counters *__restrict__ ctr, const uint32_t *__restrict__ ucopies,
+                             uint32_t *__restrict__ cnt, uint32_t *__restrict__ parent,
+                             uint32_t *__restrict__ bmin) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        cnt[u] = ucopies[u];
+        parent[u] = u;
+        bmin[u] = kNone;
+    }
+}
+
+// count pass: degrees for the CSR and copies-weighted neighbour counts
+__global__ void k_degree(const Counters *__restrict__ ctr, uint64_t cap, const uint2 *__restrict__ edges,
+                         const uint32_t *__restrict__ ucopies, uint32_t *__restrict__ deg,
+                         uint32_t *__restrict__ cnt) {
+    const uint32_t ne = edge_slots(ctr, cap);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
+        const uint2 ed = edges[e];
+        if (ed.x == kNone) continue;
+        atomicAdd(&deg[ed.x], 1u);
+        atomicAdd(&deg[ed.y], 1u);
+        atomicAdd(&cnt[ed.x], ucopies[ed.y]);
+        atomicAdd(&cnt[ed.y], ucopies[ed.x]);
+    }
+}
+
+// fill pass
+__global__ void k_fill_adj(const Counters *__restrict__ ctr, uint64_t cap, const uint2 *__restrict__ edges,
+                           const uint32_t *__restrict__ off, uint32_t *__restrict__ cursor,
+                           uint32_t *__restrict__ adj) {
+    const uint32_t ne = edge_slots(ctr, cap);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
+        const uint2 ed = edges[e];
+        if (ed.x == kNone) continue;
+        adj[off[ed.x] + atomicAdd(&cursor[ed.x], 1u)] = ed.y;
+        adj[off[ed.y] + atomicAdd(&cursor[ed.y], 1u)] = ed.x;
+    }
+}
+
+__global__ void k_core(const Counters *__restrict__ ctr0, Counters *ctr, const uint32_t *__restrict__ cnt,
+                       uint32_t min_pts, uint32_t *__restrict__ ucore) {
+    const uint32_t nu = ctr0->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t local = 0;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t c = cnt[u] >= min_pts;
+        ucore[u] = c;
+        local += c;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) local += __shfl_xor_sync(0xFFFFFFFFu, local, d);
+    if ((threadIdx.x & 31) == 0 && local) atomicAdd(&ctr->n_cores, local);
+}
+
+__device__ __forceinline__ uint32_t uf_find(uint32_t *p, uint32_t x) {
+    volatile uint32_t *vp = p;
+    while (true) {   // parent[y] <= y always, so x strictly decreases: terminates
+        const uint32_t px = vp[x];
+        if (px == x) return x;
+        const uint32_t ppx = vp[px];
+        if (ppx == px) return px;
+        vp[x] = ppx;           // path halving
+        x = ppx;
+    }
+}
+
+__global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ edges,
+                        const uint32_t *__restrict__ ucore, uint32_t *parent) {
+    const uint32_t ne = edge_slots(ctr, cap);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
+        const uint2 ed = edges[e];
+        if (ed.x == kNone || !ucore[ed.x] || !ucore[ed.y]) continue;
+        uint32_t a = ed.x, b = ed.y;
+        uint32_t it = 0;
+        for (; it < kSpinCap; ++it) {
+            uint32_t ra = uf_find(parent, a), rb = uf_find(parent, b);
+            if (ra == rb) break;
+            if (ra < rb) { const uint32_t t = ra; ra = rb; rb = t; }
+            // hook the larger root under the smaller one
+            if (atomicCAS(&parent[ra], ra, rb) == ra) break;
+            a = ra;
+            b = rb;
+        }
+        if (it == kSpinCap) atomicOr(&ctr->error, kErrUnionStall);
+    }
+}
+
+// border rule: a non-core unique joins its minimum-index core neighbour
+__global__ void k_border(const Counters *__restrict__ ctr, const uint32_t *__restrict__ off,
+                         const uint32_t *__restrict__ adj, const uint32_t *__restrict__ ucore,
+                         uint32_t *__restrict__ bmin) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        if (ucore[u]) continue;
+        uint32_t best = kNone;
+        for (uint32_t k = off[u]; k < off[u + 1]; ++k) {
+            const uint32_t w = adj[k];
+            if (ucore[w] && w < best) best = w;
+        }
+        bmin[u] = best;
+    }
+}
+
+// depth of every row in the union-find forest before compression (diagnostic)
+__global__ void k_depth(uint32_t N, const uint32_t *__restrict__ row2uid, const uint32_t *__restrict__ urow,
+                        const uint32_t *__restrict__ ucore, const uint32_t *__restrict__ bmin,
+                        const uint32_t *parent, uint32_t *__restrict__ hist) {
+    __shared__ uint32_t h[kDepthMax + 1];
+    for (int k = threadIdx.x; k <= kDepthMax; k += blockDim.x) h[k] = 0;
+    __syncthreads();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+        const uint32_t u = row2uid[i];
+        uint32_t depth = urow[u] != i;                  // duplicate -> representative
+        uint32_t x = u;
+        if (!ucore[u]) {
+            if (bmin[u] == kNone) x = kNone;
+            else { x = bmin[u]; ++depth; }
+        }
+        if (x != kNone)
+            while (depth < kDepthMax) {
+                const uint32_t px = parent[x];
+                if (px == x) break;
+                x = px;
+                ++depth;
+            }
+        atomicAdd(&h[min(depth, (uint32_t)kDepthMax)], 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k <= kDepthMax; k += blockDim.x)
+        if (h[k]) atomicAdd(&hist[k], h[k]);
+}
+
+__global__ void k_compress(const Counters *__restrict__ ctr, const uint32_t *__restrict__ ucore,
+                           uint32_t *parent, uint32_t *__restrict__ rootflag) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        uint32_t r = u;
+        if (ucore[u]) {
+            r = uf_find(parent, u);
+            parent[u] = r;
+        }
+        rootflag[u] = ucore[u] && r == u;
+    }
+}
+
+__global__ void k_labels(const Counters *__restrict__ ctr, const uint32_t *__restrict__ ucore,
+                         const uint32_t *__restrict__ parent, const uint32_t *__restrict__ bmin,
+                         const uint32_t *__restrict__ rank, const uint32_t *__restrict__ urep,
+                         const uint32_t *__restrict__ uid_first, uint32_t *__restrict__ ulabel) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        uint32_t root = kNone;
+        if (ucore[u]) root = parent[u];
+        else if (bmin[u] != kNone) root = parent[bmin[u]];
+        uint32_t lab = 0;
+        if (root != kNone) lab = rank[root] - rank[uid_first[urep[u]]] + 1;
+        ulabel[u] = lab;
+    }
+}
+
+__global__ void k_rows_out(uint32_t N, uint32_t min_pts, const uint32_t *__restrict__ row2uid,
+                           const uint32_t *__restrict__ urow, const uint32_t *__restrict__ ucopies,
+                           const uint32_t *__restrict__ ucore, const uint32_t *__restrict__ ulabel,
+                           uint32_t *__restrict__ clone_id, int32_t *__restrict__ core,
+                           uint32_t *__restrict__ copies, Counters *ctr) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t noise = 0;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+        const uint32_t u = row2uid[i];
+        const bool rep = urow[u] == i;
+        const uint32_t lab = ulabel[u];
+        clone_id[i] = lab;
+        copies[i] = rep ? ucopies[u] : 0u;
+        // a duplicate keeps count 0 and is core only for minPts == 0
+        core[i] = rep ? (int32_t)ucore[u] : (int32_t)(min_pts == 0);
+        noise += lab == 0;
+    }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) noise += __shfl_xor_sync(0xFFFFFFFFu, noise, d);
+    if ((threadIdx.x & 31) == 0 && noise) atomicAdd(&ctr->n_noise_rows, noise);
+}
+
+__global__ void k_uniques_out(const Counters *__restrict__ ctr, const uint32_t *__restrict__ urow,
+                              uint32_t *__restrict__ out) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) out[u] = urow[u];
+}
+
+}  // namespace
+
+void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s) {
+    const uint64_t ecap = P.cap_edges;
+    const int ge = grid_for(ecap);
+    const int gu = grid_for(P.N);
+    cudaMemsetAsync(B.deg, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
+    cudaMemsetAsync(B.gcur, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
+    k_graph_init<<<gu, kThreads, 0, s>>>(B.ctr, B.ucopies, B.cnt, B.parent, B.bmin);
+    k_degree<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucopies, B.deg, B.cnt);
+    scan_u32(B.deg, B.goff, P.N + 1, nullptr, nullptr, B.scan_part, B.scan_part_cap, s);
+    k_fill_adj<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.goff, B.gcur, B.adj);
+    k_core<<<gu, kThreads, 0, s>>>(B.ctr, B.ctr, B.cnt, P.min_pts, B.ucore);
+    k_union<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.parent);
+    k_border<<<gu, kThreads, 0, s>>>(B.ctr, B.goff, B.adj, B.ucore, B.bmin);
+    if (trees) {
+        cudaMemsetAsync(B.depth_hist, 0, sizeof(uint32_t) * (kDepthMax + 1), s);
+        k_depth<<<gu, kThreads, 0, s>>>(P.N, B.row2uid, B.urow, B.ucore, B.bmin, B.parent,
+                                         B.depth_hist);
+    }
+    cudaMemsetAsync(B.rootflag, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
+    k_compress<<<gu, kThreads, 0, s>>>(B.ctr, B.ucore, B.parent, B.rootflag);
+    scan_u32(B.rootflag, B.rootflag, P.N + 1, nullptr, &B.ctr->n_clusters, B.scan_part,
+             B.scan_part_cap, s);
+    k_labels<<<gu, kThreads, 0, s>>>(B.ctr, B.ucore, B.parent, B.bmin, B.rootflag, B.urep,
+                                      B.uid_first, B.cnt);
+}
+
+void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s) {
+    const int gu = grid_for(P.N);
+    k_rows_out<<<gu, kThreads, 0, s>>>(P.N, P.min_pts, B.row2uid, B.urow, B.ucopies, B.ucore,
+                                        B.cnt, B.clone_id, B.core, B.copies, B.ctr);
+    if (B.uniques) k_uniques_out<<<gu, kThreads, 0, s>>>(B.ctr, B.urow, B.uniques);
+}
+
+}  // namespace idb

@@ -1,0 +1,160 @@
+/*
+ * immunodbscan_gb300.h -- C ABI of the GB300 (sm_103a) DBSCAN clone-collapsing
+ * path of immunodbscan.
+ *
+ * This is the drop-in for the reference's only host<->CUDA boundary, the
+ * constructor of InterlinkClass (cuda/Interlink.hpp:54-57, body
+ * cuda/Interlink.cu:34-95) and its getters (cuda/Interlink.hpp:59-67), called
+ * from TableHolderClass::do_the_clustering (cpp/TableHolder.hpp:340-343).
+ *
+ * Conventions
+ *  - Plain C types only; every entry point returns an idb_status (0 = success)
+ *    and never throws.  idb_last_error() returns the calling thread's message.
+ *  - Strings are passed as a byte blob plus int64 offsets (n+1 entries, blob
+ *    bytes [off[i], off[i+1]) are string i; strings hold no NUL terminator).
+ *  - The caller owns all memory.  Host entry points take host pointers and are
+ *    synchronous.  Device entry points take device pointers and run on the
+ *    context's stream.
+ *  - Results follow the reference's rules: same duplicate classes and copies,
+ *    same core flags,
+ *    same core partition and noise set, clone ids numbered by ascending minimum
+ *    core row index.  A border row (non-core, with core neighbours) joins the
+ *    cluster of its minimum-index core neighbour; the reference lets the first
+ *    of its core neighbours win a race (cuda/PSDBSCAN.hcu:113-122).
+ */
+#ifndef IMMUNODBSCAN_GB300_H
+#define IMMUNODBSCAN_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IDB_ABI_VERSION 1
+
+typedef enum idb_status {
+    IDB_OK = 0,
+    IDB_ERR_INVALID_ARG = 1,   /* NULL pointer, inconsistent sizes, bad enum      */
+    IDB_ERR_CUDA = 2,          /* a CUDA runtime call failed                      */
+    IDB_ERR_NO_DEVICE = 3,     /* no CUDA device / device is not sm_103           */
+    IDB_ERR_UNSUPPORTED = 4,   /* outside the documented limits                   */
+    IDB_ERR_OUT_OF_MEMORY = 5, /* device allocation failed / memory budget hit    */
+    IDB_ERR_CAPACITY = 6,      /* a replayed plan's capacities were exceeded      */
+    IDB_ERR_DEVICE_STALL = 7,  /* a bounded device-side wait gave up              */
+    IDB_ERR_REPLAN = 8         /* input no longer matches a captured plan         */
+} idb_status;
+
+typedef enum idb_alphabet {
+    IDB_ALPHABET_AUTO = 0,     /* derived from the bytes present (exact, any data) */
+} idb_alphabet;
+
+/* Clustering parameters (INFO keys of the reference, cpp/ConfigHolder.hpp:181-205). */
+typedef struct idb_params {
+    float    threshold;        /* maximum_relative_edit_distance (NaN = unused)    */
+    int32_t  abs_eps;          /* absolute eps (new key; < 0 = unused)             */
+    uint32_t min_pts;          /* minimum_number_of_neighbors (counts itself)      */
+    int32_t  use_hamming;      /* use_hamming                                      */
+    int32_t  eval_trees;       /* get_tree_depth_statistics                        */
+    int32_t  schedule;         /* 0 = static (pair-count) order, 1 = learned       */
+    int32_t  reserved[6];
+} idb_params;
+
+/* Input rows (cuda/Interlink.hpp:54-57: zip(V calls, J calls, sequences)). */
+typedef struct idb_input {
+    uint32_t n_rows;
+    /* V and J gene calls; NULL data = column not configured: every row matches
+       the single gene "V" (cpp/TableHolder.hpp:388-391, 406-409). */
+    const char    *v_calls;
+    const int64_t *v_offsets;
+    const char    *j_calls;
+    const int64_t *j_offsets;
+    /* sequences; NULL = every row is "Gene" (cpp/TableHolder.hpp:421-423) */
+    const char    *seqs;
+    const int64_t *seq_offsets;
+    /* reference gene names (cpp/GeneReader.hpp:65-76), host memory always */
+    const char    *v_genes;
+    const int64_t *v_gene_offsets;
+    uint32_t       n_v_genes;
+    const char    *j_genes;
+    const int64_t *j_gene_offsets;
+    uint32_t       n_j_genes;
+    /* independent repertoires: rows [rep_offsets[r], rep_offsets[r+1]) form
+       repertoire r (n_repertoires+1 entries, host memory); NULL = one.
+       Clone ids are numbered per repertoire. */
+    uint32_t        n_repertoires;
+    const uint32_t *rep_offsets;
+} idb_input;
+
+typedef struct idb_stats {
+    uint32_t n_uniques;
+    uint32_t n_cores;          /* core uniques                                     */
+    uint32_t n_clusters;
+    uint32_t n_noise_rows;
+    uint64_t pairs_evaluated;  /* distance evaluations performed by the kernels    */
+    uint64_t neighbour_pairs;  /* unique pairs that are neighbours (graph edges)   */
+    uint64_t n_entries;        /* bucket entries (unique x V gene x J gene)        */
+    uint64_t n_units;          /* scheduled work units                             */
+    double   ms_total;         /* device time of the whole call                    */
+    double   ms_distance;      /* device time of the distance kernel               */
+    double   ms_phase[8];      /* front+dedupe, buckets+schedule, distance, graph,
+                                  outputs (device time; eager calls include waits
+                                  on host read-backs)                              */
+    uint32_t kernel_launches;  /* kernels launched (graph replays)                 */
+    uint32_t reserved;
+} idb_stats;
+
+/* Outputs (cuda/Interlink.hpp:59-67).  clone_id/core/copies are required. */
+typedef struct idb_output {
+    uint32_t  *clone_id;        /* [n_rows] 0 = noise (get_clusters_iterator)      */
+    int32_t   *core;            /* [n_rows] 0/1 (get_cores_iterator)               */
+    uint32_t  *copies;          /* [n_rows] class size at the representative,
+                                   0 at duplicates (get_copies_iterator)           */
+    uint32_t  *uniques;         /* optional [n_rows]: ascending representative rows
+                                   (get_uniques_iterator)                          */
+    uint32_t  *n_uniques;       /* optional (get_n_uniques)                        */
+    uint32_t  *tree_depth_hist; /* optional [51]: union-find depth histogram
+                                   (cuda/PSDBSCAN.hcu:1020-1040)                   */
+    idb_stats *stats;           /* optional                                        */
+} idb_output;
+
+typedef struct idb_context idb_context;
+
+/* Context = device + stream + workspace.  One context per host thread. */
+idb_status idb_context_create(int device, idb_context **ctx);
+idb_status idb_context_destroy(idb_context *ctx);
+
+/* The InterlinkClass replacement: host inputs, host outputs, synchronous.
+   ctx may be NULL (a per-thread default context on device 0 is used, matching
+   the reference's implicit device 0, cuda/PSDBSCAN.hcu:977). */
+idb_status idb_cluster(idb_context *ctx, const idb_input *in, const idb_params *prm,
+                       idb_output *out);
+
+/* Same, with the row columns (calls, sequences and their offsets) and the
+   outputs in device memory.  Gene name lists and rep_offsets stay in host
+   memory.  Synchronous. */
+idb_status idb_cluster_device(idb_context *ctx, const idb_input *in, const idb_params *prm,
+                              idb_output *out);
+
+/* Batched, graph-captured path: plan once for a set of repertoires whose
+   device-resident columns stay at the same addresses, then replay.  The plan
+   sizes the workspace and captures the complete launch sequence (bitsets,
+   duplicate collapse, bucketing, one persistent distance launch over all
+   repertoires, graph, labels) into a CUDA graph; idb_batch_run replays it and
+   recomputes everything from the inputs.  If new data at the same addresses
+   exceeds the plan, idb_batch_run returns IDB_ERR_CAPACITY or IDB_ERR_REPLAN
+   and the caller plans again. */
+idb_status idb_batch_plan(idb_context *ctx, const idb_input *in, const idb_params *prm,
+                          const idb_output *out);
+idb_status idb_batch_run(idb_context *ctx, idb_stats *stats);
+
+/* Thread-local message of the last failing call ("" if none). */
+size_t idb_last_error(char *buf, size_t size);
+const char *idb_status_string(idb_status s);
+int idb_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMMUNODBSCAN_GB300_H */

@@ -1,0 +1,34 @@
+/*
+ * immunodbscan_gb300_diag.h -- measurement entry points of libimmunodbscan_gb300.
+ *
+ * These have no counterpart in the reference (its only boundary is
+ * InterlinkClass, cuda/Interlink.hpp:54-57).  They exist so that throughput can
+ * be reported against a schedule-independent numerator and a measured peak.
+ */
+#ifndef IMMUNODBSCAN_GB300_DIAG_H
+#define IMMUNODBSCAN_GB300_DIAG_H
+
+#include <stdint.h>
+
+#include "immunodbscan_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Measured 32-bit integer-logic throughput of `device` in Gop/s (lop3/add
+   chains, all SMs, best of 5 launches); *ms_out = duration of the best launch.
+   Returns 0 on success. */
+int idb_diag_int_peak(int device, double *gops_out, double *ms_out);
+
+/* Number of admissible unique pairs of the input: pairs of uniques (after the
+   duplicate collapse) in one repertoire whose V sets and J sets overlap and
+   whose length gap is admissible (equal lengths in Hamming mode, |Lx-Ly| <=
+   eps(Lx,Ly) otherwise), each pair counted once.  Host inputs as idb_cluster. */
+idb_status idb_count_admissible(idb_context *ctx, const idb_input *in, const idb_params *prm,
+                                uint64_t *pairs_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IMMUNODBSCAN_GB300_DIAG_H */

@@ -1,0 +1,204 @@
+"""GPU path (libimmunodbscan_gb300 through the C ABI) against the oracle.
+
+Integer work throughout, so the bar is bit-exact: clone ids, core flags and
+copies identical to the oracle (both use the minimum-index core neighbour for
+border rows), plus the reference-semantics check that every border label is one
+of the clusters the reference's first-wins race could have produced.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from immunodbscan_gb300 import DeviceBatch, IdbError, cluster_workload, synth
+from kat_cases import cases, no_seq_case
+
+pytestmark = pytest.mark.gpu
+
+
+def assert_same(gpu, ora, w, label=""):
+    assert np.array_equal(gpu.copies, ora.copies), f"{label}: copies differ"
+    assert np.array_equal(gpu.core, ora.core), f"{label}: core flags differ"
+    bad = np.nonzero(gpu.clone_id != ora.clone_id)[0]
+    assert bad.size == 0, (f"{label}: {bad.size} clone ids differ, first rows {bad[:8].tolist()} "
+                           f"gpu={gpu.clone_id[bad[:8]].tolist()} ora={ora.clone_id[bad[:8]].tolist()}")
+    assert gpu.n_uniques == ora.n_uniques
+    # reference semantics: a border row may carry any of its core neighbours' clusters
+    K = ora.cand.shape[1]
+    for i in np.nonzero(ora.n_cand > 1)[0][:2000]:
+        nc = int(ora.n_cand[i])
+        if nc <= K:
+            assert int(gpu.clone_id[i]) in ora.cand[i, :nc].tolist()
+
+
+@pytest.mark.parametrize("case", cases(), ids=lambda c: c["name"])
+def test_known_answers(gpu_ctx, case):
+    r = cluster_workload(case["w"], gpu_ctx)
+    assert r.clone_id.tolist() == case["clone"]
+    assert r.core.tolist() == case["core"]
+    assert r.copies.tolist() == case["copies"]
+
+
+def test_no_sequence_column(gpu_ctx):
+    w, want = no_seq_case()
+    r = cluster_workload(w, gpu_ctx, no_seq=True)
+    assert r.clone_id.tolist() == want["clone"]
+    assert r.core.tolist() == want["core"]
+    assert r.copies.tolist() == want["copies"]
+
+
+@pytest.mark.parametrize("k,scale", [(0, 1.0), (0, 0.2), (1, 0.03), (2, 0.004), (3, 0.01),
+                                     (4, 0.0015)])
+def test_workloads_vs_oracle(gpu_ctx, k, scale):
+    w = synth.workload(k, scale=scale)
+    g = cluster_workload(w, gpu_ctx)
+    o = oracle.cluster(w)
+    assert_same(g, o, w, f"workload{k}@{scale}")
+    assert g.stats.neighbour_pairs == o.neighbour_pairs
+    assert g.stats.n_clusters == o.n_clusters
+
+
+@pytest.mark.parametrize("k", [1, 3, 4])
+def test_relative_threshold_only(gpu_ctx, k):
+    w = synth.workload(k, scale=0.004 if k != 4 else 0.001)
+    w.abs_eps = -1
+    w.threshold = 0.15
+    g = cluster_workload(w, gpu_ctx)
+    o = oracle.cluster(w)
+    assert_same(g, o, w, f"relative{k}")
+
+
+@pytest.mark.parametrize("hamming", [True, False])
+def test_no_gene_columns(gpu_ctx, hamming):
+    w = synth.workload(0, scale=0.1)
+    w.use_hamming = hamming
+    g = cluster_workload(w, gpu_ctx, no_v=True, no_j=True)
+    o = oracle.cluster(w, no_v=True, no_j=True)
+    assert_same(g, o, w, "no genes")
+
+
+def _random_workload(rng, n, lo, hi, alphabet, hamming, eps, min_pts, n_fam=None):
+    fam = n_fam or max(n // 8, 1)
+    roots = [rng.choice(alphabet, size=int(rng.integers(lo, hi + 1))).astype(np.uint8).tobytes()
+             for _ in range(fam)]
+    seqs = []
+    for i in range(n):
+        s = bytearray(roots[int(rng.integers(0, fam))])
+        for _ in range(int(rng.poisson(1.0))):
+            p = int(rng.integers(0, len(s)))
+            s[p] = int(rng.choice(alphabet))
+        if not hamming and rng.random() < 0.2 and len(s) > lo:
+            del s[int(rng.integers(0, len(s)))]
+        seqs.append(bytes(s))
+    vg = [b"IGHV%d*" % g for g in range(1, 9)]
+    jg = [b"IGHJ%d*" % g for g in range(1, 4)]
+    vc = [b"IGHV%d*01, or IGHV%d*01" % (1 + rng.integers(0, 8), 1 + rng.integers(0, 8))
+          for _ in range(n)]
+    jc = [b"IGHJ%d*02" % (1 + rng.integers(0, 3)) for _ in range(n)]
+    return synth.from_strings(seqs, vc, jc, vg, jg, abs_eps=eps, min_pts=min_pts,
+                              use_hamming=hamming)
+
+
+@pytest.mark.parametrize("hamming", [True, False])
+@pytest.mark.parametrize("lo,hi", [(30, 40), (60, 70), (90, 128)])
+def test_multiword_lengths(gpu_ctx, hamming, lo, hi):
+    rng = np.random.default_rng(lo + hamming)
+    w = _random_workload(rng, 1500, lo, hi, list(b"ACDEFGHIKLMNPQRSTVWY"), hamming, 3, 2)
+    g = cluster_workload(w, gpu_ctx)
+    o = oracle.cluster(w)
+    assert_same(g, o, w, f"multiword {lo}-{hi}")
+
+
+@pytest.mark.parametrize("hamming", [True, False])
+def test_generic_alphabet(gpu_ctx, hamming):
+    """More than 32 distinct byte values: the generic (byte) kernels."""
+    rng = np.random.default_rng(7)
+    w = _random_workload(rng, 1200, 10, 20, list(range(33, 127)), hamming, 2, 2)
+    g = cluster_workload(w, gpu_ctx)
+    o = oracle.cluster(w)
+    assert_same(g, o, w, "generic alphabet")
+
+
+@pytest.mark.parametrize("hamming", [True, False])
+def test_generic_long(gpu_ctx, hamming):
+    """Sequences longer than 128: the generic kernels (Levenshtein up to 1024)."""
+    rng = np.random.default_rng(11)
+    w = _random_workload(rng, 400, 150, 300, list(b"ACGT"), hamming, 6, 2, n_fam=40)
+    g = cluster_workload(w, gpu_ctx)
+    o = oracle.cluster(w)
+    assert_same(g, o, w, "generic long")
+
+
+def test_nucleotide_two_planes(gpu_ctx):
+    w = synth.workload(1, scale=0.02)
+    w.use_hamming = True
+    g = cluster_workload(w, gpu_ctx)
+    o = oracle.cluster(w)
+    assert_same(g, o, w, "nt hamming")
+
+
+def test_deterministic_and_stats(gpu_ctx):
+    w = synth.workload(3, scale=0.01)
+    a = cluster_workload(w, gpu_ctx)
+    b = cluster_workload(w, gpu_ctx)
+    assert np.array_equal(a.clone_id, b.clone_id)
+    assert a.stats.n_uniques == b.stats.n_uniques
+    assert a.stats.pairs_evaluated == b.stats.pairs_evaluated
+    assert a.stats.pairs_evaluated >= a.stats.neighbour_pairs
+
+
+def test_tree_depth_histogram(gpu_ctx):
+    w = synth.workload(0, scale=0.3)
+    r = cluster_workload(w, gpu_ctx, eval_trees=True)
+    assert r.tree_depth_hist is not None
+    assert int(r.tree_depth_hist.sum()) == w.n
+
+
+def test_uniques_getter(gpu_ctx):
+    w = synth.workload(0, scale=0.1)
+    r = cluster_workload(w, gpu_ctx)
+    want = np.nonzero(r.copies)[0]
+    assert np.array_equal(r.uniques[: r.n_uniques], want)
+
+
+def test_empty_and_single(gpu_ctx):
+    w = synth.from_strings([], None, None, [], [], abs_eps=1, min_pts=2, use_hamming=True)
+    r = cluster_workload(w, gpu_ctx)
+    assert r.clone_id.size == 0
+    w = synth.from_strings([b"CARDY"], None, None, [], [], abs_eps=1, min_pts=1, use_hamming=True)
+    r = cluster_workload(w, gpu_ctx)
+    assert r.clone_id.tolist() == [1] and r.core.tolist() == [1] and r.copies.tolist() == [1]
+
+
+def test_invalid_arguments(gpu_ctx):
+    w = synth.workload(0, scale=0.01)
+    w.abs_eps = -1
+    w.threshold = math.nan
+    with pytest.raises(IdbError) as e:
+        cluster_workload(w, gpu_ctx)
+    assert e.value.status == 1
+
+
+def test_batch_graph_matches_plain(gpu_ctx):
+    w = synth.workload(2, scale=0.003)
+    plain = cluster_workload(w, gpu_ctx)
+    b = DeviceBatch(w, gpu_ctx)
+    b.plan()
+    for _ in range(2):
+        st = b.run()
+        clone, core, copies = b.results()
+        assert np.array_equal(clone, plain.clone_id)
+        assert np.array_equal(core, plain.core)
+        assert np.array_equal(copies, plain.copies)
+        assert st.n_uniques == plain.stats.n_uniques
+
+
+def test_device_api_matches_host_api(gpu_ctx):
+    w = synth.workload(1, scale=0.01)
+    plain = cluster_workload(w, gpu_ctx)
+    b = DeviceBatch(w, gpu_ctx)
+    b.cluster_once()
+    clone, core, copies = b.results()
+    assert np.array_equal(clone, plain.clone_id)
+    assert np.array_equal(copies, plain.copies)

@@ -1,0 +1,88 @@
+"""The CPU oracle against the hand-derived known answers (rules S1-S7).
+
+These pin the oracle (the reference ships no tests or fixtures; its CUDA path
+cannot run here), which then serves as the checker for the GPU path.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from kat_cases import S1_CALLS, S1_GENES, S1_WORDS, S2_TABLE, cases, no_seq_case
+
+
+def test_s1_gene_bitsets():
+    got = oracle.gene_bitsets(S1_CALLS, S1_GENES)
+    assert got.tolist() == S1_WORDS
+
+
+def test_s1_width_is_ceil_genes_over_32():
+    genes = [b"G%d*" % g for g in range(40)]
+    got = oracle.gene_bitsets([b"xG39*", b"G0*G1*"], genes)
+    assert got.shape == (2, 2)
+    assert got[0].tolist() == [0, 1 << 7]
+    assert got[1].tolist() == [3, 0]
+
+
+@pytest.mark.parametrize("lx,ly,t,a,want", S2_TABLE)
+def test_s2_eps(lx, ly, t, a, want):
+    assert oracle.eps(lx, ly, t, a) == want
+
+
+def test_s4_distances():
+    assert oracle.levenshtein(b"kitten", b"sitting") == 3
+    assert oracle.levenshtein(b"ACDEFGHIKL", b"ACDFGHIKLM") == 2
+    assert oracle.levenshtein(b"ACDEFGHIK", b"ACDFGHIKLM") == 3
+    assert oracle.levenshtein(b"ACDFGHIKLM", b"ACDEFGHIKLMN") == 2
+    assert oracle.levenshtein(b"", b"ABC") == 3
+    assert oracle.hamming(b"ACDFGHIKLM", b"ACDEFGHIKL") == 7
+
+
+@pytest.mark.parametrize("case", cases(), ids=lambda c: c["name"])
+def test_known_answers(case):
+    r = oracle.cluster(case["w"])
+    assert r.clone_id.tolist() == case["clone"]
+    assert r.core.tolist() == case["core"]
+    assert r.copies.tolist() == case["copies"]
+    for row, labels in case["cand"].items():
+        assert r.n_cand[row] == len(labels)
+        assert sorted(r.cand[row, : len(labels)].tolist()) == labels
+
+
+def test_no_sequence_column():
+    w, want = no_seq_case()
+    r = oracle.cluster(w, no_seq=True)
+    assert r.clone_id.tolist() == want["clone"]
+    assert r.core.tolist() == want["core"]
+    assert r.copies.tolist() == want["copies"]
+
+
+def test_no_gene_columns_equals_single_gene_v():
+    from immunodbscan_gb300 import synth
+    w = synth.workload(0, scale=0.05)
+    a = oracle.cluster(w, no_v=True, no_j=True)
+    w2 = synth.from_strings([w.seq(i) for i in range(w.n)], None, None, [], [],
+                            abs_eps=w.abs_eps, min_pts=w.min_pts, use_hamming=w.use_hamming)
+    b = oracle.cluster(w2)
+    assert np.array_equal(a.clone_id, b.clone_id)
+    assert np.array_equal(a.copies, b.copies)
+
+
+def test_invariants_workload0():
+    """Properties that hold for any input: copies sum to the row count, duplicates
+    carry copies 0 and follow their representative, labels are dense 1..K."""
+    from immunodbscan_gb300 import synth
+    w = synth.workload(0, scale=0.2)
+    r = oracle.cluster(w)
+    assert int(r.copies.sum()) == w.n
+    assert (r.copies > 0).sum() == r.n_uniques
+    labs = np.unique(r.clone_id[r.clone_id > 0])
+    assert labs.tolist() == list(range(1, r.n_clusters + 1))
+    # core rows are representatives (minPts > 0) and are never noise
+    assert np.all(r.copies[r.core == 1] > 0)
+    assert np.all(r.clone_id[r.core == 1] > 0)
+    # labels ascend with the first core row of each cluster
+    first = {}
+    for i in np.nonzero(r.core)[0]:
+        first.setdefault(int(r.clone_id[i]), int(i))
+    order = [first[k] for k in sorted(first)]
+    assert order == sorted(order)
