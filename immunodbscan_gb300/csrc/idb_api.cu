@@ -210,7 +210,14 @@ struct Pipeline {
 };
 
 void record(Pipeline &pl, int k) {
-    if (pl.timing) cudaEventRecord(pl.c->ev[k], pl.c->stream);
+    if (pl.timing) launch_stamp(&pl.B.ctr->stamp[k], pl.c->stream);
+}
+
+// phase durations from the device time stamps (ms)
+void phase_times(const Counters &h, idb_stats *st) {
+    for (int k = 0; k < 5; ++k)
+        st->ms_phase[k] = h.stamp[k + 1] > h.stamp[k] ? 1e-6 * (double)(h.stamp[k + 1] - h.stamp[k]) : 0.0;
+    st->ms_distance = st->ms_phase[2];
 }
 
 // Stage 0: inputs in place, counters zeroed, survey run and read back.
@@ -559,14 +566,8 @@ idb_status fill_stats(Pipeline &pl, idb_stats *st) {
     st->n_entries = h.n_entries;
     st->n_units = h.n_units;
     if (pl.timing) {
-        float ms = 0;
-        for (int k = 0; k < 5; ++k) {
-            cudaEventElapsedTime(&ms, pl.c->ev[k], pl.c->ev[k + 1]);
-            st->ms_phase[k] = ms;
-        }
-        cudaEventElapsedTime(&ms, pl.c->ev[0], pl.c->ev[5]);
-        st->ms_total = ms;
-        st->ms_distance = st->ms_phase[2];
+        phase_times(h, st);
+        st->ms_total = h.stamp[5] > h.stamp[0] ? 1e-6 * (double)(h.stamp[5] - h.stamp[0]) : 0.0;
     }
     return IDB_OK;
 }
@@ -575,6 +576,7 @@ idb_status cluster_impl(idb_context *c, const idb_input *in, const idb_params *p
                         idb_output *out, bool host_io) {
     TRY(validate(in, prm, out));
     CU(cudaSetDevice(c->device));
+    cudaGetLastError();   // a stale error of an unrelated call must not fail this one
     Pipeline pl;
     pl.c = c;
     pl.trees = prm->eval_trees != 0 && out->tree_depth_hist != nullptr;
@@ -776,8 +778,9 @@ idb_status idb_batch_plan(idb_context *c, const idb_input *in, const idb_params 
     CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(pl.B.ctr, 0, sizeof(Counters), s);
     cudaMemsetAsync(&pl.B.ctr->lmin, 0xFF, sizeof(uint32_t), s);
+    pl.timing = true;   // time-stamp kernels between the phases
+    record(pl, 0);
     launch_survey(pl.P, pl.B, s);
-    pl.timing = true;   // event-record nodes between the phases
     idb_status st = run_phases(pl, false);
     cudaGraph_t g = nullptr;
     cudaError_t ce = cudaStreamEndCapture(s, &g);
@@ -814,7 +817,7 @@ idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
     cudaStream_t s = c->stream;
     CU(cudaEventRecord(c->ev[0], s));
     CU(cudaGraphLaunch(c->exec, s));
-    CU(cudaEventRecord(c->ev[6], s));
+    CU(cudaEventRecord(c->ev[1], s));
     CU(cudaMemcpyAsync(c->h_ctr, c->bufs.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
     TRY(device_errors(*c->h_ctr));
@@ -830,13 +833,9 @@ idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
         stats->n_entries = h.n_entries;
         stats->n_units = h.n_units;
         float ms = 0;
-        cudaEventElapsedTime(&ms, c->ev[0], c->ev[6]);
+        CU(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
         stats->ms_total = ms;
-        for (int k = 0; k < 5; ++k) {
-            cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]);
-            stats->ms_phase[k] = ms;
-        }
-        stats->ms_distance = stats->ms_phase[2];
+        phase_times(h, stats);
         stats->kernel_launches = c->graph_kernels;
     }
     return IDB_OK;

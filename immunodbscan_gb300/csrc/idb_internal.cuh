@@ -47,6 +47,7 @@ struct Counters {
     uint32_t heavy_count;
     unsigned long long pairs_evaluated;
     unsigned long long admissible_pairs;
+    unsigned long long stamp[8];  // %globaltimer at the phase boundaries (ns)
     uint32_t pad[4];
 };
 
@@ -153,6 +154,7 @@ struct Buffers {
 // ---- launchers (each enqueues on `s`, never synchronises) ----
 void launch_survey(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_check_plan(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_stamp(unsigned long long *dst, cudaStream_t s);
 void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream_t s);
 void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s);

@@ -41,6 +41,7 @@ __global__ void __launch_bounds__(256) k_int_probe(uint32_t iters, uint32_t seed
 extern "C" int idb_diag_int_peak(int device, double *gops_out, double *ms_out) {
     if (!gops_out) return 1;
     if (cudaSetDevice(device) != cudaSuccess) return 3;
+    cudaGetLastError();
     int sms = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     int per_sm = 0;

@@ -349,6 +349,14 @@ k_scan_down(const uint32_t *in, uint32_t *out, uint32_t n_host, const uint32_t *
     }
 }
 
+// Phase time stamps: the device's global nanosecond timer, written by a
+// one-thread kernel between phases (works inside a captured graph).
+__global__ void k_stamp(unsigned long long *dst) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *dst = t;
+}
+
 // A replayed plan is only valid while lengths and byte values stay inside the
 // ones it was built for.
 struct PlanShape {
@@ -390,6 +398,8 @@ void scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, const uint32_t *n_d
     k_scan_parts<<<1, 1024, 0, s>>>(part, nb, total);
     k_scan_down<<<nb, kScanThreads, 0, s>>>(in, out, n, n_dev, part);
 }
+
+void launch_stamp(unsigned long long *dst, cudaStream_t s) { k_stamp<<<1, 1, 0, s>>>(dst); }
 
 void launch_check_plan(const Plan &P, const Buffers &B, cudaStream_t s) {
     PlanShape ps;
