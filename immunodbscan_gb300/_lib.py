@@ -68,6 +68,8 @@ SIGNATURES = {
     "idb_last_error": (C.c_size_t, [C.c_char_p, C.c_size_t]),
     "idb_status_string": (C.c_char_p, [C.c_int]),
     "idb_abi_version": (C.c_int, []),
+    "idb_dedupe_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                     C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "idb_diag_int_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "idb_count_admissible": (C.c_int, [C.c_void_p, C.POINTER(Input), C.POINTER(Params),
                                        C.POINTER(C.c_uint64)]),

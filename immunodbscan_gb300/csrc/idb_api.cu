@@ -647,6 +647,8 @@ idb_status get_ctx(idb_context **pc) {
 }  // namespace
 
 namespace idb {
+void set_last_error(const char *msg) { g_err = msg ? msg : ""; }
+
 int sm_count() {
     static thread_local int dev = -1, n = 0;
     int d = 0;

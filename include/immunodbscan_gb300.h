@@ -149,6 +149,33 @@ idb_status idb_batch_plan(idb_context *ctx, const idb_input *in, const idb_param
                           const idb_output *out);
 idb_status idb_batch_run(idb_context *ctx, idb_stats *stats);
 
+/* No-allocation duplicate collapse.  This entry point has no counterpart in
+   the reference; it serves callers that cannot allocate device memory (for
+   example a host whose GPU memory is owned by another allocator, or a serving
+   loop that may not call cudaMalloc/cudaFree because they synchronise the
+   device).  It performs the duplicate-collapse step of the path (rows are
+   duplicates iff they have equal length, equal V and J bitsets when given, and
+   equal bytes): rep_out[i] = the minimum row of i's class, copies_out[i] = the
+   class size at that row and 0 elsewhere -- the copies column idb_cluster
+   returns for the same rows.  Inputs and outputs are caller-owned device
+   memory; v_bits / j_bits (n_rows x v_words / j_words uint64 words, bit g =
+   reference gene g) may be NULL.  Its hash table lives in a fixed ~5 MB
+   __device__ array inside the library, which every GPU that loads the library
+   holds until the process exits; at most IDB_DEDUPE_NOALLOC_MAX_ROWS rows
+   (larger inputs are rejected with IDB_ERR_UNSUPPORTED).  Runs on the calling
+   thread's current device and on `stream` (a cudaStream_t, NULL = legacy
+   default stream) and returns when the results are complete.  The first call
+   on a device resolves the array's address (cudaGetSymbolAddress); make that
+   first call before any stream capture.  All calls on a device share the
+   array, which keeps the last call's contents (each call resets it first):
+   calls that overlap on the GPU race and must be serialised by the caller.
+   Calls no cudaMalloc, cudaFree or allocating library routine. */
+#define IDB_DEDUPE_NOALLOC_MAX_ROWS (1u << 18)
+idb_status idb_dedupe_noalloc(const char *seqs, const int64_t *seq_offsets,
+                              const uint64_t *v_bits, uint32_t v_words,
+                              const uint64_t *j_bits, uint32_t j_words, uint32_t n_rows,
+                              uint32_t *rep_out, uint32_t *copies_out, void *stream);
+
 /* Thread-local message of the last failing call ("" if none). */
 size_t idb_last_error(char *buf, size_t size);
 const char *idb_status_string(idb_status s);
