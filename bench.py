@@ -53,7 +53,9 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-rows", type=int, default=60000)
+    ap.add_argument("--cpu-seconds", type=float, default=None,
+                    help="CPU time budget of the oracle sample (per step for --impl reference; "
+                         "default 10 s, or 150 s / steps for the reference arm)")
     return ap.parse_args()
 
 
@@ -136,28 +138,39 @@ def allreduce_max(world, x: float) -> float:
     return float(t.item())
 
 
-def cpu_sample(w, rows: int):
-    """The smallest prefix of repertoires (in order of size) holding about `rows` rows."""
-    sizes = np.diff(w.rep_off)
-    order = np.argsort(sizes, kind="stable")
-    pick, total = [], 0
+def _pick(sizes, order, rate, seconds):
+    pick, budget = [], 0.0
     for r in order:
-        if total >= rows:
+        cost = sizes[r] ** 2 / rate
+        if pick and budget + cost > seconds:
             break
         pick.append(int(r))
-        total += int(sizes[r])
-    pick.sort()
-    return w.subset_repertoires(pick), pick
+        budget += cost
+    return sorted(pick)
 
 
-def run_cpu(w, rows: int, threads: int):
+def run_cpu(w, seconds: float, threads: int):
+    """Oracle on the smallest repertoires that fill about `seconds` of CPU time.
+
+    The oracle visits every pair of uniques of a repertoire, so its cost grows
+    with the sum of squared repertoire sizes; the rate is calibrated on the
+    smallest repertoire and refined once on the first full sample."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
-    sub, pick = cpu_sample(w, rows)
-    oracle.lib()
+    sizes = np.diff(w.rep_off).astype(np.float64)
+    order = np.argsort(sizes, kind="stable")
     t0 = time.perf_counter()
-    r = oracle.cluster(sub, n_threads=threads, max_candidates=0)
-    dt = time.perf_counter() - t0
+    oracle.cluster(w.subset_repertoires([int(order[0])]), n_threads=threads, max_candidates=0)
+    rate = sizes[order[0]] ** 2 / max(time.perf_counter() - t0, 1e-3)
+    for attempt in range(3):
+        pick = _pick(sizes, order, rate, seconds)
+        sub = w.subset_repertoires(pick)
+        t0 = time.perf_counter()
+        r = oracle.cluster(sub, n_threads=threads, max_candidates=0)
+        dt = time.perf_counter() - t0
+        if dt >= 0.5 * seconds or len(pick) == len(order):
+            break
+        rate = float(np.sum(sizes[pick] ** 2)) / max(dt, 1e-3)
     return dict(value=r.admissible_pairs / dt / 1e9, seq_per_s=sub.n / dt, seconds=dt,
                 rows=sub.n, reps=len(pick), pairs=r.admissible_pairs)
 
@@ -166,12 +179,12 @@ def reference_arm(args, world, rank, w):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    rows = max(args.cpu_rows // 2, 5000)
-    for _ in range(max(args.warmup, 0) and 1):
-        run_cpu(w, min(rows, 5000), threads)
+    if args.warmup > 0:
+        run_cpu(w, 0.5, threads)
     vals, secs = [], []
+    per_step = args.cpu_seconds or min(10.0, 150.0 / max(args.steps, 1))
     for _ in range(args.steps):
-        res = run_cpu(w, rows, threads)
+        res = run_cpu(w, per_step, threads)
         vals.append(res["value"])
         secs.append(res["seconds"])
     value = float(np.median(vals))
@@ -271,12 +284,19 @@ def main():
     L.idb_diag_int_peak(local, C.byref(gops), C.byref(pms))
     ops_pair = ops_per_pair(w, batch)
     t_dist = float(np.mean(ms_dist)) * 1e-3
-    achieved = ops_pair * last.pairs_evaluated / t_dist / 1e9 if t_dist > 0 else 0.0
+    if w.use_hamming:
+        work_ops = ops_pair * last.pairs_evaluated
+    else:                       # Myers/Hyyro: ops per text column actually consumed
+        work_ops = ops_pair * last.lev_columns
+    achieved = work_ops / t_dist / 1e9 if t_dist > 0 else 0.0
     out["roofline"] = {"bound": "int", "achieved": achieved, "peak": gops.value,
                        "unit": "Gop/s (32-bit integer logic)",
                        "frac": achieved / gops.value if gops.value else None,
                        "traffic": None, "kernel": "k_hamming" if w.use_hamming else "k_levenshtein",
-                       "ops_per_pair": ops_pair, "kernel_ms": t_dist * 1e3,
+                       "ops_per_unit": ops_pair,
+                       "work_unit": "pair" if w.use_hamming else "pair-column (text residue)",
+                       "work_units": int(last.pairs_evaluated if w.use_hamming else last.lev_columns),
+                       "kernel_ms": t_dist * 1e3,
                        "peak_source": "measured: idb_diag_int_peak (lop3/add chains, all SMs)"}
 
     # e2e through idb_cluster with pinned host buffers
@@ -331,7 +351,7 @@ def main():
                         "batched_speedup": pm / step_ms, "identical_partitions": bool(same)}
 
     if rank == 0 and not args.no_cpu:
-        res = run_cpu(w, args.cpu_rows, os.cpu_count() or 1)
+        res = run_cpu(w, args.cpu_seconds or 10.0, os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": res["value"], "unit": UNIT, "cores": os.cpu_count(),
                                "kind": "port",
                                "sample": f"{res['reps']} smallest repertoires ({res['rows']} rows, "
@@ -347,7 +367,9 @@ def ops_per_pair(w, batch) -> int:
 
     Hamming (bit planes): one LOP3 per plane word folds XOR and OR, then the
     population test (eps==1: x & (x-1) == 0 -> 2 ops + 1 compare; otherwise
-    popc + add per word + 1 compare).  Levenshtein: ~16 ops per text column.
+    popc + add per word + 1 compare).  Levenshtein: ops per text column per
+    32-residue pattern word of the Myers/Hyyro step (Peq load, 4 LOP3, add,
+    2 shifts/or, 2 LOP3 -> 16 with the code extraction).
     """
     L = int(w.lengths().max())
     Wd = max(1, (L + 31) // 32)
@@ -356,7 +378,7 @@ def ops_per_pair(w, batch) -> int:
         if Wd == 1 and w.abs_eps == 1 and math.isnan(w.threshold):
             return planes + 3
         return planes * Wd + 2 * Wd + 1
-    return 16 * int(np.mean(w.lengths()))
+    return 16 * Wd
 
 
 def build_host_input(w, pinned: bool):

@@ -46,7 +46,8 @@ class Stats(C.Structure):
                 ("n_noise_rows", C.c_uint32), ("pairs_evaluated", C.c_uint64),
                 ("neighbour_pairs", C.c_uint64), ("n_entries", C.c_uint64), ("n_units", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_distance", C.c_double), ("ms_phase", C.c_double * 8),
-                ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32)]
+                ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32),
+                ("lev_columns", C.c_uint64)]
 
 
 class Output(C.Structure):
@@ -71,6 +72,8 @@ SIGNATURES = {
     "idb_dedupe_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                      C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
     "idb_diag_int_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "idb_diag_gene_bits": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                     C.c_void_p, C.c_uint32, C.c_void_p]),
     "idb_count_admissible": (C.c_int, [C.c_void_p, C.POINTER(Input), C.POINTER(Params),
                                        C.POINTER(C.c_uint64)]),
 }

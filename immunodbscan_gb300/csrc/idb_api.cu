@@ -69,7 +69,7 @@ enum BufId {
     bURow, bUCopies, bULen, bURep, bBinHist, bBinCursor, bEntUid, bEntRec, bBpCount, bBp,
     bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bDeg, bGOff, bGCur, bAdj, bCnt, bUCore,
     bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
-    bCtr, bNumBufs
+    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bNumBufs
 };
 
 }  // namespace
@@ -183,19 +183,44 @@ idb_status validate(const idb_input *in, const idb_params *prm, const idb_output
     return IDB_OK;
 }
 
-// Gene name lists -> device (host memory always).
+// Gene name lists -> device (host memory always), plus the hash table of the
+// names used by the gene-bitset kernel.
 idb_status upload_genes(idb_context *c, const char *names, const int64_t *off, uint32_t G,
-                        BufId blob_id, BufId off_id, uint32_t *bytes_out) {
+                        BufId blob_id, BufId off_id, BufId tab_id, uint32_t *bytes_out,
+                        GeneMatcher *gm) {
     std::vector<int32_t> o(G + 1);
     const int64_t base = G ? off[0] : 0;
     for (uint32_t g = 0; g <= G; ++g) o[g] = (int32_t)(off[g] - base);
     const size_t nb = G ? (size_t)(off[G] - base) : 0;
+    // table: slots >= 2*G, power of two
+    *gm = GeneMatcher();
+    uint32_t ts = 16;
+    while (ts < 2 * G) ts <<= 1;
+    std::vector<GeneEntry> tab(ts, GeneEntry{0, 0, 0});
+    for (uint32_t g = 0; g < G; ++g) {
+        const uint32_t L = (uint32_t)(o[g + 1] - o[g]);
+        if (L == 0) continue;                         // an empty name never matches
+        if (L > 255) { gm->long_names = 1; continue; }
+        const uint8_t *nm = reinterpret_cast<const uint8_t *>(names + base + o[g]);
+        uint32_t h = 0;
+        for (uint32_t k = 0; k < L; ++k) h = h * kGeneHashMul + nm[k];
+        uint32_t sl = h & (ts - 1);
+        while (tab[sl].len != 0) sl = (sl + 1) & (ts - 1);
+        tab[sl] = GeneEntry{h, (uint16_t)L, (uint16_t)g};
+        gm->firstmask[nm[0] >> 5] |= 1u << (nm[0] & 31);
+        gm->lenmask[L >> 5] |= 1u << (L & 31);
+        gm->maxlen = std::max(gm->maxlen, L);
+    }
+    gm->ts = ts;
     TRY(ensure(c, blob_id, nb + 16));
     TRY(ensure(c, off_id, sizeof(int32_t) * (G + 1)));
+    TRY(ensure(c, tab_id, sizeof(GeneEntry) * ts));
     if (nb) CU(cudaMemcpyAsync(c->buf[blob_id].p, names + base, nb, cudaMemcpyHostToDevice, c->stream));
     CU(cudaMemcpyAsync(c->buf[off_id].p, o.data(), sizeof(int32_t) * (G + 1), cudaMemcpyHostToDevice,
                        c->stream));
-    CU(cudaStreamSynchronize(c->stream));   // o is a local
+    CU(cudaMemcpyAsync(c->buf[tab_id].p, tab.data(), sizeof(GeneEntry) * ts, cudaMemcpyHostToDevice,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));   // o and tab are locals
     *bytes_out = (uint32_t)nb;
     return IDB_OK;
 }
@@ -278,10 +303,15 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
     // gene lists
     P.Gv = P.no_v ? 1 : in->n_v_genes;
     P.Gj = P.no_j ? 1 : in->n_j_genes;
-    if (!P.no_v) TRY(upload_genes(c, in->v_genes, in->v_gene_offsets, P.Gv, bVGenes, bVGOff, &P.gene_bytes_v));
-    if (!P.no_j) TRY(upload_genes(c, in->j_genes, in->j_gene_offsets, P.Gj, bJGenes, bJGOff, &P.gene_bytes_j));
+    if (!P.no_v)
+        TRY(upload_genes(c, in->v_genes, in->v_gene_offsets, P.Gv, bVGenes, bVGOff, bVTab,
+                         &P.gene_bytes_v, &P.vmatch));
+    if (!P.no_j)
+        TRY(upload_genes(c, in->j_genes, in->j_gene_offsets, P.Gj, bJGenes, bJGOff, bJTab,
+                         &P.gene_bytes_j, &P.jmatch));
     B.vgenes = ptr<uint8_t>(c, bVGenes); B.vg_off = ptr<int32_t>(c, bVGOff);
     B.jgenes = ptr<uint8_t>(c, bJGenes); B.jg_off = ptr<int32_t>(c, bJGOff);
+    B.vtab = ptr<GeneEntry>(c, bVTab); B.jtab = ptr<GeneEntry>(c, bJTab);
     P.VW = P.Gv > 64 ? (P.Gv + 63) / 64 : 1;
     P.JW = P.Gj > 64 ? (P.Gj + 63) / 64 : 1;
     if (P.Gv == 0) P.Gv = 1;   // a V column with an empty reference list: all bitsets 0
@@ -367,7 +397,10 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
     P.hamming_eps_mode = 0;
     if (P.hamming && emin_same == emax_same && emin_same == 1) P.hamming_eps_mode = 1;
     if (P.hamming && emin_same == emax_same && emin_same == 0) P.hamming_eps_mode = 2;
-    P.nbins = (uint64_t)P.R * P.Gv * P.Gj * P.NL;
+    P.K = 4;
+    P.big_group = 64;
+    P.sig_exact = P.Gv <= 64 && P.Gj <= 32;
+    P.nbins = (uint64_t)P.R * P.Gv * P.Gj * P.NL * P.K;
     if (P.nbins >= (1ull << 31))
         return fail(IDB_ERR_UNSUPPORTED, "too many buckets (repertoires x V genes x J genes x lengths = %llu)",
                     (unsigned long long)P.nbins);
@@ -403,6 +436,8 @@ idb_status alloc_fixed(Pipeline &pl) {
     TRY(ensure(c, bURep, 4 * N1));
     TRY(ensure(c, bBinHist, 4 * (P.nbins + 1)));
     TRY(ensure(c, bBinCursor, 4 * (P.nbins + 1)));
+    TRY(ensure(c, bSigAnd, 16 * (P.nbins + 1)));
+    TRY(ensure(c, bUClass, 4 * N1));
     TRY(ensure(c, bBpCount, 4 * (P.nbins + 1)));
     TRY(ensure(c, bClsHist, 4 * 130));
     TRY(ensure(c, bDeg, 4 * N1));
@@ -427,6 +462,7 @@ idb_status alloc_fixed(Pipeline &pl) {
     B.urow = ptr<uint32_t>(c, bURow); B.ucopies = ptr<uint32_t>(c, bUCopies);
     B.ulen = ptr<uint32_t>(c, bULen); B.urep = ptr<uint32_t>(c, bURep);
     B.bin_hist = ptr<uint32_t>(c, bBinHist); B.bin_cursor = ptr<uint32_t>(c, bBinCursor);
+    B.sig_and = ptr<unsigned long long>(c, bSigAnd); B.uclass = ptr<uint32_t>(c, bUClass);
     B.bp_count = ptr<uint32_t>(c, bBpCount); B.cls_hist = ptr<uint32_t>(c, bClsHist);
     B.deg = ptr<uint32_t>(c, bDeg); B.goff = ptr<uint32_t>(c, bGOff); B.gcur = ptr<uint32_t>(c, bGCur);
     B.cnt = ptr<uint32_t>(c, bCnt); B.ucore = ptr<uint32_t>(c, bUCore);
@@ -442,6 +478,8 @@ idb_status alloc_entries(Pipeline &pl, uint64_t n_entries) {
     pl.P.cap_entries = std::max<uint64_t>(n_entries, 1);
     TRY(ensure(c, bEntUid, 4 * pl.P.cap_entries));
     TRY(ensure(c, bEntRec, (size_t)pl.P.RS * pl.P.cap_entries));
+    TRY(ensure(c, bEntMeta, 16 * pl.P.cap_entries));
+    pl.B.ent_meta = ptr<uint4>(c, bEntMeta);
     pl.B.ent_uid = ptr<uint32_t>(c, bEntUid);
     pl.B.ent_rec = ptr<uint4>(c, bEntRec);
     return IDB_OK;
@@ -565,6 +603,7 @@ idb_status fill_stats(Pipeline &pl, idb_stats *st) {
     st->neighbour_pairs = h.n_edges;
     st->n_entries = h.n_entries;
     st->n_units = h.n_units;
+    st->lev_columns = h.lev_columns;
     if (pl.timing) {
         phase_times(h, st);
         st->ms_total = h.stamp[5] > h.stamp[0] ? 1e-6 * (double)(h.stamp[5] - h.stamp[0]) : 0.0;
@@ -834,12 +873,53 @@ idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
         stats->neighbour_pairs = h.n_edges;
         stats->n_entries = h.n_entries;
         stats->n_units = h.n_units;
+        stats->lev_columns = h.lev_columns;
         float ms = 0;
         CU(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
         stats->ms_total = ms;
         phase_times(h, stats);
         stats->kernel_launches = c->graph_kernels;
     }
+    return IDB_OK;
+}
+
+idb_status idb_diag_gene_bits(idb_context *c, const char *calls, const int64_t *offsets,
+                              uint32_t n_rows, const char *genes, const int64_t *gene_offsets,
+                              uint32_t n_genes, uint64_t *words_out) {
+    TRY(get_ctx(&c));
+    if (!calls || !offsets || !words_out || (n_genes && (!genes || !gene_offsets)))
+        return fail(IDB_ERR_INVALID_ARG, "NULL argument");
+    if (n_genes > 64u * kMaxGeneWords)
+        return fail(IDB_ERR_UNSUPPORTED, "at most %d genes", 64 * kMaxGeneWords);
+    if (n_rows == 0) return IDB_OK;
+    CU(cudaSetDevice(c->device));
+    cudaGetLastError();
+    Pipeline pl;
+    pl.c = c;
+    Plan &P = pl.P;
+    Buffers &B = pl.B;
+    P.N = n_rows;
+    P.no_v = false;
+    P.Gv = n_genes;
+    P.VW = n_genes > 64 ? (n_genes + 63) / 64 : 1;
+    const size_t nbytes = (size_t)offsets[n_rows];
+    TRY(ensure(c, bV, nbytes + 16));
+    TRY(ensure(c, bVOff, sizeof(int64_t) * ((size_t)n_rows + 1)));
+    TRY(ensure(c, bVBits, sizeof(uint64_t) * n_rows * P.VW));
+    if (nbytes) CU(cudaMemcpyAsync(c->buf[bV].p, calls, nbytes, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemcpyAsync(c->buf[bVOff].p, offsets, sizeof(int64_t) * ((size_t)n_rows + 1),
+                       cudaMemcpyHostToDevice, c->stream));
+    TRY(upload_genes(c, genes, gene_offsets, n_genes, bVGenes, bVGOff, bVTab, &P.gene_bytes_v,
+                     &P.vmatch));
+    B.vcall = ptr<uint8_t>(c, bV); B.v_off = ptr<int64_t>(c, bVOff);
+    B.vgenes = ptr<uint8_t>(c, bVGenes); B.vg_off = ptr<int32_t>(c, bVGOff);
+    B.vtab = ptr<GeneEntry>(c, bVTab);
+    B.vbits = ptr<uint64_t>(c, bVBits);
+    launch_gene_bits(P, B, true, c->stream);
+    TRY(check_launch());
+    CU(cudaMemcpyAsync(words_out, B.vbits, sizeof(uint64_t) * n_rows * P.VW, cudaMemcpyDeviceToHost,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));
     return IDB_OK;
 }
 

@@ -29,6 +29,22 @@ enum : uint32_t {
     kErrEntryOverflow = 128u,
 };
 
+// Gene-name lookup table (built on the host per call): open addressing on the
+// rolling hash h = h*kGeneHashMul + byte of a name; len 0 marks an empty slot.
+constexpr uint32_t kGeneHashMul = 0x01000193u;
+struct GeneEntry {
+    uint32_t h;
+    uint16_t len;
+    uint16_t gene;
+};
+struct GeneMatcher {
+    uint32_t ts = 0;             // table slots (power of two), 0 = no table
+    uint32_t maxlen = 0;         // longest name
+    uint32_t firstmask[8] = {};  // bytes that start some name
+    uint32_t lenmask[8] = {};    // name lengths present (1..255)
+    uint32_t long_names = 0;     // a name longer than 255 bytes exists
+};
+
 // Device-resident counters of one clustering call (one struct, zeroed first).
 struct Counters {
     uint32_t lmax, lmin;
@@ -48,6 +64,7 @@ struct Counters {
     unsigned long long pairs_evaluated;
     unsigned long long admissible_pairs;
     unsigned long long stamp[8];  // %globaltimer at the phase boundaries (ns)
+    unsigned long long lev_columns;  // text columns consumed by live Levenshtein pairs
     uint32_t pad[4];
 };
 
@@ -75,6 +92,7 @@ struct Plan {
     uint32_t N = 0, R = 1;
     uint32_t Gv = 1, Gj = 1, VW = 1, JW = 1;     // genes and uint64 words per column
     uint32_t gene_bytes_v = 0, gene_bytes_j = 0; // bytes of the reference name lists
+    GeneMatcher vmatch, jmatch;
     bool no_v = true, no_j = true, no_seq = false;
     bool hamming = false;
     uint32_t min_pts = 2;
@@ -83,10 +101,13 @@ struct Plan {
     bool fast = true;
     uint32_t RS = 16;                             // record bytes per entry
     int dLmax = 0;                                // largest admissible length gap
-    uint64_t nbins = 0;
+    uint64_t nbins = 0;                           // sub-buckets (bins x K classes)
+    uint32_t K = 4;                               // classes per bin
+    uint32_t big_group = 64;                      // call-group size that gets its own class
     uint32_t TX = 256, TY = 256, RX = 8;          // unit shape (entries)
     int schedule = 0;
     int hamming_eps_mode = 0;                     // 0 popcount, 1 eps==1, 2 eps==0
+    bool sig_exact = true;                        // V genes <= 64 and J genes <= 32
     uint8_t codemap[256];
     int first_byte = -1;                          // byte value with code 0
     // capacities
@@ -101,6 +122,7 @@ struct Buffers {
     const uint8_t *jcall = nullptr; const int64_t *j_off = nullptr;
     const uint8_t *vgenes = nullptr; const int32_t *vg_off = nullptr;
     const uint8_t *jgenes = nullptr; const int32_t *jg_off = nullptr;
+    const GeneEntry *vtab = nullptr, *jtab = nullptr;
     const uint32_t *rep_off = nullptr;              // [R+1]
     const int16_t *eps_tab = nullptr;               // [NL*NL]
     const uint8_t *codemap = nullptr;               // [256]
@@ -117,7 +139,10 @@ struct Buffers {
     // bins
     uint32_t *bin_hist = nullptr;                   // [nbins+1] -> bin_start
     uint32_t *bin_cursor = nullptr;                 // [nbins]
+    uint32_t *uclass = nullptr;                     // [N] sub-bucket class per unique
+    unsigned long long *sig_and = nullptr;          // [2*nbins] AND of V / J signatures
     uint32_t *ent_uid = nullptr;                    // [cap_entries]
+    uint4 *ent_meta = nullptr;                      // [cap_entries] {sigV lo, sigV hi, sigJ, uid}
     uint4 *ent_rec = nullptr;                       // [cap_entries * RS/16]
     uint32_t *bp_count = nullptr;                   // [nbins+1]
     BinPair *bp = nullptr, *bp_sorted = nullptr;    // [cap_binpairs]

@@ -11,6 +11,16 @@
 // bin, or between the bins of one (repertoire, V, J) whose lengths are within
 // the threshold, are ever evaluated.  Bins are laid out densely with the length
 // fastest, so the partner bin of length L+g is the bin index + g.
+//
+// Each bin is further split into kKeyClasses sub-buckets: class 0 holds the
+// uniques of small call groups, classes 1.. hold the uniques of large groups
+// of identical (V set, J set) -- the members of a big clonal family.  Every
+// sub-bucket keeps the AND of its entries' signatures (the genes each entry
+// has below the bin's V gene and below its J gene).  A pair of sub-buckets whose
+// signature ANDs intersect shares a lower gene in every pair, so none of its
+// pairs is canonical here and the pair of sub-buckets is not scheduled: a
+// family's internal pairs are evaluated once, in its lowest (V, J) bin, and not
+// again in each of the |V|*|J| bins it occupies.
 #include "idb_internal.cuh"
 
 namespace idb {
@@ -28,17 +38,87 @@ inline int grid_for(uint64_t n, int threads = kThreads) {
 }
 
 struct BinGeom {
-    uint32_t Gv, Gj, NL, Lmin, VW, JW;
+    uint32_t Gv, Gj, NL, Lmin, VW, JW, K;
     __device__ __forceinline__ bool in_range(uint32_t L) const { return L >= Lmin && L - Lmin < NL; }
-    __device__ __forceinline__ uint32_t bin(uint32_t r, uint32_t v, uint32_t j, uint32_t L) const {
-        return ((r * Gv + v) * Gj + j) * NL + (L - Lmin);
+    // sub-bucket index: ((((r*Gv + v)*Gj + j)*NL + L-Lmin)*K + class
+    __device__ __forceinline__ uint32_t bin(uint32_t r, uint32_t v, uint32_t j, uint32_t L,
+                                            uint32_t c) const {
+        return (((r * Gv + v) * Gj + j) * NL + (L - Lmin)) * K + c;
     }
 };
+
+// genes of `bits` (first word) below gene index g
+__device__ __forceinline__ uint64_t below(uint64_t word0, uint32_t g) {
+    return g >= 64 ? word0 : (word0 & ((1ull << g) - 1ull));
+}
+
+// ---------------------------------------------------------------------------
+// Call groups: uniques with identical (repertoire, length, V bits, J bits).
+// Open addressing on the (reset) duplicate table; a group of >= kBigGroup
+// members gets class 1 + (slot % (K-1)), all others class 0.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool same_group(const uint64_t *vbits, const uint64_t *jbits,
+                                           uint32_t VW, uint32_t JW, uint32_t ra, uint32_t rb) {
+    for (uint32_t w = 0; w < VW; ++w)
+        if (vbits[(size_t)ra * VW + w] != vbits[(size_t)rb * VW + w]) return false;
+    for (uint32_t w = 0; w < JW; ++w)
+        if (jbits[(size_t)ra * JW + w] != jbits[(size_t)rb * JW + w]) return false;
+    return true;
+}
+
+__global__ void k_group_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
+                               const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
+                               const uint64_t *__restrict__ vbits, const uint64_t *__restrict__ jbits,
+                               uint32_t *table, uint32_t *tcount, uint32_t *uslot, uint64_t mask) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t row = urow[u], L = ulen[u], r = urep[u];
+        uint64_t h = mix64(0xA0761D6478BD642Full + r, L);
+        for (uint32_t w = 0; w < g.VW; ++w) h = mix64(h, vbits[(size_t)row * g.VW + w]);
+        for (uint32_t w = 0; w < g.JW; ++w) h = mix64(h, jbits[(size_t)row * g.JW + w]);
+        uint64_t sl = h & mask;
+        uint32_t it = 0;
+        for (;; ++it) {
+            if (it > mask || it >= kSpinCap) {
+                atomicOr(&ctr->error, kErrHashStall);
+                sl = kNone;
+                break;
+            }
+            uint32_t cur = *((volatile uint32_t *)&table[sl]);
+            if (cur == kNone) {
+                const uint32_t prev = atomicCAS(&table[sl], kNone, u);
+                if (prev == kNone) break;
+                cur = prev;
+            }
+            if (urep[cur] == r && ulen[cur] == L &&
+                same_group(vbits, jbits, g.VW, g.JW, urow[cur], row))
+                break;
+            sl = (sl + 1) & mask;
+        }
+        uslot[u] = (uint32_t)sl;
+        if (sl != kNone) atomicAdd(&tcount[sl], 1u);
+    }
+}
+
+__global__ void k_group_class(const Counters *__restrict__ ctr, const uint32_t *__restrict__ uslot,
+                              const uint32_t *__restrict__ tcount, uint32_t K, uint32_t big,
+                              uint32_t *__restrict__ uclass) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t sl = uslot[u];
+        uint32_t c = 0;
+        if (K > 1 && sl != kNone && tcount[sl] >= big) c = 1 + (uint32_t)(mix64(sl, 7) % (K - 1));
+        uclass[u] = c;
+    }
+}
 
 // Entries per unique: |V bits| * |J bits|, one histogram increment per entry.
 __global__ void k_bin_hist(BinGeom g, const Counters *__restrict__ ctr,
                            const uint32_t *__restrict__ urow, const uint32_t *__restrict__ ulen,
-                           const uint32_t *__restrict__ urep, const uint64_t *__restrict__ vbits,
+                           const uint32_t *__restrict__ urep, const uint32_t *__restrict__ uclass,
+                           const uint64_t *__restrict__ vbits,
                            const uint64_t *__restrict__ jbits, uint32_t *__restrict__ hist) {
     const uint32_t nu = ctr->n_uniques;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -57,7 +137,7 @@ __global__ void k_bin_hist(BinGeom g, const Counters *__restrict__ ctr,
                         const uint32_t j = jw * 64 + lowest_bit64(jb);
                         jb &= jb - 1;
                         if (j >= g.Gj) break;
-                        atomicAdd(&hist[g.bin(r, v, j, L)], 1u);
+                        atomicAdd(&hist[g.bin(r, v, j, L, uclass[u])], 1u);
                     }
                 }
             }
@@ -74,11 +154,14 @@ __global__ void k_bin_hist(BinGeom g, const Counters *__restrict__ ctr,
 // equality of bytes.
 __global__ void k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                            const uint32_t *__restrict__ urow, const uint32_t *__restrict__ ulen,
-                           const uint32_t *__restrict__ urep, const uint64_t *__restrict__ vbits,
+                           const uint32_t *__restrict__ urep, const uint32_t *__restrict__ uclass,
+                           unsigned long long *__restrict__ sig_and,
+                           const uint64_t *__restrict__ vbits,
                            const uint64_t *__restrict__ jbits, const uint8_t *__restrict__ seq,
                            const int64_t *__restrict__ seq_off, const uint8_t *__restrict__ codemap,
                            const uint32_t *__restrict__ bin_start, uint32_t *__restrict__ cursor,
                            uint32_t *__restrict__ ent_uid, uint4 *__restrict__ ent_rec,
+                           uint4 *__restrict__ ent_meta,
                            uint32_t rs16, int planes, uint32_t W, uint64_t cap_entries,
                            uint32_t *err) {
     __shared__ uint8_t cm[256];
@@ -102,10 +185,16 @@ __global__ void k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                         const uint32_t j = jw * 64 + lowest_bit64(jb);
                         jb &= jb - 1;
                         if (j >= g.Gj) break;
-                        const uint32_t b = g.bin(r, v, j, L);
+                        const uint32_t b = g.bin(r, v, j, L, uclass[u]);
+                        const uint64_t sv = below(vbits[(size_t)row * g.VW], v);
+                        const uint64_t sj = below(jbits[(size_t)row * g.JW], j);
+                        atomicAnd(&sig_and[2 * (size_t)b], sv);
+                        atomicAnd(&sig_and[2 * (size_t)b + 1], sj);
                         const uint64_t pos = (uint64_t)bin_start[b] + atomicAdd(&cursor[b], 1u);
                         if (pos >= cap_entries) { atomicOr(err, kErrEntryOverflow); continue; }
                         ent_uid[pos] = u;
+                        // side record: signature below (v, j) and the unique id
+                        ent_meta[pos] = make_uint4((uint32_t)sv, (uint32_t)(sv >> 32), (uint32_t)sj, u);
                         uint4 *dst = ent_rec + pos * rs16;
                         if (planes > 0) {
                             // bit planes, written word by word (16 bytes at a time)
@@ -150,10 +239,12 @@ __global__ void k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
     }
 }
 
-// Bin pairs: (bin, bin+g) for every admissible length gap g (eps(L,L+g) >= g;
-// Hamming compares equal lengths only, cuda/PSDBSCAN.hcu:615).
+// Bin pairs: sub-bucket pairs (b,c) x (b+g,c') for every admissible length gap
+// g (eps(L,L+g) >= g; Hamming compares equal lengths only,
+// cuda/PSDBSCAN.hcu:615); for g = 0 only c <= c'.  Pairs whose signature ANDs
+// intersect hold no canonical pair and are left out.
 struct PairGeom {
-    uint32_t NL, Lmin, Gv, Gj;
+    uint32_t NL, Lmin, Gv, Gj, K;
     int dLmax;
     bool hamming;
     uint32_t TX, TY, q;
@@ -167,58 +258,69 @@ __device__ __forceinline__ bool pair_ok(const PairGeom &pg, const int16_t *eps_t
     return e >= gap;
 }
 
-__global__ void k_binpairs_count(uint32_t nbins, PairGeom pg, const int16_t *__restrict__ eps_tab,
-                                 const uint32_t *__restrict__ bin_start, uint32_t *__restrict__ cnt) {
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += stride) {
-        const uint32_t nA = bin_start[b + 1] - bin_start[b];
-        uint32_t c = 0;
-        if (nA > 0) {
-            const uint32_t li = b % pg.NL;
-            for (int g = 0; g <= pg.dLmax; ++g) {
-                if (!pair_ok(pg, eps_tab, li, g)) continue;
-                const uint32_t nB = bin_start[b + g + 1] - bin_start[b + g];
-                if (nB == 0) continue;
-                if (g == 0 && nA < 2) continue;
-                ++c;
-            }
-        }
-        cnt[b] = c;
-    }
+__device__ __forceinline__ bool sig_disjoint(const unsigned long long *sig, uint32_t a, uint32_t b) {
+    return ((sig[2 * (size_t)a] & sig[2 * (size_t)b]) | (sig[2 * (size_t)a + 1] & sig[2 * (size_t)b + 1])) == 0;
 }
 
-__global__ void k_binpairs_fill(uint32_t nbins, PairGeom pg, const int16_t *__restrict__ eps_tab,
+template <bool FILL>
+__device__ __forceinline__ uint32_t visit_pairs(uint32_t sb, const PairGeom &pg,
+                                                const int16_t *eps_tab, const uint32_t *bin_start,
+                                                const unsigned long long *sig, BinPair *out,
+                                                uint32_t k, uint64_t cap_bp, uint32_t *err) {
+    const uint32_t a0 = bin_start[sb], nA = bin_start[sb + 1] - a0;
+    if (nA == 0) return 0;
+    const uint32_t b = sb / pg.K, c = sb % pg.K;
+    const uint32_t li = b % pg.NL;
+    uint32_t n = 0;
+    for (int g = 0; g <= pg.dLmax; ++g) {
+        if (!pair_ok(pg, eps_tab, li, g)) continue;
+        for (uint32_t c2 = (g == 0 ? c : 0); c2 < pg.K; ++c2) {
+            const uint32_t sb2 = (b + g) * pg.K + c2;
+            const uint32_t b0 = bin_start[sb2], nB = bin_start[sb2 + 1] - b0;
+            if (nB == 0) continue;
+            const bool same = g == 0 && c2 == c;
+            if (same && nA < 2) continue;
+            if (!sig_disjoint(sig, sb, sb2)) continue;
+            if (FILL) {
+                const uint32_t kk = k + n;
+                if (kk >= cap_bp) { atomicOr(err, kErrBinPairOverflow); ++n; continue; }
+                const uint32_t rest = b / pg.NL;
+                BinPair P;
+                P.a_start = a0; P.a_n = nA; P.b_start = b0; P.b_n = nB;
+                P.unit_base = 0;
+                P.ncx = (nA + pg.TX - 1) / pg.TX;
+                P.la = (uint16_t)(pg.Lmin + li); P.lb = (uint16_t)(pg.Lmin + li + g);
+                P.v = (uint16_t)((rest / pg.Gj) % pg.Gv); P.j = (uint16_t)(rest % pg.Gj);
+                P.eps = eps_tab[(size_t)li * pg.NL + li + g];
+                P.same = same;
+                const uint64_t cost = same ? (uint64_t)nA * (nA - 1) / 2 : (uint64_t)nA * nB;
+                P.cls = (uint8_t)(cost ? 63 - __clzll((long long)cost) : 0);
+                P.cost_lo = (uint32_t)min(cost, (uint64_t)0xFFFFFFFFu);
+                out[kk] = P;
+            }
+            ++n;
+        }
+    }
+    return n;
+}
+
+__global__ void k_binpairs_count(uint32_t nsub, PairGeom pg, const int16_t *__restrict__ eps_tab,
+                                 const uint32_t *__restrict__ bin_start,
+                                 const unsigned long long *__restrict__ sig,
+                                 uint32_t *__restrict__ cnt) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t sb = blockIdx.x * blockDim.x + threadIdx.x; sb < nsub; sb += stride)
+        cnt[sb] = visit_pairs<false>(sb, pg, eps_tab, bin_start, sig, nullptr, 0, 0, nullptr);
+}
+
+__global__ void k_binpairs_fill(uint32_t nsub, PairGeom pg, const int16_t *__restrict__ eps_tab,
                                 const uint32_t *__restrict__ bin_start,
+                                const unsigned long long *__restrict__ sig,
                                 const uint32_t *__restrict__ bp_off, uint64_t cap_bp,
                                 BinPair *__restrict__ out, uint32_t *err) {
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t b = blockIdx.x * blockDim.x + threadIdx.x; b < nbins; b += stride) {
-        const uint32_t a0 = bin_start[b], nA = bin_start[b + 1] - a0;
-        if (nA == 0) continue;
-        uint32_t k = bp_off[b];
-        const uint32_t li = b % pg.NL;
-        const uint32_t rest = b / pg.NL;
-        const uint32_t j = rest % pg.Gj, v = (rest / pg.Gj) % pg.Gv;
-        for (int g = 0; g <= pg.dLmax; ++g) {
-            if (!pair_ok(pg, eps_tab, li, g)) continue;
-            const uint32_t b0 = bin_start[b + g], nB = bin_start[b + g + 1] - b0;
-            if (nB == 0) continue;
-            if (g == 0 && nA < 2) continue;
-            if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); ++k; continue; }
-            BinPair P;
-            P.a_start = a0; P.a_n = nA; P.b_start = b0; P.b_n = nB;
-            P.unit_base = 0;
-            P.ncx = (nA + pg.TX - 1) / pg.TX;
-            P.la = (uint16_t)(pg.Lmin + li); P.lb = (uint16_t)(pg.Lmin + li + g);
-            P.v = (uint16_t)v; P.j = (uint16_t)j;
-            P.eps = eps_tab[(size_t)li * pg.NL + li + g];
-            P.same = g == 0;
-            const uint64_t cost = g == 0 ? (uint64_t)nA * (nA - 1) / 2 : (uint64_t)nA * nB;
-            P.cls = (uint8_t)(cost ? 63 - __clzll((long long)cost) : 0);
-            P.cost_lo = (uint32_t)min(cost, (uint64_t)0xFFFFFFFFu);
-            out[k++] = P;
-        }
-    }
+    for (uint32_t sb = blockIdx.x * blockDim.x + threadIdx.x; sb < nsub; sb += stride)
+        visit_pairs<true>(sb, pg, eps_tab, bin_start, sig, out, bp_off[sb], cap_bp, err);
 }
 
 // Schedule: heavy bin pairs first (counting sort on log2 of the cost, cost =
@@ -281,38 +383,49 @@ __global__ void k_set_unit_base(const Counters *__restrict__ ctr, BinPair *__res
 }  // namespace
 
 void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
-    BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW};
+    BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
     const uint32_t nb = (uint32_t)P.nbins;
+    // call groups (the duplicate table is free again once the uniques exist)
+    cudaMemsetAsync(B.table, 0xFF, sizeof(uint32_t) * (B.table_mask + 1), s);
+    cudaMemsetAsync(B.tcount, 0, sizeof(uint32_t) * (B.table_mask + 1), s);
+    k_group_insert<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.vbits,
+                                                       B.jbits, B.table, B.tcount, B.slot,
+                                                       B.table_mask);
+    k_group_class<<<grid_for(P.N), kThreads, 0, s>>>(B.ctr, B.slot, B.tcount, P.K, P.big_group,
+                                                      B.uclass);
     cudaMemsetAsync(B.bin_hist, 0, sizeof(uint32_t) * (P.nbins + 1), s);
-    k_bin_hist<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.vbits,
-                                                    B.jbits, B.bin_hist);
+    k_bin_hist<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.uclass,
+                                                    B.vbits, B.jbits, B.bin_hist);
     scan_u32(B.bin_hist, B.bin_hist, nb + 1, nullptr, &B.ctr->n_entries, B.scan_part,
              B.scan_part_cap, s);
 }
 
 void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
-    BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW};
+    BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
     cudaMemsetAsync(B.bin_cursor, 0, sizeof(uint32_t) * P.nbins, s);
+    cudaMemsetAsync(B.sig_and, 0xFF, sizeof(unsigned long long) * 2 * P.nbins, s);
     const int planes = (P.fast && P.hamming) ? (int)P.B : 0;
     k_bin_fill<<<grid_for(P.N), kThreads, 0, s>>>(
-        g, B.ctr, B.urow, B.ulen, B.urep, B.vbits, B.jbits, B.seq, B.seq_off, B.codemap,
-        B.bin_hist, B.bin_cursor, B.ent_uid, B.ent_rec, P.RS / 16, planes, P.W, P.cap_entries,
-        &B.ctr->error);
+        g, B.ctr, B.urow, B.ulen, B.urep, B.uclass, B.sig_and, B.vbits, B.jbits, B.seq, B.seq_off,
+        B.codemap, B.bin_hist, B.bin_cursor, B.ent_uid, B.ent_rec, B.ent_meta, P.RS / 16, planes, P.W,
+        P.cap_entries, &B.ctr->error);
 }
 
 void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s) {
-    PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
+    PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.K, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
     const uint32_t nb = (uint32_t)P.nbins;
-    k_binpairs_count<<<grid_for(nb), kThreads, 0, s>>>(nb, pg, B.eps_tab, B.bin_hist, B.bp_count);
+    k_binpairs_count<<<grid_for(nb), kThreads, 0, s>>>(nb, pg, B.eps_tab, B.bin_hist, B.sig_and,
+                                                        B.bp_count);
     scan_u32(B.bp_count, B.bp_count, nb, nullptr, &B.ctr->n_binpairs, B.scan_part,
              B.scan_part_cap, s);
 }
 
 void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
-    PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
+    PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.K, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
     const uint32_t nb = (uint32_t)P.nbins;
-    k_binpairs_fill<<<grid_for(nb), kThreads, 0, s>>>(nb, pg, B.eps_tab, B.bin_hist, B.bp_count,
-                                                       P.cap_binpairs, B.bp, &B.ctr->error);
+    k_binpairs_fill<<<grid_for(nb), kThreads, 0, s>>>(nb, pg, B.eps_tab, B.bin_hist, B.sig_and,
+                                                       B.bp_count, P.cap_binpairs, B.bp,
+                                                       &B.ctr->error);
 }
 
 void launch_schedule(const Plan &P, const Buffers &B, cudaStream_t s) {

@@ -50,6 +50,8 @@ struct DistArgs {
     Counters *ctr;
     unsigned long long *bp_cycles;   // optional per bin-pair cycle log
     uint32_t *bp_hits;
+    const uint4 *meta;               // per entry {sigV lo, sigV hi, sigJ, uid}
+    int sig_exact;                   // signatures decide canonicity exactly
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -185,15 +187,73 @@ __device__ __forceinline__ void finish(const DistArgs &a, EdgeWriter &ew, uint64
 }
 
 // ---------------------------------------------------------------------------
+// Neighbour hits of one y against the calling lane's x-entries (bit r of `hit`
+// = x-entry xbase + 32*r + lane).  Kept out of line: hits are rare, and the
+// hot loops stay small enough for the instruction cache.
+// ---------------------------------------------------------------------------
+__device__ __noinline__ void emit_hits(const DistArgs &a, EdgeWriter &ew, uint32_t hit,
+                                       uint32_t a_start, uint32_t xbase, uint32_t y_entry,
+                                       uint32_t ypos, uint32_t same, uint32_t v, uint32_t j,
+                                       int lane) {
+    uint32_t any = __reduce_or_sync(0xFFFFFFFFu, hit);
+    const uint32_t uy = a.ent_uid[y_entry];
+    while (any) {
+        const int r = __ffs(any) - 1;
+        any &= any - 1;
+        const uint32_t xpos = xbase + 32u * r + lane;
+        bool ok = (hit >> r) & 1u;
+        if (ok && same && ypos <= xpos) ok = false;
+        uint32_t ux = 0;
+        if (ok) {
+            ux = a.ent_uid[a_start + xpos];
+            const uint32_t rx = a.urow[ux], ry = a.urow[uy];
+            ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)v &&
+                 lowest_common(a.jbits, a.JW, rx, ry) == (int)j;
+        }
+        ew.append(a, lane, ok, min(ux, uy), max(ux, uy));
+    }
+}
+
+// Same, with the entries' side records in shared memory: the canonical test is
+// (sig_x & sig_y) == 0 over the genes below the bin's V and J gene, and the
+// unique ids come with the records, so a hit reads no global memory.
+__device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, uint32_t hit,
+                                            const uint4 *xm, uint4 ym, uint32_t xbase,
+                                            uint32_t ypos, uint32_t same, uint32_t v, uint32_t j,
+                                            int lane) {
+    uint32_t any = __reduce_or_sync(0xFFFFFFFFu, hit);
+    while (any) {
+        const int r = __ffs(any) - 1;
+        any &= any - 1;
+        const uint32_t xpos = xbase + 32u * r + lane;
+        bool ok = (hit >> r) & 1u;
+        if (ok && same && ypos <= xpos) ok = false;
+        const uint4 m = xm[32 * r + lane];
+        if (ok) {
+            if (a.sig_exact) {
+                ok = ((m.x & ym.x) | (m.y & ym.y) | (m.z & ym.z)) == 0;
+            } else {
+                const uint32_t rx = a.urow[m.w], ry = a.urow[ym.w];
+                ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)v &&
+                     lowest_common(a.jbits, a.JW, rx, ry) == (int)j;
+            }
+        }
+        ew.append(a, lane, ok, min(m.w, ym.w), max(m.w, ym.w));
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Hamming, fast path.  BP planes x W words per record; RX x-entries per lane.
 // EM: 0 = popcount test, 1 = eps == 1 (d & (d-1)) == 0, 2 = eps == 0.
 // ---------------------------------------------------------------------------
 template <int BP, int W, int RX, int EM>
-__global__ void __launch_bounds__(kWarps * 32)
+__global__ void __launch_bounds__(kWarps * 32, (W == 1 ? 5 : 4))
 k_hamming(DistArgs a) {
     constexpr int NW = BP * W;                 // words per record used
     constexpr int R16 = (NW + 3) / 4;          // 16-byte words per record
     __shared__ uint4 sy[kWarps][kYB * R16];
+    __shared__ uint4 sym[kWarps][kYB];            // y side records
+    __shared__ uint4 sxm[kWarps][32 * RX];        // x side records
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
     EdgeWriter ew;
@@ -201,81 +261,79 @@ k_hamming(DistArgs a) {
     uint64_t pairs = 0;
     Unit U;
     while (next_unit(a, n_units, n_bp, lane, U)) {
-        uint32_t x[RX][R16 * 4];
-        uint32_t xpos[RX];
-        bool xval[RX];
+        uint32_t x[RX][NW];
+        uint32_t valid = 0;
 #pragma unroll
         for (int r = 0; r < RX; ++r) {
-            xpos[r] = U.xbase + r * 32 + lane;
-            xval[r] = xpos[r] < U.xbase + U.nx;
-            const uint4 *src = a.rec + (size_t)(U.P.a_start + (xval[r] ? xpos[r] : U.xbase)) * R16;
+            const uint32_t xi = (uint32_t)r * 32 + lane;
+            const bool ok = xi < U.nx;
+            valid |= (uint32_t)ok << r;
+            const uint4 *src = a.rec + (size_t)(U.P.a_start + U.xbase + (ok ? xi : 0)) * R16;
 #pragma unroll
             for (int q = 0; q < R16; ++q) {
                 const uint4 v = __ldg(src + q);
-                x[r][4 * q + 0] = v.x; x[r][4 * q + 1] = v.y;
-                x[r][4 * q + 2] = v.z; x[r][4 * q + 3] = v.w;
+                const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (4 * q + e < NW) x[r][4 * q + e] = w4[e];
             }
-            if (xval[r]) pairs += unit_pairs(U, xpos[r]);
+            if (ok) pairs += unit_pairs(U, U.xbase + xi);
+            sxm[wid][xi] = __ldg(a.meta + U.P.a_start + U.xbase + (ok ? xi : 0));
         }
         const int eps = U.P.eps;
-        const uint32_t yrow0 = (U.P.same ? U.P.a_start : U.P.b_start) + U.ybase;
+        const uint32_t same = U.P.same;
+        const uint32_t yrow0 = (same ? U.P.a_start : U.P.b_start) + U.ybase;
         for (uint32_t yb = 0; yb < U.ny; yb += kYB) {
             const uint32_t nb = min((uint32_t)kYB, U.ny - yb);
             const uint4 *src = a.rec + (size_t)(yrow0 + yb) * R16;
             for (uint32_t t = lane; t < nb * R16; t += 32) sy[wid][t] = __ldg(src + t);
+            for (uint32_t t = lane; t < nb; t += 32) sym[wid][t] = __ldg(a.meta + yrow0 + yb + t);
             __syncwarp();
             for (uint32_t t = 0; t < nb; ++t) {
                 // x-entries before this y (all of them unless the bin pairs with itself)
                 const uint32_t yp = U.ybase + yb + t;
                 uint32_t nact = U.nx;
-                if (U.P.same) nact = yp > U.xbase ? min(U.nx, yp - U.xbase) : 0u;
+                if (same) nact = yp > U.xbase ? min(U.nx, yp - U.xbase) : 0u;
                 if (nact == 0) continue;
-                uint32_t y[R16 * 4];
+                uint32_t y[NW];
 #pragma unroll
                 for (int q = 0; q < R16; ++q) {
                     const uint4 v = sy[wid][t * R16 + q];
-                    y[4 * q + 0] = v.x; y[4 * q + 1] = v.y; y[4 * q + 2] = v.z; y[4 * q + 3] = v.w;
+                    const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                    for (int e = 0; e < 4; ++e)
+                        if (4 * q + e < NW) y[4 * q + e] = w4[e];
                 }
                 uint32_t hit = 0;
 #pragma unroll
                 for (int r = 0; r < RX; ++r) {
-                    if ((uint32_t)r * 32 >= nact) break;   // warp-uniform
-                    bool h;
-                    if (W == 1) {
-                        uint32_t d = x[r][0] ^ y[0];
+                    if ((uint32_t)r * 32 < nact) {   // warp-uniform
+                        bool h;
+                        if (W == 1) {
+                            uint32_t d = x[r][0] ^ y[0];
 #pragma unroll
-                        for (int p = 1; p < BP; ++p) d |= x[r][p] ^ y[p];
-                        if (EM == 2) h = d == 0;
-                        else if (EM == 1) h = (d & (d - 1)) == 0;
-                        else h = __popc(d) <= eps;
-                    } else {
-                        int dist = 0;
+                            for (int p = 1; p < BP; ++p) d |= x[r][p] ^ y[p];
+                            if (EM == 2) h = d == 0;
+                            else if (EM == 1) h = (d & (d - 1)) == 0;
+                            else h = __popc(d) <= eps;
+                        } else {
+                            int dist = 0;
 #pragma unroll
-                        for (int w = 0; w < W; ++w) {
-                            uint32_t d = x[r][w] ^ y[w];
+                            for (int w = 0; w < W; ++w) {
+                                uint32_t d = x[r][w] ^ y[w];
 #pragma unroll
-                            for (int p = 1; p < BP; ++p) d |= x[r][p * W + w] ^ y[p * W + w];
-                            dist += __popc(d);
+                                for (int p = 1; p < BP; ++p) d |= x[r][p * W + w] ^ y[p * W + w];
+                                dist += __popc(d);
+                            }
+                            h = dist <= eps;
                         }
-                        h = dist <= eps;
-                    }
-                    hit |= (uint32_t)(h && xval[r]) << r;
-                }
-                if (__any_sync(0xFFFFFFFFu, hit)) {
-                    const uint32_t ypos = U.ybase + yb + t;
-                    const uint32_t uy = a.ent_uid[yrow0 + yb + t];
-#pragma unroll
-                    for (int r = 0; r < RX; ++r) {
-                        bool ok = (hit >> r) & 1u;
-                        uint32_t ux = 0;
-                        if (ok && U.P.same && ypos <= xpos[r]) ok = false;
-                        if (ok) {
-                            ux = a.ent_uid[U.P.a_start + xpos[r]];
-                            ok = canonical(a, U.P, ux, uy);
-                        }
-                        ew.append(a, lane, ok, min(ux, uy), max(ux, uy));
+                        hit |= (uint32_t)h << r;
                     }
                 }
+                hit &= valid;
+                if (__any_sync(0xFFFFFFFFu, hit))
+                    emit_hits_meta(a, ew, hit, sxm[wid], sym[wid][t], U.xbase, yp, same, U.P.v,
+                                   U.P.j, lane);
             }
             __syncwarp();
         }
@@ -288,19 +346,22 @@ k_hamming(DistArgs a) {
 // pattern <= 32*W residues; RX patterns per lane.
 // ---------------------------------------------------------------------------
 template <int W, int RX>
-__global__ void __launch_bounds__(kWarps * 32)
+__global__ void __launch_bounds__(kWarps * 32, 4)
 k_levenshtein(DistArgs a) {
     extern __shared__ uint32_t smem[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t A = a.A;
     const uint32_t peq_words = RX * A * W * 32;          // per warp
     const uint32_t ybuf_words = kYB * a.rs16 * 4;        // per warp
-    uint32_t *peq = smem + wid * (peq_words + ybuf_words);
+    const uint32_t meta_words = (kYB + 32 * RX) * 4;     // per warp
+    uint32_t *peq = smem + wid * (peq_words + ybuf_words + meta_words);
     uint4 *sy = reinterpret_cast<uint4 *>(peq + peq_words);
+    uint4 *sym = sy + kYB * a.rs16;                      // y side records
+    uint4 *sxm = sym + kYB;                              // x side records
     const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
     EdgeWriter ew;
     ew.init();
-    uint64_t pairs = 0;
+    uint64_t pairs = 0, cols = 0;
     Unit U;
     while (next_unit(a, n_units, n_bp, lane, U)) {
         const int m = U.P.la, n = U.P.lb, eps = U.P.eps;
@@ -314,6 +375,7 @@ k_levenshtein(DistArgs a) {
         for (int r = 0; r < RX; ++r) {
             xpos[r] = U.xbase + r * 32 + lane;
             xval[r] = xpos[r] < U.xbase + U.nx;
+            sxm[r * 32 + lane] = __ldg(a.meta + U.P.a_start + (xval[r] ? xpos[r] : U.xbase));
             if (xval[r]) {
                 pairs += unit_pairs(U, xpos[r]);
                 const uint8_t *codes =
@@ -330,6 +392,7 @@ k_levenshtein(DistArgs a) {
             const uint32_t nb = min((uint32_t)kYB, U.ny - yb);
             const uint4 *src = a.rec + (size_t)(yrow0 + yb) * a.rs16;
             for (uint32_t t = lane; t < nb * a.rs16; t += 32) sy[t] = __ldg(src + t);
+            for (uint32_t t = lane; t < nb; t += 32) sym[t] = __ldg(a.meta + yrow0 + yb + t);
             __syncwarp();
             for (uint32_t t = 0; t < nb; ++t) {
                 const uint32_t ypos = U.ybase + yb + t;
@@ -366,7 +429,10 @@ k_levenshtein(DistArgs a) {
                             bool live = false;
 #pragma unroll
                             for (int r = 0; r < RX; ++r) {
-                                if (alive[r] && myers_value<W>(Pv[r], Mv[r], i, col) > eps) alive[r] = false;
+                                if (alive[r] && myers_value<W>(Pv[r], Mv[r], i, col) > eps) {
+                                    alive[r] = false;
+                                    cols += (uint32_t)col;
+                                }
                                 live |= alive[r];
                             }
                             if (!__any_sync(0xFFFFFFFFu, live)) break;
@@ -376,24 +442,20 @@ k_levenshtein(DistArgs a) {
                 uint32_t hit = 0;
 #pragma unroll
                 for (int r = 0; r < RX; ++r)
-                    if (alive[r] && myers_value<W>(Pv[r], Mv[r], m, n) <= eps) hit |= 1u << r;
-                if (__any_sync(0xFFFFFFFFu, hit)) {
-                    const uint32_t uy = a.ent_uid[yrow0 + yb + t];
-#pragma unroll
-                    for (int r = 0; r < RX; ++r) {
-                        bool ok = (hit >> r) & 1u;
-                        uint32_t ux = 0;
-                        if (ok) {
-                            ux = a.ent_uid[U.P.a_start + xpos[r]];
-                            ok = canonical(a, U.P, ux, uy);
-                        }
-                        ew.append(a, lane, ok, min(ux, uy), max(ux, uy));
+                    if (alive[r]) {
+                        cols += (uint32_t)n;
+                        if (myers_value<W>(Pv[r], Mv[r], m, n) <= eps) hit |= 1u << r;
                     }
-                }
+                if (__any_sync(0xFFFFFFFFu, hit))
+                    emit_hits_meta(a, ew, hit, sxm, sym[t], U.xbase, ypos, U.P.same, U.P.v, U.P.j,
+                                   lane);
             }
             __syncwarp();
         }
     }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) cols += __shfl_xor_sync(0xFFFFFFFFu, cols, d);
+    if (lane == 0 && cols) atomicAdd(&a.ctr->lev_columns, (unsigned long long)cols);
     finish(a, ew, pairs, lane);
 }
 
@@ -550,6 +612,8 @@ static DistArgs make_args(const Plan &P, const Buffers &B) {
     a.ctr = B.ctr;
     a.bp_cycles = nullptr;
     a.bp_hits = nullptr;
+    a.meta = B.ent_meta;
+    a.sig_exact = P.sig_exact ? 1 : 0;
     return a;
 }
 
@@ -590,7 +654,8 @@ void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s) 
         }
         return;
     }
-    const size_t smem = (size_t)kWarps * ((size_t)P.RX * P.A * P.W * 32 * 4 + (size_t)kYB * P.RS);
+    const size_t smem = (size_t)kWarps * ((size_t)P.RX * P.A * P.W * 32 * 4 + (size_t)kYB * P.RS +
+                                          16 * ((size_t)kYB + 32 * P.RX));
     switch (P.W) {
         case 1: if (P.RX == 2) run(k_levenshtein<1, 2>, a, smem, grid, s); else run(k_levenshtein<1, 1>, a, smem, grid, s); break;
         case 2: run(k_levenshtein<2, 1>, a, smem, grid, s); break;

@@ -9,6 +9,8 @@
 //  duplicates (S3)     cuda/PSDBSCAN.hcu:525-573 (an N^2 thread grid) + 1074-1085
 //                      (sort / reduce_by_key / scatter); here one hash-table pass
 //  uniques             cuda/PSDBSCAN.hcu:1102-1111 (remove_if over copies != 0)
+#include <algorithm>
+
 #include "idb_internal.cuh"
 
 namespace idb {
@@ -76,57 +78,158 @@ __global__ void k_const_strings(uint8_t *blob, int64_t *off, uint32_t N) {
 
 // ---------------------------------------------------------------------------
 // S1 -- gene bitsets.  Bit g of a row is set iff reference gene name g is a
-// byte-exact substring of the row's call (cuda/BitsetVector.inl:149-175).  One
-// warp per row; lane l tests genes l, l+32, ...; a ballot assembles 32 bits.
-// Names live in shared memory.  An empty name never matches (the reference
-// launches a zero-thread block for it).
+// byte-exact substring of the row's call (cuda/BitsetVector.inl:149-175, one
+// launch and one block per row per gene there).
+//
+// Here a block takes 128 rows at a time and stages their call bytes in shared
+// memory with coalesced loads.  A byte that starts some gene name is a
+// candidate; candidates are collected into a queue, then each thread takes one
+// candidate and extends a rolling hash over the following bytes (up to the end
+// of the row's call), looking the hash up in the gene table at every length
+// that some name has, and verifying the bytes of every hit.  Each candidate
+// thus costs one pass over at most the longest name instead of one scan per
+// gene.  Empty names never match (the reference launches a zero-thread block
+// for them).  A chunk whose calls exceed the staging buffer, or a table with a
+// name longer than 255 bytes, falls back to one warp per row and one lane per
+// gene.
 // ---------------------------------------------------------------------------
+constexpr int kGbRows = 128;
+constexpr int kGbBytes = 12288;
+
+__device__ __forceinline__ bool name_at(const uint8_t *c, uint32_t cl, const uint8_t *name,
+                                        uint32_t nl) {
+    if (nl == 0 || nl > cl) return false;
+    const uint8_t first = name[0];
+    for (uint32_t p = 0; p + nl <= cl; ++p) {
+        if (c[p] != first) continue;
+        uint32_t k = 1;
+        while (k < nl && c[p + k] == name[k]) ++k;
+        if (k == nl) return true;
+    }
+    return false;
+}
+
+// one warp, one row: lane l tests genes l, l+32, ...
+__device__ void gene_bits_row_naive(const uint8_t *c, uint32_t cl, const uint8_t *genes,
+                                    const int32_t *goff, uint32_t G, uint32_t GW, int lane,
+                                    uint64_t *out) {
+    uint64_t acc[kMaxGeneWords];
+#pragma unroll
+    for (int w = 0; w < kMaxGeneWords; ++w) acc[w] = 0;
+    for (uint32_t gb = 0; gb * 32 < G; ++gb) {
+        const uint32_t g = gb * 32 + lane;
+        bool found = false;
+        if (g < G) {
+            const int32_t n0 = goff[g];
+            found = name_at(c, cl, genes + n0, (uint32_t)(goff[g + 1] - n0));
+        }
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, found);
+#pragma unroll
+        for (int w = 0; w < kMaxGeneWords; ++w)
+            if ((int)(gb >> 1) == w) acc[w] |= (uint64_t)m << (32 * (gb & 1));
+    }
+#pragma unroll
+    for (int w = 0; w < kMaxGeneWords; ++w)
+        if (lane == w && (uint32_t)w < GW) out[w] = acc[w];
+}
+
 __global__ void __launch_bounds__(kThreads)
 k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, uint32_t N,
             const uint8_t *__restrict__ genes, const int32_t *__restrict__ goff, uint32_t G,
-            uint32_t GW, uint32_t smem_genes, uint64_t *__restrict__ bits) {
+            uint32_t GW, const GeneEntry *__restrict__ tab, GeneMatcher gm,
+            uint64_t *__restrict__ bits) {
     extern __shared__ uint8_t sm[];
-    int32_t *s_goff = reinterpret_cast<int32_t *>(sm);
-    uint8_t *s_genes = sm + sizeof(int32_t) * (G + 1);
+    GeneEntry *s_tab = reinterpret_cast<GeneEntry *>(sm);
+    int32_t *s_goff = reinterpret_cast<int32_t *>(s_tab + gm.ts);
+    uint64_t *s_bits = reinterpret_cast<uint64_t *>(
+        reinterpret_cast<uintptr_t>(s_goff + G + 1 + 1) & ~(uintptr_t)7);
+    uint32_t *s_roff = reinterpret_cast<uint32_t *>(s_bits + kGbRows * GW);
+    uint16_t *s_cand = reinterpret_cast<uint16_t *>(s_roff + kGbRows + 1);
+    uint8_t *s_bytes = reinterpret_cast<uint8_t *>(s_cand + kGbBytes);
+    __shared__ uint32_t s_ncand, s_first[8], s_len[8];
+    __shared__ int s_fit;
+    for (uint32_t k = threadIdx.x; k < gm.ts; k += blockDim.x) s_tab[k] = tab[k];
     for (uint32_t k = threadIdx.x; k <= G; k += blockDim.x) s_goff[k] = goff[k];
-    for (uint32_t k = threadIdx.x; k < smem_genes; k += blockDim.x) s_genes[k] = genes[k];
+    if (threadIdx.x < 8) {
+        s_first[threadIdx.x] = gm.firstmask[threadIdx.x];
+        s_len[threadIdx.x] = gm.lenmask[threadIdx.x];
+    }
     __syncthreads();
-    const uint8_t *gsrc = (uint32_t)goff[G] <= smem_genes ? s_genes : genes;
-    const int lane = threadIdx.x & 31;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t i = warp; i < N; i += nwarps) {
-        const int64_t c0 = off[i];
-        const uint32_t cl = (uint32_t)(off[i + 1] - c0);
-        const uint8_t *c = calls + c0;
-        uint64_t acc[kMaxGeneWords];
-#pragma unroll
-        for (int w = 0; w < kMaxGeneWords; ++w) acc[w] = 0;
-        for (uint32_t gb = 0; gb * 32 < G; ++gb) {
-            const uint32_t g = gb * 32 + lane;
-            bool found = false;
-            if (g < G) {
-                const int32_t n0 = s_goff[g];
-                const uint32_t nl = (uint32_t)(s_goff[g + 1] - n0);
-                const uint8_t *name = gsrc + n0;
-                if (nl > 0 && nl <= cl) {
-                    const uint8_t first = name[0];
-                    for (uint32_t p = 0; p + nl <= cl && !found; ++p) {
-                        if (c[p] != first) continue;
-                        uint32_t k = 1;
-                        while (k < nl && c[p + k] == name[k]) ++k;
-                        found = (k == nl);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t nchunks = (N + kGbRows - 1) / kGbRows;
+    for (uint32_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+        const uint32_t r0 = ch * kGbRows, nr = min((uint32_t)kGbRows, N - r0);
+        const int64_t base = off[r0];
+        const int64_t total = off[r0 + nr] - base;
+        if (threadIdx.x == 0) {
+            s_ncand = 0;
+            s_fit = total <= kGbBytes && !gm.long_names;
+        }
+        __syncthreads();
+        if (!s_fit) {   // slow path: one warp per row, names from global memory
+            for (uint32_t r = wid; r < nr; r += blockDim.x / 32) {
+                const int64_t c0 = off[r0 + r];
+                gene_bits_row_naive(calls + c0, (uint32_t)(off[r0 + r + 1] - c0), genes, s_goff, G,
+                                    GW, lane, bits + (size_t)(r0 + r) * GW);
+            }
+            __syncthreads();
+            continue;
+        }
+        for (uint32_t k = threadIdx.x; k <= nr; k += blockDim.x)
+            s_roff[k] = (uint32_t)(off[r0 + k] - base);
+        for (uint32_t k = threadIdx.x; k < nr * GW; k += blockDim.x) s_bits[k] = 0;
+        for (uint32_t q = threadIdx.x; q < (uint32_t)total; q += blockDim.x) s_bytes[q] = calls[base + q];
+        __syncthreads();
+        // candidate positions (warp-aggregated append)
+        for (uint32_t q0 = 0; q0 < (uint32_t)total; q0 += blockDim.x) {
+            const uint32_t q = q0 + threadIdx.x;
+            bool cand = false;
+            if (q < (uint32_t)total) {
+                const uint32_t c = s_bytes[q];
+                cand = (s_first[c >> 5] >> (c & 31)) & 1u;
+            }
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, cand);
+            uint32_t b = 0;
+            if (lane == 0 && m) b = atomicAdd(&s_ncand, (uint32_t)__popc(m));
+            b = __shfl_sync(0xFFFFFFFFu, b, 0);
+            if (cand) s_cand[b + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+        }
+        __syncthreads();
+        // verify candidates: rolling hash + table lookups at the name lengths
+        const uint32_t nc = s_ncand;
+        for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
+            const uint32_t q = s_cand[k];
+            uint32_t lo = 0, hi = nr;   // row: largest r with s_roff[r] <= q
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (s_roff[mid] <= q) lo = mid; else hi = mid;
+            }
+            const uint32_t row = lo, end = s_roff[row + 1];
+            uint32_t h = 0;
+            for (uint32_t t = 0; t < gm.maxlen && q + t < end; ++t) {
+                h = h * kGeneHashMul + s_bytes[q + t];
+                const uint32_t L = t + 1;
+                if (!((s_len[L >> 5] >> (L & 31)) & 1u)) continue;
+                uint32_t sl = h & (gm.ts - 1);
+                while (s_tab[sl].len != 0) {
+                    const GeneEntry e = s_tab[sl];
+                    if (e.h == h && e.len == L) {
+                        const uint8_t *name = genes + s_goff[e.gene];
+                        uint32_t i = 0;
+                        while (i < L && name[i] == s_bytes[q + i]) ++i;
+                        if (i == L)
+                            atomicOr(reinterpret_cast<unsigned long long *>(
+                                         &s_bits[row * GW + (e.gene >> 6)]),
+                                     1ull << (e.gene & 63));
                     }
+                    sl = (sl + 1) & (gm.ts - 1);
                 }
             }
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, found);
-#pragma unroll
-            for (int w = 0; w < kMaxGeneWords; ++w)
-                if ((int)(gb >> 1) == w) acc[w] |= (uint64_t)m << (32 * (gb & 1));
         }
-#pragma unroll
-        for (int w = 0; w < kMaxGeneWords; ++w)
-            if (lane == w && (uint32_t)w < GW) bits[(size_t)i * GW + w] = acc[w];
+        __syncthreads();
+        for (uint32_t k = threadIdx.x; k < nr * GW; k += blockDim.x)
+            bits[(size_t)r0 * GW + k] = s_bits[k];
+        __syncthreads();
     }
 }
 
@@ -432,11 +535,21 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     const int64_t *off = v_column ? B.v_off : B.j_off;
     const uint8_t *genes = v_column ? B.vgenes : B.jgenes;
     const int32_t *goff = v_column ? B.vg_off : B.jg_off;
-    const uint32_t gene_bytes = v_column ? P.gene_bytes_v : P.gene_bytes_j;
-    const uint32_t smem_genes = gene_bytes <= 40000u ? gene_bytes : 0u;
-    const size_t smem = sizeof(int32_t) * (G + 1) + smem_genes;
-    const int grid = grid_for((uint64_t)P.N * 32);
-    k_gene_bits<<<grid, kThreads, smem, s>>>(calls, off, P.N, genes, goff, G, GW, smem_genes, bits);
+    const GeneEntry *tab = v_column ? B.vtab : B.jtab;
+    const GeneMatcher &gm = v_column ? P.vmatch : P.jmatch;
+    size_t smem = sizeof(GeneEntry) * gm.ts + sizeof(int32_t) * (G + 2) + 8 +
+                  sizeof(uint64_t) * kGbRows * GW + sizeof(uint32_t) * (kGbRows + 1) +
+                  sizeof(uint16_t) * kGbBytes + kGbBytes + 16;
+    static thread_local size_t attr_set = 0;
+    if (smem > 48 * 1024 && smem > attr_set) {
+        cudaFuncSetAttribute(k_gene_bits, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        attr_set = smem;
+    }
+    const uint32_t nchunks = (P.N + kGbRows - 1) / kGbRows;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gene_bits, kThreads, smem);
+    const int grid = (int)std::min<uint64_t>(nchunks, (uint64_t)sm_count() * (per_sm > 0 ? per_sm : 1));
+    k_gene_bits<<<grid, kThreads, smem, s>>>(calls, off, P.N, genes, goff, G, GW, tab, gm, bits);
 }
 
 void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s) {

@@ -103,6 +103,7 @@ typedef struct idb_stats {
                                   on host read-backs)                              */
     uint32_t kernel_launches;  /* kernels launched (graph replays)                 */
     uint32_t reserved;
+    uint64_t lev_columns;      /* text columns consumed by live Levenshtein pairs  */
 } idb_stats;
 
 /* Outputs (cuda/Interlink.hpp:59-67).  clone_id/core/copies are required. */

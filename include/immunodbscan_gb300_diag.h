@@ -28,6 +28,13 @@ int idb_diag_int_peak(int device, double *gops_out, double *ms_out);
 idb_status idb_count_admissible(idb_context *ctx, const idb_input *in, const idb_params *prm,
                                 uint64_t *pairs_out);
 
+/* Gene bitsets alone (rule S1): words_out[i * W + w] (W = max(1, ceil(n_genes/64)))
+   has bit g%64 of word g/64 set iff gene name g is a byte-exact substring of
+   call i.  Host inputs and output; synchronous. */
+idb_status idb_diag_gene_bits(idb_context *ctx, const char *calls, const int64_t *offsets,
+                              uint32_t n_rows, const char *genes, const int64_t *gene_offsets,
+                              uint32_t n_genes, uint64_t *words_out);
+
 #ifdef __cplusplus
 }
 #endif

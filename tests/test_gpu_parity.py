@@ -202,3 +202,61 @@ def test_device_api_matches_host_api(gpu_ctx):
     clone, core, copies = b.results()
     assert np.array_equal(clone, plain.clone_id)
     assert np.array_equal(copies, plain.copies)
+
+
+def _gpu_bits(ctx, calls, genes):
+    import ctypes as C
+    from immunodbscan_gb300 import _lib
+    from immunodbscan_gb300.interlink import _as_blob
+    cb, co = _as_blob(calls)
+    gb, go = _as_blob(genes)
+    W = max(1, (len(genes) + 63) // 64)
+    out = np.zeros((len(calls), W), np.uint64)
+    _lib.check(_lib.lib().idb_diag_gene_bits(ctx.handle, cb.ctypes.data, co.ctypes.data,
+                                             len(calls), gb.ctypes.data, go.ctypes.data,
+                                             len(genes), out.ctypes.data))
+    return out
+
+
+def _as_words32(bits64, n_genes):
+    w32 = (n_genes + 31) // 32
+    out = np.zeros((bits64.shape[0], w32), np.uint32)
+    for k in range(w32):
+        out[:, k] = (bits64[:, k // 2] >> np.uint64(32 * (k % 2))) & np.uint64(0xFFFFFFFF)
+    return out
+
+
+def test_gene_bits_known_answers(gpu_ctx):
+    from kat_cases import S1_CALLS, S1_GENES, S1_WORDS
+    got = _as_words32(_gpu_bits(gpu_ctx, S1_CALLS, S1_GENES), len(S1_GENES))
+    assert got.tolist() == S1_WORDS
+
+
+@pytest.mark.parametrize("long_calls", [False, True])
+def test_gene_bits_vs_oracle(gpu_ctx, long_calls):
+    """Random names (incl. empty, repeated, overlapping and prefix-sharing ones)
+    against random calls; long calls overflow the staging buffer and take the
+    per-row path."""
+    rng = np.random.default_rng(5 + long_calls)
+    alpha = list(b"ACGT*-I0123")
+    genes = [bytes(rng.choice(alpha, size=int(rng.integers(1, 7))).astype(np.uint8)) for _ in range(150)]
+    genes += [b"", genes[3], genes[7] + b"*"] + ([b"A" * 300] if long_calls else [])
+    calls = []
+    for i in range(3000):
+        n = int(rng.integers(0, 400 if long_calls else 60))
+        s = bytearray(rng.choice(alpha, size=n).astype(np.uint8).tobytes())
+        if rng.random() < 0.5 and n > 10:
+            g = genes[int(rng.integers(0, len(genes)))]
+            p = int(rng.integers(0, n))
+            s[p:p] = g
+        calls.append(bytes(s))
+    got = _as_words32(_gpu_bits(gpu_ctx, calls, genes), len(genes))
+    want = oracle.gene_bitsets(calls, genes)
+    assert np.array_equal(got, want)
+
+
+def test_gene_bits_synthetic(gpu_ctx):
+    w = synth.workload(2, scale=0.002)
+    calls = [w.vcall(i) for i in range(w.n)]
+    got = _as_words32(_gpu_bits(gpu_ctx, calls, w.v_genes), len(w.v_genes))
+    assert np.array_equal(got, oracle.gene_bitsets(calls, w.v_genes))
