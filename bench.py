@@ -44,12 +44,12 @@ UNIT = "Gpair-distances/s"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=40)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", type=int, default=2)
     ap.add_argument("--scale", type=float, default=1.0)
-    ap.add_argument("--schedule", type=int, default=0)
+    ap.add_argument("--mlp-epochs", type=int, default=200)
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -74,7 +74,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self.proc = None
@@ -205,6 +205,31 @@ def reference_arm(args, world, rank, w):
     print(json.dumps(line), flush=True)
 
 
+def time_batch(batch, steps, warmup, world, clocks=None):
+    """Warm up, then time exactly `steps` graph replays (device time per step)."""
+    import torch
+    for _ in range(warmup):
+        batch.run()
+    if clocks:
+        clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ms, ms_dist, phases, launches = [], [], [], 0
+    wall0 = time.perf_counter()
+    for _ in range(steps):
+        st = batch.run()
+        ms.append(st.ms_total)
+        ms_dist.append(st.ms_distance)
+        phases.append([st.ms_phase[k] for k in range(5)])
+        launches += st.kernel_launches
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    barrier(world)
+    clk = clocks.stop() if clocks else None
+    return dict(step_ms=allreduce_max(world, float(np.mean(ms))), ms_dist=float(np.mean(ms_dist)),
+                phases=phases, launches=launches, wall=wall, last=st, clocks=clk)
+
+
 def main():
     args = parse()
     world, rank, local = dist_init(args)
@@ -216,46 +241,49 @@ def main():
         reference_arm(args, world, rank, w)
         return
     import torch
-    from immunodbscan_gb300 import Context, DeviceBatch, _lib
-    from immunodbscan_gb300.interlink import Interlink, _as_blob, _p, make_params
+    from immunodbscan_gb300 import Context, DeviceBatch, _lib, learned, tuning
+    from immunodbscan_gb300.interlink import make_params
     torch.cuda.set_device(local)
     L = _lib.lib()
-    ctx = Context(local)
+    # one context per captured plan: eager calls on a context may regrow its
+    # workspace, which would invalidate a graph captured on it
+    ctx_setup, ctx_static, ctx_learned = Context(local), Context(local), Context(local)
     n = w.n
 
     # numerator: admissible unique pairs (setup, untimed)
     inp, keep = build_host_input(w, pinned=False)
-    prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, args.schedule)
+    prm0 = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming)
     adm = C.c_uint64()
-    _lib.check(L.idb_count_admissible(ctx.handle, C.byref(inp), C.byref(prm), C.byref(adm)))
+    _lib.check(L.idb_count_admissible(ctx_setup.handle, C.byref(inp), C.byref(prm0), C.byref(adm)))
     admissible = int(adm.value)
 
-    # batched graph path (value)
-    batch = DeviceBatch(w, ctx, schedule=args.schedule)
-    batch.plan()
-    for _ in range(args.warmup):
-        batch.run()
+    # autotuner: work-unit shape measured on this workload (setup, untimed)
+    tune_rec = tuning.measure(w, ctx_setup)
+    shape = (tune_rec["rx"], tune_rec["ty"])
+
+    # learned schedule: trained on a profile of a differently seeded workload of
+    # the same kind (setup, untimed)
+    t0 = time.time()
+    wt = synth.workload(args.workload, scale=min(args.scale, 0.1), seed=4242 + args.workload)
+    X, T = learned.profile(wt, ctx_setup, tune=shape)
+    params, loss = learned.train(X, T, ctx_setup, epochs=args.mlp_epochs)
+    learned.install(ctx_learned, params)
+    train_s = time.time() - t0
+
+    # batched graph path, static heavy-first order
+    b_static = DeviceBatch(w, ctx_static, schedule=0, tune=shape)
+    b_static.plan()
+    r_static = time_batch(b_static, args.steps, args.warmup, world)
+    # batched graph path, learned order (the headline value)
+    b_learned = DeviceBatch(w, ctx_learned, schedule=1, tune=shape)
+    b_learned.plan()
     clocks = ClockSampler(local)
-    clocks.start()
-    barrier(world)
-    torch.cuda.synchronize()
-    ms, ms_dist, phases, launches = [], [], [], 0
-    wall0 = time.perf_counter()
-    for _ in range(args.steps):
-        st = batch.run()
-        ms.append(st.ms_total)
-        ms_dist.append(st.ms_distance)
-        phases.append([st.ms_phase[k] for k in range(5)])
-        launches += st.kernel_launches
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - wall0
-    barrier(world)
-    clk = clocks.stop()
-    step_ms = allreduce_max(world, float(np.mean(ms)))
+    r = time_batch(b_learned, args.steps, args.warmup, world, clocks)
+    step_ms = r["step_ms"]
     value = world * admissible / (step_ms * 1e-3) / 1e9
-    seq_per_s = world * n / (step_ms * 1e-3)
-    last = st
-    clone_b, core_b, copies_b = batch.results()
+    last = r["last"]
+    clone_b, core_b, copies_b = b_learned.results()
+    clone_s, core_s, _ = b_static.results()
 
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
@@ -267,23 +295,32 @@ def main():
                       "global_batch": n * world, "seq_len": int(w.lengths().max()),
                       "parallelism": "replicas only" if world > 1 else "single GPU",
                       "l2": "inputs and working set larger than L2 (129 MB)",
-                      "schedule": "learned" if args.schedule == 1 else "static heavy-first"},
-           "seq_per_s": seq_per_s, "admissible_pairs": admissible,
+                      "schedule": "learned (2x64 MLP, BF16 inference)",
+                      "tile": {"rx": shape[0], "ty": shape[1], "source": "autotuner"}},
+           "seq_per_s": world * n / (step_ms * 1e-3), "admissible_pairs": admissible,
            "pairs_evaluated": int(last.pairs_evaluated),
            "neighbour_pairs": int(last.neighbour_pairs), "n_uniques": int(last.n_uniques),
-           "n_clusters": int(last.n_clusters), "gpu_launches": int(launches),
-           "phase_ms": {k: float(np.mean([p[i] for p in phases])) for i, k in
+           "n_clusters": int(last.n_clusters), "gpu_launches": int(r["launches"]),
+           "phase_ms": {k: float(np.mean([p[i] for p in r["phases"]])) for i, k in
                         enumerate(["front_dedupe", "buckets_schedule", "distance", "graph",
                                    "outputs"])},
-           "wall_ms_per_step": 1e3 * wall / args.steps, "gen_seconds": gen_s,
-           "clocks": clk}
+           "wall_ms_per_step": 1e3 * r["wall"] / args.steps, "gen_seconds": gen_s,
+           "clocks": r["clocks"],
+           "static_schedule": {"ms_per_step": r_static["step_ms"],
+                               "distance_ms": r_static["ms_dist"],
+                               "learned_gain": r_static["step_ms"] / step_ms,
+                               "identical_partitions": bool(np.array_equal(clone_s, clone_b) and
+                                                            np.array_equal(core_s, core_b))},
+           "autotune": {"tried": tune_rec["tried"]},
+           "learned_model": {"train_binpairs": int(len(T)), "mse_log2_cycles": loss,
+                             "setup_seconds": train_s}}
 
     # roofline of the distance kernel: integer logic against the measured int peak
     gops = C.c_double()
     pms = C.c_double()
     L.idb_diag_int_peak(local, C.byref(gops), C.byref(pms))
-    ops_pair = ops_per_pair(w, batch)
-    t_dist = float(np.mean(ms_dist)) * 1e-3
+    ops_pair = ops_per_pair(w, None)
+    t_dist = r["ms_dist"] * 1e-3
     if w.use_hamming:
         work_ops = ops_pair * last.pairs_evaluated
     else:                       # Myers/Hyyro: ops per text column actually consumed
@@ -299,21 +336,22 @@ def main():
                        "kernel_ms": t_dist * 1e3,
                        "peak_source": "measured: idb_diag_int_peak (lop3/add chains, all SMs)"}
 
-    # e2e through idb_cluster with pinned host buffers
+    # e2e through idb_cluster (the InterlinkClass replacement) with pinned host buffers
     if not args.no_e2e:
         hin, hkeep = build_host_input(w, pinned=True)
+        prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, 1, shape)
         clone = torch.empty(n, dtype=torch.int32).pin_memory()
         core = torch.empty(n, dtype=torch.int32).pin_memory()
         copies = torch.empty(n, dtype=torch.int32).pin_memory()
         o = _lib.Output(clone.data_ptr(), core.data_ptr(), copies.data_ptr(), None, None, None,
                         None)
         for _ in range(max(1, args.warmup)):
-            _lib.check(L.idb_cluster(ctx.handle, C.byref(hin), C.byref(prm), C.byref(o)))
+            _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
         barrier(world)
         times = []
         for _ in range(args.steps):
             t0 = time.perf_counter()
-            _lib.check(L.idb_cluster(ctx.handle, C.byref(hin), C.byref(prm), C.byref(o)))
+            _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
             times.append(time.perf_counter() - t0)
         barrier(world)
         e2e_s = allreduce_max(world, float(np.mean(times)))
@@ -321,16 +359,16 @@ def main():
         out["e2e"] = {"value": world * admissible / e2e_s / 1e9, "unit": UNIT,
                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * n,
                       "ms_per_step": e2e_s * 1e3, "seq_per_s": world * n / e2e_s,
-                      "api": "idb_cluster (host buffers)"}
+                      "api": "idb_cluster (host buffers, learned schedule)"}
         same = (np.array_equal(clone.numpy().view(np.uint32), clone_b) and
                 np.array_equal(core.numpy(), core_b))
         out["e2e"]["identical_partitions_vs_batched"] = bool(same)
 
-    # plain per-repertoire path
+    # plain per-repertoire path: one eager call per repertoire, default shape, static order
     if not args.no_plain:
+        ctx_plain = Context(local)
         plain_ms = []
-        subs = [DeviceBatch(w.subset_repertoires([r]), ctx, schedule=args.schedule)
-                for r in range(w.n_rep)]
+        subs = [DeviceBatch(w.subset_repertoires([rr]), ctx_plain) for rr in range(w.n_rep)]
         for sb in subs:
             sb.cluster_once()
         for _ in range(max(1, min(args.steps, 3))):
@@ -342,13 +380,15 @@ def main():
             plain_ms.append(1e3 * (time.perf_counter() - t0))
         pm = float(np.mean(plain_ms))
         same = True
-        for r, sb in enumerate(subs):
+        for rr, sb in enumerate(subs):
             c_, k_, p_ = sb.results()
-            lo, hi = int(w.rep_off[r]), int(w.rep_off[r + 1])
+            lo, hi = int(w.rep_off[rr]), int(w.rep_off[rr + 1])
             same &= np.array_equal(c_, clone_b[lo:hi]) and np.array_equal(k_, core_b[lo:hi])
         out["plain"] = {"value": admissible / (pm * 1e-3) / 1e9, "unit": UNIT, "ms_per_step": pm,
-                        "api": "64 x idb_cluster_device (eager, per repertoire)",
-                        "batched_speedup": pm / step_ms, "identical_partitions": bool(same)}
+                        "api": f"{w.n_rep} x idb_cluster_device (eager, per repertoire)",
+                        "batched_learned_speedup": pm / step_ms,
+                        "identical_partitions": bool(same)}
+        ctx_plain.close()
 
     if rank == 0 and not args.no_cpu:
         res = run_cpu(w, args.cpu_seconds or 10.0, os.cpu_count() or 1)
@@ -359,7 +399,8 @@ def main():
                                          f"{res['seconds']:.1f} s"}
     if rank == 0:
         print(json.dumps(out), flush=True)
-    ctx.close()
+    for c in (ctx_setup, ctx_static, ctx_learned):
+        c.close()
 
 
 def ops_per_pair(w, batch) -> int:

@@ -12,6 +12,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libimmunodbscan_gb300.so")
 
 IDB_OK = 0
+MLP_FEATURES = 16
+MLP_PARAMS = 16 * 64 + 64 + 64 * 64 + 64 + 64 + 1
 STATUS_NAMES = {
     0: "IDB_OK", 1: "IDB_ERR_INVALID_ARG", 2: "IDB_ERR_CUDA", 3: "IDB_ERR_NO_DEVICE",
     4: "IDB_ERR_UNSUPPORTED", 5: "IDB_ERR_OUT_OF_MEMORY", 6: "IDB_ERR_CAPACITY",
@@ -28,7 +30,13 @@ class IdbError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [("threshold", C.c_float), ("abs_eps", C.c_int32), ("min_pts", C.c_uint32),
                 ("use_hamming", C.c_int32), ("eval_trees", C.c_int32), ("schedule", C.c_int32),
-                ("reserved", C.c_int32 * 6)]
+                ("tile_rx", C.c_int32), ("tile_ty", C.c_int32), ("reserved", C.c_int32 * 4)]
+
+
+class Tuning(C.Structure):
+    _fields_ = [("tile_rx", C.c_int32), ("tile_ty", C.c_int32), ("ms_distance", C.c_double),
+                ("n_tried", C.c_int32), ("tried_rx", C.c_int32 * 16), ("tried_ty", C.c_int32 * 16),
+                ("tried_ms", C.c_double * 16)]
 
 
 class Input(C.Structure):
@@ -71,6 +79,14 @@ SIGNATURES = {
     "idb_abi_version": (C.c_int, []),
     "idb_dedupe_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                      C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "idb_autotune": (C.c_int, [C.c_void_p, C.POINTER(Input), C.POINTER(Params), C.POINTER(Tuning)]),
+    "idb_profile_binpairs": (C.c_int, [C.c_void_p, C.POINTER(Input), C.POINTER(Params), C.c_void_p,
+                                       C.c_void_p, C.c_uint64, C.POINTER(C.c_uint64)]),
+    "idb_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_float,
+                                C.c_void_p, C.POINTER(C.c_float)]),
+    "idb_mlp_load": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "idb_diag_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                    C.c_void_p, C.POINTER(C.c_float)]),
     "idb_diag_int_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "idb_diag_gene_bits": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                      C.c_void_p, C.c_uint32, C.c_void_p]),

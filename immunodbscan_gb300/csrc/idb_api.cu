@@ -89,6 +89,9 @@ struct idb_context {
     idb_output out_dev{};
     bool trees = false;
     uint32_t graph_kernels = 0;
+    // learned schedule: MLP parameters (BF16 for inference)
+    void *mlp_bf16 = nullptr;
+    bool has_model = false;
 };
 
 namespace {
@@ -324,6 +327,19 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
     return IDB_OK;
 }
 
+// Work-unit shape: rx x-entries per lane (the kernels are compiled for
+// Hamming 4 or 8 with one word, 4 otherwise; Levenshtein 1, or 2 with one word)
+// and ty y-entries, a multiple of 32*rx up to 4096.  Invalid values are ignored.
+void apply_shape(Plan &P, int rx, int ty) {
+    if (rx > 0) {
+        if (P.hamming && (rx == 4 || (rx == 8 && P.W == 1))) P.RX = rx;
+        if (!P.hamming && (rx == 1 || (rx == 2 && P.W == 1))) P.RX = rx;
+        P.TX = 32 * P.RX;
+    }
+    if (P.TY % P.TX) P.TY = P.TX * ((P.TY + P.TX - 1) / P.TX);
+    if (ty > 0 && ty >= (int)P.TX && ty % (int)P.TX == 0 && ty <= 4096) P.TY = ty;
+}
+
 // Plan constants from the survey.
 idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
     Plan &P = pl.P;
@@ -372,14 +388,7 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
         P.TX = 32;
         P.TY = 256;
     }
-    if (prm->reserved[0] > 0 && P.fast) {   // tuned shape: reserved[0] = RX, reserved[1] = TY
-        const int rx = prm->reserved[0];
-        if (P.hamming && (rx == 4 || (rx == 8 && P.W == 1))) P.RX = rx;
-        if (!P.hamming && (rx == 1 || (rx == 2 && P.W == 1))) P.RX = rx;
-        P.TX = 32 * P.RX;
-        const int ty = prm->reserved[1];
-        if (ty >= (int)P.TX && ty % (int)P.TX == 0 && ty <= 4096) P.TY = ty;
-    }
+    if (P.fast) apply_shape(P, prm->tile_rx, prm->tile_ty);
     // eps table over the length range, and the largest admissible gap
     pl.eps_host.assign((size_t)P.NL * P.NL, 0);
     int dl = 0;
@@ -560,6 +569,10 @@ idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false
         TRY(alloc_binpairs(pl, c->h_ctr->n_binpairs));
     }
     launch_binpairs_fill(P, B, s);
+    if (P.schedule == 1) {
+        if (!c->has_model) return fail(IDB_ERR_INVALID_ARG, "learned schedule requested but no model loaded (idb_mlp_load)");
+        launch_mlp_predict(B, (uint32_t)P.cap_binpairs, c->mlp_bf16, s);
+    }
     launch_schedule(P, B, s);
     TRY(check_launch());
     record(pl, 2);
@@ -763,6 +776,7 @@ idb_status idb_context_destroy(idb_context *c) {
     for (auto &e : c->ev)
         if (e) cudaEventDestroy(e);
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
+    if (c->mlp_bf16) cudaFree(c->mlp_bf16);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c == t_default_ctx) t_default_ctx = nullptr;
     delete c;
@@ -920,6 +934,277 @@ idb_status idb_diag_gene_bits(idb_context *c, const char *calls, const int64_t *
     CU(cudaMemcpyAsync(words_out, B.vbits, sizeof(uint64_t) * n_rows * P.VW, cudaMemcpyDeviceToHost,
                        c->stream));
     CU(cudaStreamSynchronize(c->stream));
+    return IDB_OK;
+}
+
+idb_status idb_profile_binpairs(idb_context *c, const idb_input *in, const idb_params *prm,
+                                float *features, float *log2_cycles, uint64_t cap,
+                                uint64_t *n_out) {
+    TRY(get_ctx(&c));
+    if (!features || !log2_cycles || !n_out) return fail(IDB_ERR_INVALID_ARG, "NULL output");
+    uint32_t dummy = 0;
+    idb_output o{};
+    o.clone_id = &dummy; o.core = reinterpret_cast<int32_t *>(&dummy); o.copies = &dummy;
+    TRY(validate(in, prm, &o));
+    *n_out = 0;
+    if (in->n_rows == 0) return IDB_OK;
+    CU(cudaSetDevice(c->device));
+    cudaGetLastError();
+    idb_params p0 = *prm;
+    p0.schedule = 0;
+    Pipeline pl;
+    pl.c = c;
+    TRY(stage_inputs_and_survey(pl, in, true));
+    TRY(derive_plan(pl, &p0));
+    TRY(alloc_fixed(pl));
+    Plan &P = pl.P;
+    Buffers &B = pl.B;
+    cudaStream_t s = c->stream;
+    TRY(run_phases(pl, true, true));   // up to the static schedule
+    TRY(read_counters(pl));
+    const uint32_t nbp = c->h_ctr->n_binpairs;
+    if (P.cap_edges == 0) TRY(alloc_edges(pl, std::max<uint64_t>(4ull * P.N, 1ull << 16)));
+    unsigned long long *cyc = nullptr;
+    float *feat = nullptr;
+    CU(cudaMalloc(&cyc, sizeof(unsigned long long) * (nbp + 1)));
+    cudaError_t e = cudaMalloc(&feat, sizeof(float) * kMlpIn * (nbp + 1));
+    if (e != cudaSuccess) { cudaFree(cyc); return fail(IDB_ERR_OUT_OF_MEMORY, "profile buffers"); }
+    idb_status st = IDB_OK;
+    for (int attempt = 0; attempt < 3; ++attempt) {
+        cudaMemsetAsync(cyc, 0, sizeof(unsigned long long) * (nbp + 1), s);
+        cudaMemsetAsync(&B.ctr->unit_cursor, 0, 4, s);
+        cudaMemsetAsync(&B.ctr->edge_reserved, 0, 4, s);
+        B.bp_cycles = cyc;
+        launch_distance(P, B, 0, s);
+        B.bp_cycles = nullptr;
+        st = read_counters(pl);
+        if (st != IDB_OK || !(c->h_ctr->error & kErrEdgeOverflow)) break;
+        st = alloc_edges(pl, (uint64_t)c->h_ctr->edge_reserved + 64ull * kEdgeChunk * 1024);
+        if (st != IDB_OK) break;
+        uint32_t clear = 0;
+        cudaMemcpyAsync(&B.ctr->error, &clear, 4, cudaMemcpyHostToDevice, s);
+    }
+    const uint64_t n = std::min<uint64_t>(nbp, cap);
+    if (st == IDB_OK) {
+        launch_features(B, nbp, feat, s);
+        std::vector<unsigned long long> hc(nbp);
+        cudaMemcpyAsync(hc.data(), cyc, sizeof(unsigned long long) * nbp, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(features, feat, sizeof(float) * kMlpIn * n, cudaMemcpyDeviceToHost, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) st = fail(IDB_ERR_CUDA, "profile copy failed");
+        for (uint64_t i = 0; i < n; ++i) log2_cycles[i] = std::log2(1.0 + (double)hc[i]);
+        *n_out = n;
+    }
+    cudaFree(cyc);
+    cudaFree(feat);
+    return st;
+}
+
+idb_status idb_mlp_train(idb_context *c, const float *features, const float *targets, uint64_t n,
+                         int epochs, float lr, float *params, float *final_loss) {
+    TRY(get_ctx(&c));
+    if (!features || !targets || !params || n == 0 || epochs <= 0)
+        return fail(IDB_ERR_INVALID_ARG, "idb_mlp_train: bad arguments");
+    CU(cudaSetDevice(c->device));
+    cudaGetLastError();
+    cudaStream_t s = c->stream;
+    float *X = nullptr, *T = nullptr, *p = nullptr, *g = nullptr, *m = nullptr, *v = nullptr,
+          *loss = nullptr;
+    auto cleanup = [&]() {
+        cudaFree(X); cudaFree(T); cudaFree(p); cudaFree(g); cudaFree(m); cudaFree(v); cudaFree(loss);
+    };
+    if (cudaMalloc(&X, sizeof(float) * kMlpIn * n) != cudaSuccess ||
+        cudaMalloc(&T, sizeof(float) * n) != cudaSuccess ||
+        cudaMalloc(&p, sizeof(float) * kMlpParams) != cudaSuccess ||
+        cudaMalloc(&g, sizeof(float) * kMlpParams) != cudaSuccess ||
+        cudaMalloc(&m, sizeof(float) * kMlpParams) != cudaSuccess ||
+        cudaMalloc(&v, sizeof(float) * kMlpParams) != cudaSuccess ||
+        cudaMalloc(&loss, sizeof(float)) != cudaSuccess) {
+        cleanup();
+        cudaGetLastError();
+        return fail(IDB_ERR_OUT_OF_MEMORY, "idb_mlp_train: allocation failed");
+    }
+    cudaMemcpyAsync(X, features, sizeof(float) * kMlpIn * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(T, targets, sizeof(float) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(m, 0, sizeof(float) * kMlpParams, s);
+    cudaMemsetAsync(v, 0, sizeof(float) * kMlpParams, s);
+    const uint64_t batch = std::min<uint64_t>(n, 8192);
+    int step = 0;
+    for (int ep = 0; ep < epochs; ++ep) {
+        for (uint64_t b0 = 0; b0 < n; b0 += batch) {
+            const uint32_t nb = (uint32_t)std::min<uint64_t>(batch, n - b0);
+            cudaMemsetAsync(g, 0, sizeof(float) * kMlpParams, s);
+            cudaMemsetAsync(loss, 0, sizeof(float), s);
+            launch_mlp_grad(X + kMlpIn * b0, T + b0, nb, p, 1.0f / (float)nb, g, loss, s);
+            launch_adam(p, g, m, v, lr, ++step, s);
+        }
+    }
+    // loss over the full set with the final parameters
+    cudaMemsetAsync(g, 0, sizeof(float) * kMlpParams, s);
+    cudaMemsetAsync(loss, 0, sizeof(float), s);
+    launch_mlp_grad(X, T, (uint32_t)n, p, 1.0f / (float)n, g, loss, s);
+    float hl = 0;
+    cudaMemcpyAsync(params, p, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hl, loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    cleanup();
+    if (e != cudaSuccess) return fail(IDB_ERR_CUDA, "idb_mlp_train: %s", cudaGetErrorString(e));
+    TRY(check_launch());
+    if (final_loss) *final_loss = hl / (float)n;
+    return IDB_OK;
+}
+
+idb_status idb_mlp_load(idb_context *c, const float *params) {
+    if (!c) return fail(IDB_ERR_INVALID_ARG, "idb_mlp_load needs an explicit context");
+    CU(cudaSetDevice(c->device));
+    if (!params) { c->has_model = false; return IDB_OK; }
+    float *p = nullptr;
+    CU(cudaMalloc(&p, sizeof(float) * kMlpParams));
+    if (!c->mlp_bf16) {
+        cudaError_t e = cudaMalloc(&c->mlp_bf16, 2 * kMlpParams);
+        if (e != cudaSuccess) { cudaFree(p); return fail(IDB_ERR_OUT_OF_MEMORY, "model buffer"); }
+    }
+    cudaMemcpyAsync(p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, c->stream);
+    launch_to_bf16(p, c->mlp_bf16, c->stream);
+    const cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(p);
+    if (e != cudaSuccess) return fail(IDB_ERR_CUDA, "idb_mlp_load: %s", cudaGetErrorString(e));
+    c->has_model = true;
+    return IDB_OK;
+}
+
+idb_status idb_diag_mlp_grad(idb_context *c, const float *params, const float *features,
+                             const float *targets, uint32_t n, float *grad_out, float *loss_out) {
+    TRY(get_ctx(&c));
+    if (!params || !features || !targets || !grad_out || n == 0)
+        return fail(IDB_ERR_INVALID_ARG, "idb_diag_mlp_grad: bad arguments");
+    CU(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    float *X, *T, *p, *g, *loss;
+    CU(cudaMalloc(&X, sizeof(float) * kMlpIn * n));
+    CU(cudaMalloc(&T, sizeof(float) * n));
+    CU(cudaMalloc(&p, sizeof(float) * kMlpParams));
+    CU(cudaMalloc(&g, sizeof(float) * kMlpParams));
+    CU(cudaMalloc(&loss, sizeof(float)));
+    cudaMemcpyAsync(X, features, sizeof(float) * kMlpIn * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(T, targets, sizeof(float) * n, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(g, 0, sizeof(float) * kMlpParams, s);
+    cudaMemsetAsync(loss, 0, sizeof(float), s);
+    launch_mlp_grad(X, T, n, p, 1.0f / (float)n, g, loss, s);
+    float hl = 0;
+    cudaMemcpyAsync(grad_out, g, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hl, loss, sizeof(float), cudaMemcpyDeviceToHost, s);
+    const cudaError_t e = cudaStreamSynchronize(s);
+    cudaFree(X); cudaFree(T); cudaFree(p); cudaFree(g); cudaFree(loss);
+    if (e != cudaSuccess) return fail(IDB_ERR_CUDA, "idb_diag_mlp_grad: %s", cudaGetErrorString(e));
+    if (loss_out) *loss_out = hl / (float)n;
+    return IDB_OK;
+}
+
+idb_status idb_autotune(idb_context *c, const idb_input *in, const idb_params *prm,
+                        idb_tuning *best) {
+    TRY(get_ctx(&c));
+    if (!best) return fail(IDB_ERR_INVALID_ARG, "NULL output");
+    uint32_t dummy = 0;
+    idb_output o{};
+    o.clone_id = &dummy; o.core = reinterpret_cast<int32_t *>(&dummy); o.copies = &dummy;
+    TRY(validate(in, prm, &o));
+    std::memset(best, 0, sizeof *best);
+    if (in->n_rows == 0) return IDB_OK;
+    CU(cudaSetDevice(c->device));
+    cudaGetLastError();
+    Pipeline pl;
+    pl.c = c;
+    TRY(stage_inputs_and_survey(pl, in, true));
+    TRY(derive_plan(pl, prm));
+    TRY(alloc_fixed(pl));
+    Plan &P = pl.P;
+    Buffers &B = pl.B;
+    cudaStream_t s = c->stream;
+    // front and buckets once (independent of the unit shape)
+    launch_gene_bits(P, B, true, s);
+    launch_gene_bits(P, B, false, s);
+    launch_dedupe(P, B, s);
+    launch_uniques(P, B, s);
+    launch_buckets(P, B, s);
+    TRY(read_counters(pl));
+    TRY(alloc_entries(pl, c->h_ctr->n_entries));
+    launch_fill(P, B, s);
+    TRY(check_launch());
+    // candidate shapes
+    std::vector<std::pair<int, int>> cand;
+    if (!P.fast) {
+        cand = {{1, 64}, {1, 256}, {1, 1024}};
+    } else if (P.hamming) {
+        const int rxs[2] = {4, 8};
+        for (int rx : rxs) {
+            if (rx == 8 && P.W != 1) continue;
+            for (int ty : {128, 256, 512, 1024})
+                if (ty >= 32 * rx) cand.push_back({rx, ty});
+        }
+    } else {
+        for (int rx : {1, 2}) {
+            if (rx == 2 && P.W != 1) continue;
+            for (int ty : {64, 128, 256, 512, 1024}) cand.push_back({rx, ty});
+        }
+    }
+    if (cand.size() > 16) cand.resize(16);
+    if (P.cap_edges == 0) TRY(alloc_edges(pl, std::max<uint64_t>(4ull * P.N, 1ull << 16)));
+    double best_ms = 1e30;
+    for (auto &cd : cand) {
+        Plan Q = P;
+        if (P.fast) {
+            Q.RX = cd.first;
+            Q.TX = 32 * Q.RX;
+            Q.TY = cd.second;
+        } else {
+            Q.TY = cd.second;
+        }
+        CU(cudaMemsetAsync(&B.ctr->n_binpairs, 0, 4, s));
+        launch_binpairs(Q, B, s);
+        TRY(read_counters(pl));
+        pl.P = Q;
+        TRY(alloc_binpairs(pl, c->h_ctr->n_binpairs));
+        Q.cap_binpairs = pl.P.cap_binpairs;
+        launch_binpairs_fill(Q, B, s);
+        launch_schedule(Q, B, s);
+        float ms_best = 1e30f;
+        for (int rep = 0; rep < 3; ++rep) {
+            CU(cudaMemsetAsync(&B.ctr->unit_cursor, 0, 4, s));
+            CU(cudaMemsetAsync(&B.ctr->edge_reserved, 0, 4, s));
+            CU(cudaMemsetAsync(&B.ctr->n_edges, 0, 4, s));
+            CU(cudaMemsetAsync(&B.ctr->pairs_evaluated, 0, 8, s));
+            CU(cudaEventRecord(c->ev[0], s));
+            Q.cap_edges = pl.P.cap_edges;
+            launch_distance(Q, B, 0, s);
+            CU(cudaEventRecord(c->ev[1], s));
+            TRY(check_launch());
+            CU(cudaEventSynchronize(c->ev[1]));
+            float ms = 0;
+            CU(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+            ms_best = std::min(ms_best, ms);
+            TRY(read_counters(pl));
+            if (c->h_ctr->error & kErrEdgeOverflow) {   // grow and repeat this shape
+                TRY(alloc_edges(pl, (uint64_t)c->h_ctr->edge_reserved + 64ull * kEdgeChunk * 1024));
+                uint32_t clear = 0;
+                CU(cudaMemcpyAsync(&B.ctr->error, &clear, 4, cudaMemcpyHostToDevice, s));
+                --rep;
+                ms_best = 1e30f;
+            }
+        }
+        const int k = best->n_tried++;
+        best->tried_rx[k] = Q.RX;
+        best->tried_ty[k] = (int)Q.TY;
+        best->tried_ms[k] = ms_best;
+        if (ms_best < best_ms) {
+            best_ms = ms_best;
+            best->tile_rx = Q.RX;
+            best->tile_ty = (int)Q.TY;
+            best->ms_distance = ms_best;
+        }
+    }
+    TRY(device_errors(*c->h_ctr));
     return IDB_OK;
 }
 

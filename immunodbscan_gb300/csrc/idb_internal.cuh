@@ -16,6 +16,10 @@ constexpr int kGenericMaxLen = 1024;    // Levenshtein on the generic path
 constexpr int kDepthMax = 50;           // tree-depth histogram cap (cuda/PSDBSCAN.hcu:1029)
 constexpr uint32_t kEdgeChunk = 256;    // edge slots reserved per warp at a time
 constexpr uint32_t kSpinCap = 1u << 22; // bound of every device-side retry loop
+constexpr int kMlpIn = 16;              // learned scheduler: features per bin pair
+constexpr int kMlpHidden = 64;          // two hidden layers of 64
+constexpr int kMlpParams = kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +
+                           kMlpHidden + 1;
 
 // error bits raised by kernels (Counters::error)
 enum : uint32_t {
@@ -196,6 +200,13 @@ void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s);
 void scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, const uint32_t *n_dev,
               uint32_t *total, uint32_t *part, uint32_t part_cap, cudaStream_t s);
 uint32_t scan_part_needed(uint64_t n);
+
+void launch_features(const Buffers &B, uint32_t cap, float *feats, cudaStream_t s);
+void launch_mlp_predict(const Buffers &B, uint32_t cap, const void *wq_bf16, cudaStream_t s);
+void launch_mlp_grad(const float *X, const float *T, uint32_t n, const float *p, float scale,
+                     float *grad, float *loss, cudaStream_t s);
+void launch_adam(float *p, const float *grad, float *m, float *v, float lr, int step, cudaStream_t s);
+void launch_to_bf16(const float *p, void *q, cudaStream_t s);
 
 int sm_count();
 const char *distance_variant_name(const Plan &P);

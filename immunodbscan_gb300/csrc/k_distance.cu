@@ -142,6 +142,8 @@ __device__ __forceinline__ uint32_t find_binpair(const uint32_t *base, uint32_t 
 struct Unit {
     BinPair P;
     uint32_t xbase, nx, ybase, ny;
+    uint32_t bpi;             // index of the bin pair in schedule order
+    long long t0;             // clock64 at the start (profiling only)
 };
 
 __device__ __forceinline__ bool next_unit(const DistArgs &a, uint32_t n_units, uint32_t n_bp,
@@ -151,6 +153,8 @@ __device__ __forceinline__ bool next_unit(const DistArgs &a, uint32_t n_units, u
     u = __shfl_sync(0xFFFFFFFFu, u, 0);
     if (u >= n_units) return false;
     const uint32_t i = find_binpair(a.unit_base, n_bp, u, lane);
+    U.bpi = i;
+    if (a.bp_cycles) U.t0 = clock64();
     U.P = a.bp[i];
     const uint64_t k = u - a.unit_base[i];
     uint32_t cx, cy;
@@ -166,6 +170,12 @@ __device__ __forceinline__ bool next_unit(const DistArgs &a, uint32_t n_units, u
     const uint32_t bn = U.P.same ? U.P.a_n : U.P.b_n;
     U.ny = min(a.TY, bn - U.ybase);
     return true;
+}
+
+// profiling: device cycles spent on each bin pair (learned-schedule training data)
+__device__ __forceinline__ void log_unit(const DistArgs &a, const Unit &U, int lane) {
+    if (a.bp_cycles && lane == 0)
+        atomicAdd(&a.bp_cycles[U.bpi], (unsigned long long)(clock64() - U.t0));
 }
 
 // pairs of the unit that the method evaluates (y after x for a same-bin pair)
@@ -337,6 +347,7 @@ k_hamming(DistArgs a) {
             }
             __syncwarp();
         }
+        log_unit(a, U, lane);
     }
     finish(a, ew, pairs, lane);
 }
@@ -452,6 +463,7 @@ k_levenshtein(DistArgs a) {
             }
             __syncwarp();
         }
+        log_unit(a, U, lane);
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) cols += __shfl_xor_sync(0xFFFFFFFFu, cols, d);
@@ -538,6 +550,7 @@ k_generic(DistArgs a) {
             }
             ew.append(a, lane, ok, min(ux, uy), max(ux, uy));
         }
+        log_unit(a, U, lane);
     }
     finish(a, ew, pairs, lane);
 }

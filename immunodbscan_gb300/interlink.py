@@ -82,8 +82,8 @@ def make_params(threshold=float("nan"), abs_eps=-1, min_pts=2, use_hamming=False
     p.eval_trees = int(bool(eval_trees))
     p.schedule = int(schedule)
     if tune:
-        p.reserved[0] = int(tune[0])
-        p.reserved[1] = int(tune[1])
+        p.tile_rx = int(tune[0])
+        p.tile_ty = int(tune[1])
     return p
 
 

@@ -58,7 +58,9 @@ typedef struct idb_params {
     int32_t  use_hamming;      /* use_hamming                                      */
     int32_t  eval_trees;       /* get_tree_depth_statistics                        */
     int32_t  schedule;         /* 0 = static (pair-count) order, 1 = learned       */
-    int32_t  reserved[6];
+    int32_t  tile_rx;          /* x-entries per lane of a work unit (0 = default)  */
+    int32_t  tile_ty;          /* y-entries of a work unit (0 = default)           */
+    int32_t  reserved[4];
 } idb_params;
 
 /* Input rows (cuda/Interlink.hpp:54-57: zip(V calls, J calls, sequences)). */
@@ -176,6 +178,39 @@ idb_status idb_dedupe_noalloc(const char *seqs, const int64_t *seq_offsets,
                               const uint64_t *v_bits, uint32_t v_words,
                               const uint64_t *j_bits, uint32_t j_words, uint32_t n_rows,
                               uint32_t *rep_out, uint32_t *copies_out, void *stream);
+
+/* Autotuner: builds the buckets of the input once, then times the distance
+   kernel for every candidate work-unit shape (x-entries per lane, y-chunk
+   length) on this data and returns the fastest in best->tile_rx/tile_ty
+   (pass them in idb_params for the real runs).  Host inputs as idb_cluster. */
+typedef struct idb_tuning {
+    int32_t tile_rx, tile_ty;   /* the fastest shape                              */
+    double  ms_distance;        /* its distance-kernel time (best of the repeats)  */
+    int32_t n_tried;
+    int32_t tried_rx[16];
+    int32_t tried_ty[16];
+    double  tried_ms[16];
+} idb_tuning;
+idb_status idb_autotune(idb_context *ctx, const idb_input *in, const idb_params *prm,
+                        idb_tuning *best);
+
+/* Learned schedule.  The persistent distance kernel hands out work units of
+   heavy bin pairs first.  With idb_params.schedule = 1 "heavy" is the cost a
+   small network predicts for the bin pair (16 features -> 64 -> 64 -> 1, ReLU,
+   predicting log2 device cycles; BF16 inference), instead of the pair count.
+   The schedule never changes the result.  Training data comes from
+   idb_profile_binpairs, which runs a clustering with per-bin-pair cycle
+   logging; idb_mlp_train fits the network on the device (FP32, Adam) and
+   idb_mlp_load installs it in a context. */
+#define IDB_MLP_FEATURES 16
+#define IDB_MLP_PARAMS (16 * 64 + 64 + 64 * 64 + 64 + 64 + 1)
+idb_status idb_profile_binpairs(idb_context *ctx, const idb_input *in, const idb_params *prm,
+                                float *features /* cap x IDB_MLP_FEATURES */,
+                                float *log2_cycles /* cap */, uint64_t cap, uint64_t *n_out);
+idb_status idb_mlp_train(idb_context *ctx, const float *features, const float *targets,
+                         uint64_t n, int epochs, float lr, float *params /* in/out */,
+                         float *final_loss);
+idb_status idb_mlp_load(idb_context *ctx, const float *params /* NULL = unload */);
 
 /* Thread-local message of the last failing call ("" if none). */
 size_t idb_last_error(char *buf, size_t size);

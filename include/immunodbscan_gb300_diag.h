@@ -35,6 +35,12 @@ idb_status idb_diag_gene_bits(idb_context *ctx, const char *calls, const int64_t
                               uint32_t n_rows, const char *genes, const int64_t *gene_offsets,
                               uint32_t n_genes, uint64_t *words_out);
 
+/* Gradient of the learned scheduler's loss (mean squared error) with respect to
+   the IDB_MLP_PARAMS parameters, computed by the training kernel (FP32) on n
+   samples; for checking against a CPU implementation. */
+idb_status idb_diag_mlp_grad(idb_context *ctx, const float *params, const float *features,
+                             const float *targets, uint32_t n, float *grad_out, float *loss_out);
+
 #ifdef __cplusplus
 }
 #endif

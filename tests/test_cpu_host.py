@@ -79,3 +79,50 @@ def test_synthetic_workloads_shapes():
             assert np.all(L % 3 == 0)
     w = synth.workload(2, scale=0.002)
     assert w.n_rep == 64
+
+
+def test_host_surface_cpp(tmp_path):
+    """INFO reader, escaped_list_separator tokenizer, CSV reader/writer quirks."""
+    exe = tmp_path / "test_host"
+    subprocess.run(["g++", "-std=c++17", "-O1", "-I", os.path.join(ROOT, "immunodbscan_gb300", "host"),
+                    "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "test_host.cpp"), "-o", str(exe)], check=True)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def _cli():
+    from immunodbscan_gb300 import build
+    return build.CLI
+
+
+def test_psdbscan_help_and_errors(tmp_path):
+    cli = _cli()
+    assert os.path.exists(cli), "build the host first (__graft_entry__.build())"
+    r = subprocess.run([cli, "--help"], capture_output=True, text=True)
+    assert r.returncode == 1 and "--config_file" in r.stdout and "--input" in r.stdout
+    r = subprocess.run([cli, "--config_file", str(tmp_path / "nope.conf")], capture_output=True,
+                       text=True)
+    assert r.returncode == 2 and "cannot open" in r.stderr
+    r = subprocess.run([cli, "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 1
+
+
+def test_mlp_cpu_gradient_is_exact():
+    """The NumPy reference gradient (used to check the device training kernel)
+    against central finite differences."""
+    from immunodbscan_gb300 import learned
+    rng = np.random.default_rng(0)
+    X = rng.normal(0, 1, size=(40, learned.F))
+    T = rng.normal(5, 2, size=40)
+    p = learned.init_params(1).astype(np.float64)
+    g, _ = learned.cpu_grad(p, X, T)
+    idx = rng.choice(len(p), size=60, replace=False)
+    h = 1e-6
+    for k in idx:
+        pp, pm = p.copy(), p.copy()
+        pp[k] += h
+        pm[k] -= h
+        fd = (np.mean((learned.forward(pp, X) - T) ** 2) -
+              np.mean((learned.forward(pm, X) - T) ** 2)) / (2 * h)
+        assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(fd))

