@@ -173,6 +173,61 @@ __global__ void k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
         const uint32_t row = urow[u], L = ulen[u], r = urep[u];
         if (!g.in_range(L)) continue;
         const uint8_t *s = seq + seq_off[row];
+        // the record depends on the unique only: build it once (registers when it
+        // is at most 128 bytes, the fast paths), store it in every bin
+        uint4 rec[8];
+        const bool small = rs16 <= 8;
+        if (small) {
+            if (planes > 0) {
+                uint32_t wd[5][4];
+#pragma unroll
+                for (int p = 0; p < 5; ++p)
+#pragma unroll
+                    for (int w = 0; w < 4; ++w) wd[p][w] = 0;
+#pragma unroll
+                for (int w = 0; w < 4; ++w) {
+                    const uint32_t i0 = 32u * w, i1 = min(L, i0 + 32u);
+                    for (uint32_t i = i0; i < i1; ++i) {
+                        const uint32_t c = cm[s[i]];
+#pragma unroll
+                        for (int p = 0; p < 5; ++p) wd[p][w] |= ((c >> p) & 1u) << (i - i0);
+                    }
+                }
+                // layout: word p*W + w
+                uint32_t flat[32];
+#pragma unroll
+                for (int k = 0; k < 32; ++k) flat[k] = 0;
+#pragma unroll
+                for (int p = 0; p < 5; ++p)
+#pragma unroll
+                    for (int w = 0; w < 4; ++w)
+                        if (p < planes && (uint32_t)w < W) {
+                            const uint32_t k = (uint32_t)p * W + w;
+#pragma unroll
+                            for (int kk = 0; kk < 32; ++kk)
+                                if ((uint32_t)kk == k) flat[kk] = wd[p][w];
+                        }
+#pragma unroll
+                for (int q = 0; q < 8; ++q) rec[q] = make_uint4(flat[4 * q], flat[4 * q + 1], flat[4 * q + 2], flat[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    uint32_t wv[4];
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        uint32_t acc = 0;
+#pragma unroll
+                        for (int t = 0; t < 4; ++t) {
+                            const uint32_t i = q * 16 + e * 4 + t;
+                            const uint32_t c = i < L ? cm[s[i]] : 0u;
+                            acc |= c << (8 * t);
+                        }
+                        wv[e] = acc;
+                    }
+                    rec[q] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+                }
+            }
+        }
         for (uint32_t vw = 0; vw < g.VW; ++vw) {
             uint64_t vb = vbits[(size_t)row * g.VW + vw];
             while (vb) {
@@ -196,41 +251,27 @@ __global__ void k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                         // side record: signature below (v, j) and the unique id
                         ent_meta[pos] = make_uint4((uint32_t)sv, (uint32_t)(sv >> 32), (uint32_t)sj, u);
                         uint4 *dst = ent_rec + pos * rs16;
-                        if (planes > 0) {
-                            // bit planes, written word by word (16 bytes at a time)
-                            for (uint32_t q = 0; q < rs16; ++q) {
-                                uint32_t wv[4];
+                        if (small) {
 #pragma unroll
-                                for (int e = 0; e < 4; ++e) {
-                                    const uint32_t widx = q * 4 + e;
-                                    const uint32_t p = widx / W, w = widx % W;
-                                    uint32_t acc = 0;
-                                    if (p < (uint32_t)planes) {
-                                        const uint32_t i0 = w * 32;
-                                        const uint32_t i1 = min(L, i0 + 32);
-                                        for (uint32_t i = i0; i < i1; ++i)
-                                            acc |= ((uint32_t)(cm[s[i]] >> p) & 1u) << (i - i0);
-                                    }
-                                    wv[e] = acc;
+                            for (int q = 0; q < 8; ++q)
+                                if ((uint32_t)q < rs16) dst[q] = rec[q];
+                            continue;
+                        }
+                        // long records (generic path): code bytes, 16 at a time
+                        for (uint32_t q = 0; q < rs16; ++q) {
+                            uint32_t wv[4];
+#pragma unroll
+                            for (int e = 0; e < 4; ++e) {
+                                uint32_t acc = 0;
+#pragma unroll
+                                for (int t = 0; t < 4; ++t) {
+                                    const uint32_t i = q * 16 + e * 4 + t;
+                                    const uint32_t c = i < L ? cm[s[i]] : 0u;
+                                    acc |= c << (8 * t);
                                 }
-                                dst[q] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+                                wv[e] = acc;
                             }
-                        } else {
-                            for (uint32_t q = 0; q < rs16; ++q) {
-                                uint32_t wv[4];
-#pragma unroll
-                                for (int e = 0; e < 4; ++e) {
-                                    uint32_t acc = 0;
-#pragma unroll
-                                    for (int t = 0; t < 4; ++t) {
-                                        const uint32_t i = q * 16 + e * 4 + t;
-                                        const uint32_t c = i < L ? cm[s[i]] : 0u;
-                                        acc |= c << (8 * t);
-                                    }
-                                    wv[e] = acc;
-                                }
-                                dst[q] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
-                            }
+                            dst[q] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
                         }
                     }
                 }

@@ -93,8 +93,10 @@ __global__ void k_const_strings(uint8_t *blob, int64_t *off, uint32_t N) {
 // name longer than 255 bytes, falls back to one warp per row and one lane per
 // gene.
 // ---------------------------------------------------------------------------
-constexpr int kGbRows = 128;
-constexpr int kGbBytes = 12288;
+constexpr int kGbWarps = 8;                 // warps per block
+constexpr int kGbRows = 32;                 // rows per warp chunk
+constexpr int kGbBytes = 2048;              // staged call bytes per warp
+constexpr int kGbNameBytes = 16384;         // gene names kept in shared memory
 
 __device__ __forceinline__ bool name_at(const uint8_t *c, uint32_t cl, const uint8_t *name,
                                         uint32_t nl) {
@@ -133,104 +135,137 @@ __device__ void gene_bits_row_naive(const uint8_t *c, uint32_t cl, const uint8_t
         if (lane == w && (uint32_t)w < GW) out[w] = acc[w];
 }
 
-__global__ void __launch_bounds__(kThreads)
+// Each warp takes 32 rows at a time: their call bytes are staged in the warp's
+// shared-memory slice with 4-byte loads, bytes that start a gene name are
+// compacted into a candidate queue with ballots, and the lanes then verify one
+// candidate each (rolling hash, table probe at every name length, byte check
+// against the names in shared memory), setting bits with shared atomics.
+__global__ void __launch_bounds__(kGbWarps * 32)
 k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, uint32_t N,
             const uint8_t *__restrict__ genes, const int32_t *__restrict__ goff, uint32_t G,
             uint32_t GW, const GeneEntry *__restrict__ tab, GeneMatcher gm,
             uint64_t *__restrict__ bits) {
-    extern __shared__ uint8_t sm[];
+    extern __shared__ __align__(16) uint8_t sm[];
+    // block-wide tables
     GeneEntry *s_tab = reinterpret_cast<GeneEntry *>(sm);
     int32_t *s_goff = reinterpret_cast<int32_t *>(s_tab + gm.ts);
-    uint64_t *s_bits = reinterpret_cast<uint64_t *>(
-        reinterpret_cast<uintptr_t>(s_goff + G + 1 + 1) & ~(uintptr_t)7);
-    uint32_t *s_roff = reinterpret_cast<uint32_t *>(s_bits + kGbRows * GW);
-    uint16_t *s_cand = reinterpret_cast<uint16_t *>(s_roff + kGbRows + 1);
-    uint8_t *s_bytes = reinterpret_cast<uint8_t *>(s_cand + kGbBytes);
-    __shared__ uint32_t s_ncand, s_first[8], s_len[8];
-    __shared__ int s_fit;
+    const uint32_t name_bytes = (uint32_t)goff[G] <= (uint32_t)kGbNameBytes ? (uint32_t)goff[G] : 0u;
+    uint8_t *s_names = reinterpret_cast<uint8_t *>(s_goff + G + 1);
+    // per-warp slices (16-byte aligned)
+    uintptr_t wbase = (reinterpret_cast<uintptr_t>(s_names + name_bytes) + 15) & ~(uintptr_t)15;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const size_t slice = (size_t)kGbBytes + 4 + 2 * kGbBytes + 4 * (kGbRows + 1) +
+                         8 * (size_t)kGbRows * GW + 16;
+    uint8_t *wsm = reinterpret_cast<uint8_t *>(wbase + (slice * wid + 15) / 16 * 16);
+    uint64_t *w_bits = reinterpret_cast<uint64_t *>(wsm);                     // [32*GW]
+    uint32_t *w_roff = reinterpret_cast<uint32_t *>(w_bits + kGbRows * GW);   // [33]
+    uint16_t *w_cand = reinterpret_cast<uint16_t *>(w_roff + kGbRows + 1);    // [kGbBytes]
+    uint32_t *w_words = reinterpret_cast<uint32_t *>(
+        (reinterpret_cast<uintptr_t>(w_cand + kGbBytes) + 3) & ~(uintptr_t)3); // [kGbBytes/4+1]
+    const uint8_t *w_bytes0 = reinterpret_cast<const uint8_t *>(w_words);
+    __shared__ uint32_t s_first[8], s_len[8];
     for (uint32_t k = threadIdx.x; k < gm.ts; k += blockDim.x) s_tab[k] = tab[k];
     for (uint32_t k = threadIdx.x; k <= G; k += blockDim.x) s_goff[k] = goff[k];
-    if (threadIdx.x < 8) {
-        s_first[threadIdx.x] = gm.firstmask[threadIdx.x];
-        s_len[threadIdx.x] = gm.lenmask[threadIdx.x];
-    }
+    for (uint32_t k = threadIdx.x; k < name_bytes; k += blockDim.x) s_names[k] = genes[k];
+#pragma unroll
+    for (int k = 0; k < 8; ++k)      // constant indices keep the parameter out of local memory
+        if (threadIdx.x == k) {
+            s_first[k] = gm.firstmask[k];
+            s_len[k] = gm.lenmask[k];
+        }
     __syncthreads();
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint8_t *names = name_bytes ? s_names : genes;
     const uint32_t nchunks = (N + kGbRows - 1) / kGbRows;
-    for (uint32_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    const uint32_t gwarp = blockIdx.x * kGbWarps + wid, nwarps = gridDim.x * kGbWarps;
+    for (uint32_t ch = gwarp; ch < nchunks; ch += nwarps) {
         const uint32_t r0 = ch * kGbRows, nr = min((uint32_t)kGbRows, N - r0);
         const int64_t base = off[r0];
         const int64_t total = off[r0 + nr] - base;
-        if (threadIdx.x == 0) {
-            s_ncand = 0;
-            s_fit = total <= kGbBytes && !gm.long_names;
-        }
-        __syncthreads();
-        if (!s_fit) {   // slow path: one warp per row, names from global memory
-            for (uint32_t r = wid; r < nr; r += blockDim.x / 32) {
+        // 4-byte words covering [calls + base, calls + base + total), aligned on the
+        // absolute address; the first and last word are read byte by byte where they
+        // reach outside that range, so no byte outside the chunk is touched.
+        const uintptr_t a0 = reinterpret_cast<uintptr_t>(calls + base);
+        const uint32_t shift = (uint32_t)(a0 & 3u);
+        if (total + shift + 4 > kGbBytes || gm.long_names) {  // slow path: warp per row
+            for (uint32_t r = 0; r < nr; ++r) {
                 const int64_t c0 = off[r0 + r];
-                gene_bits_row_naive(calls + c0, (uint32_t)(off[r0 + r + 1] - c0), genes, s_goff, G,
-                                    GW, lane, bits + (size_t)(r0 + r) * GW);
+                gene_bits_row_naive(calls + c0, (uint32_t)(off[r0 + r + 1] - c0), names, s_goff,
+                                    G, GW, lane, bits + (size_t)(r0 + r) * GW);
             }
-            __syncthreads();
             continue;
         }
-        for (uint32_t k = threadIdx.x; k <= nr; k += blockDim.x)
-            s_roff[k] = (uint32_t)(off[r0 + k] - base);
-        for (uint32_t k = threadIdx.x; k < nr * GW; k += blockDim.x) s_bits[k] = 0;
-        for (uint32_t q = threadIdx.x; q < (uint32_t)total; q += blockDim.x) s_bytes[q] = calls[base + q];
-        __syncthreads();
-        // candidate positions (warp-aggregated append)
-        for (uint32_t q0 = 0; q0 < (uint32_t)total; q0 += blockDim.x) {
-            const uint32_t q = q0 + threadIdx.x;
+        for (uint32_t k = lane; k <= nr; k += 32) w_roff[k] = (uint32_t)(off[r0 + k] - base) + shift;
+        for (uint32_t k = lane; k < nr * GW; k += 32) w_bits[k] = 0;
+        const uint32_t nwords = (uint32_t)((total + shift + 3) >> 2);
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(a0 - shift);
+        const uint32_t qend = shift + (uint32_t)total;
+        for (uint32_t k = lane; k < nwords; k += 32) {
+            if (4 * k >= shift && 4 * k + 4 <= qend) {
+                w_words[k] = src[k];
+            } else {
+                uint32_t v = 0;
+                for (uint32_t b = 0; b < 4; ++b) {
+                    const uint32_t q = 4 * k + b;
+                    if (q >= shift && q < qend) v |= (uint32_t)calls[base + (q - shift)] << (8 * b);
+                }
+                w_words[k] = v;
+            }
+        }
+        __syncwarp();
+        // candidates: positions whose byte starts some gene name
+        uint32_t ncand = 0;
+        for (uint32_t q0 = shift; q0 < qend; q0 += 32) {
+            const uint32_t q = q0 + lane;
             bool cand = false;
-            if (q < (uint32_t)total) {
-                const uint32_t c = s_bytes[q];
+            if (q < qend) {
+                const uint32_t c = w_bytes0[q];
                 cand = (s_first[c >> 5] >> (c & 31)) & 1u;
             }
             const uint32_t m = __ballot_sync(0xFFFFFFFFu, cand);
-            uint32_t b = 0;
-            if (lane == 0 && m) b = atomicAdd(&s_ncand, (uint32_t)__popc(m));
-            b = __shfl_sync(0xFFFFFFFFu, b, 0);
-            if (cand) s_cand[b + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+            if (cand) w_cand[ncand + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+            ncand += __popc(m);
         }
-        __syncthreads();
-        // verify candidates: rolling hash + table lookups at the name lengths
-        const uint32_t nc = s_ncand;
-        for (uint32_t k = threadIdx.x; k < nc; k += blockDim.x) {
-            const uint32_t q = s_cand[k];
-            uint32_t lo = 0, hi = nr;   // row: largest r with s_roff[r] <= q
+        __syncwarp();
+        for (uint32_t k = lane; k < ncand; k += 32) {
+            const uint32_t q = w_cand[k];
+            uint32_t lo = 0, hi = nr;   // row: largest r with w_roff[r] <= q
             while (hi - lo > 1) {
                 const uint32_t mid = (lo + hi) >> 1;
-                if (s_roff[mid] <= q) lo = mid; else hi = mid;
+                if (w_roff[mid] <= q) lo = mid; else hi = mid;
             }
-            const uint32_t row = lo, end = s_roff[row + 1];
+            const uint32_t row = lo, end = w_roff[row + 1];
             uint32_t h = 0;
             for (uint32_t t = 0; t < gm.maxlen && q + t < end; ++t) {
-                h = h * kGeneHashMul + s_bytes[q + t];
+                h = h * kGeneHashMul + w_bytes0[q + t];
                 const uint32_t L = t + 1;
                 if (!((s_len[L >> 5] >> (L & 31)) & 1u)) continue;
                 uint32_t sl = h & (gm.ts - 1);
                 while (s_tab[sl].len != 0) {
                     const GeneEntry e = s_tab[sl];
                     if (e.h == h && e.len == L) {
-                        const uint8_t *name = genes + s_goff[e.gene];
+                        const uint8_t *name = names + s_goff[e.gene];
                         uint32_t i = 0;
-                        while (i < L && name[i] == s_bytes[q + i]) ++i;
+                        while (i < L && name[i] == w_bytes0[q + i]) ++i;
                         if (i == L)
-                            atomicOr(reinterpret_cast<unsigned long long *>(
-                                         &s_bits[row * GW + (e.gene >> 6)]),
+                            atomicOr(reinterpret_cast<unsigned long long *>(&w_bits[row * GW + (e.gene >> 6)]),
                                      1ull << (e.gene & 63));
                     }
                     sl = (sl + 1) & (gm.ts - 1);
                 }
             }
         }
-        __syncthreads();
-        for (uint32_t k = threadIdx.x; k < nr * GW; k += blockDim.x)
-            bits[(size_t)r0 * GW + k] = s_bits[k];
-        __syncthreads();
+        __syncwarp();
+        for (uint32_t k = lane; k < nr * GW; k += 32) bits[(size_t)r0 * GW + k] = w_bits[k];
+        __syncwarp();
     }
+}
+
+size_t gene_bits_smem(uint32_t G, uint32_t GW, uint32_t ts, uint32_t name_bytes) {
+    const size_t slice = (size_t)kGbBytes + 4 + 2 * kGbBytes + 4 * (kGbRows + 1) +
+                         8 * (size_t)kGbRows * GW + 16;
+    const size_t nb = name_bytes <= (uint32_t)kGbNameBytes ? name_bytes : 0;
+    return sizeof(GeneEntry) * ts + sizeof(int32_t) * (G + 1) + nb + 16 +
+           kGbWarps * ((slice + 15) / 16 * 16);
 }
 
 // No gene column: every row carries bit 0 ("V" against ["V"]).
@@ -537,9 +572,8 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     const int32_t *goff = v_column ? B.vg_off : B.jg_off;
     const GeneEntry *tab = v_column ? B.vtab : B.jtab;
     const GeneMatcher &gm = v_column ? P.vmatch : P.jmatch;
-    size_t smem = sizeof(GeneEntry) * gm.ts + sizeof(int32_t) * (G + 2) + 8 +
-                  sizeof(uint64_t) * kGbRows * GW + sizeof(uint32_t) * (kGbRows + 1) +
-                  sizeof(uint16_t) * kGbBytes + kGbBytes + 16;
+    const uint32_t name_bytes = v_column ? P.gene_bytes_v : P.gene_bytes_j;
+    const size_t smem = gene_bits_smem(G, GW, gm.ts, name_bytes);
     static thread_local size_t attr_set = 0;
     if (smem > 48 * 1024 && smem > attr_set) {
         cudaFuncSetAttribute(k_gene_bits, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -547,9 +581,11 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     }
     const uint32_t nchunks = (P.N + kGbRows - 1) / kGbRows;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gene_bits, kThreads, smem);
-    const int grid = (int)std::min<uint64_t>(nchunks, (uint64_t)sm_count() * (per_sm > 0 ? per_sm : 1));
-    k_gene_bits<<<grid, kThreads, smem, s>>>(calls, off, P.N, genes, goff, G, GW, tab, gm, bits);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gene_bits, kGbWarps * 32, smem);
+    const uint64_t want = (nchunks + kGbWarps - 1) / kGbWarps;
+    const int grid = (int)std::min<uint64_t>(want, (uint64_t)sm_count() * (per_sm > 0 ? per_sm : 1));
+    k_gene_bits<<<grid > 0 ? grid : 1, kGbWarps * 32, smem, s>>>(calls, off, P.N, genes, goff, G, GW,
+                                                                  tab, gm, bits);
 }
 
 void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s) {

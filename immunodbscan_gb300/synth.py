@@ -146,26 +146,41 @@ def _split_sizes(raw: np.ndarray, total: int) -> np.ndarray:
     return base
 
 
-def _call_strings(rng, sets: List[np.ndarray], names: List[bytes], species=b"Homsap "):
-    """IMGT-style call string for each gene-index set."""
+def _pick_sets(rng, n_sets: int, n_genes: int, usage: Optional[np.ndarray]) -> np.ndarray:
+    """n_sets gene sets of 1-3 distinct genes (weighted by `usage` if given), as
+    bitmasks (uint64 words, one row per set).  Sampling without replacement by
+    the Gumbel top-k rule."""
+    k = rng.integers(1, 4, size=n_sets)
+    logp = np.log(usage) if usage is not None else np.zeros(n_genes)
+    keys = logp[None, :] + rng.gumbel(size=(n_sets, n_genes))
+    top = np.argsort(-keys, axis=1)[:, :3]
+    nw = (n_genes + 63) // 64
+    masks = np.zeros((n_sets, nw), np.uint64)
+    for slot in range(min(3, n_genes)):
+        sel = k > slot
+        g = top[sel, slot]
+        np.bitwise_or.at(masks, (np.nonzero(sel)[0], g // 64), np.uint64(1) << (g % 64).astype(np.uint64))
+    return masks
+
+
+def _call_strings(rng, masks: np.ndarray, names: List[bytes], species=b"Homsap ") -> List[bytes]:
+    """IMGT-style call string for each gene bitmask, alleles *01-*03 drawn at random."""
+    tokens = [[species + names[g] + b"%02d F" % a for a in (1, 2, 3)] for g in range(len(names))]
+    alle = rng.integers(0, 3, size=(len(masks), 4))
     out = []
-    for s in sets:
-        parts = [species + names[g] + b"%02d F" % (1 + int(rng.integers(0, 3))) for g in s]
+    for i in range(len(masks)):
+        parts = []
+        t = 0
+        for w in range(masks.shape[1]):
+            m = int(masks[i, w])
+            while m:
+                low = m & -m
+                g = w * 64 + low.bit_length() - 1
+                parts.append(tokens[g][alle[i, t & 3]])
+                t += 1
+                m ^= low
         out.append(b", or ".join(parts))
     return out
-
-
-def _pick_sets(rng, n_sets: int, n_genes: int, usage: Optional[np.ndarray]):
-    sets = []
-    k = rng.integers(1, 4, size=n_sets)
-    for i in range(n_sets):
-        kk = min(int(k[i]), n_genes)
-        if usage is None:
-            s = rng.choice(n_genes, size=kk, replace=False)
-        else:
-            s = rng.choice(n_genes, size=kk, replace=False, p=usage)
-        sets.append(np.sort(s))
-    return sets
 
 
 def _zipf_usage(n: int, a: float) -> np.ndarray:
@@ -244,15 +259,16 @@ def _families(rng, *, n_rows: int, n_fam: int, sizes: str, size_param: float,
     vsets = _pick_sets(rng, n_fam, len(v_names), v_usage)
     jsets = _pick_sets(rng, n_fam, len(j_names), j_usage)
 
-    def variants(sets, n_genes):
-        out = []
-        for s in sets:
-            extra = int(rng.integers(0, n_genes))
-            out.append(np.unique(np.append(s, extra)))
+    def variants(masks, n_genes):
+        # the family's set plus one random gene (possibly already in it)
+        extra = rng.integers(0, n_genes, size=len(masks))
+        out = masks.copy()
+        np.bitwise_or.at(out, (np.arange(len(masks)), extra // 64),
+                         np.uint64(1) << (extra % 64).astype(np.uint64))
         return out
 
-    vcall = _call_strings(rng, vsets + variants(vsets, len(v_names)), v_names)
-    jcall = _call_strings(rng, jsets + variants(jsets, len(j_names)), j_names)
+    vcall = _call_strings(rng, np.concatenate([vsets, variants(vsets, len(v_names))]), v_names)
+    jcall = _call_strings(rng, np.concatenate([jsets, variants(jsets, len(j_names))]), j_names)
     which_v = fam + n_fam * (rng.random(n) < variant_rate)
     which_j = fam + n_fam * (rng.random(n) < variant_rate)
 

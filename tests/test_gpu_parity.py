@@ -232,18 +232,19 @@ def test_gene_bits_known_answers(gpu_ctx):
     assert got.tolist() == S1_WORDS
 
 
-@pytest.mark.parametrize("long_calls", [False, True])
-def test_gene_bits_vs_oracle(gpu_ctx, long_calls):
+@pytest.mark.parametrize("mode", ["short", "long_calls", "long_names"])
+def test_gene_bits_vs_oracle(gpu_ctx, mode):
     """Random names (incl. empty, repeated, overlapping and prefix-sharing ones)
-    against random calls; long calls overflow the staging buffer and take the
-    per-row path."""
-    rng = np.random.default_rng(5 + long_calls)
+    against random calls.  Long calls overflow a warp's staging buffer for some
+    32-row chunks (those take the per-row path, the rest the staged path); a name
+    longer than 255 bytes sends every row through the per-row path."""
+    rng = np.random.default_rng(5 + ["short", "long_calls", "long_names"].index(mode))
     alpha = list(b"ACGT*-I0123")
     genes = [bytes(rng.choice(alpha, size=int(rng.integers(1, 7))).astype(np.uint8)) for _ in range(150)]
-    genes += [b"", genes[3], genes[7] + b"*"] + ([b"A" * 300] if long_calls else [])
+    genes += [b"", genes[3], genes[7] + b"*"] + ([b"A" * 300] if mode == "long_names" else [])
     calls = []
     for i in range(3000):
-        n = int(rng.integers(0, 400 if long_calls else 60))
+        n = int(rng.integers(0, 60 if mode == "short" else (400 if i % 200 < 40 else 30)))
         s = bytearray(rng.choice(alpha, size=n).astype(np.uint8).tobytes())
         if rng.random() < 0.5 and n > 10:
             g = genes[int(rng.integers(0, len(genes)))]
