@@ -53,6 +53,10 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--tile", default=None,
+                    help="work-unit shape RX,TY (x-entries per lane, y-chunk); skips the autotuner")
+    ap.add_argument("--static-only", action="store_true",
+                    help="time the static schedule only (no network is trained)")
     ap.add_argument("--cpu-seconds", type=float, default=None,
                     help="CPU time budget of the oracle sample (per step for --impl reference; "
                          "default 10 s, or 150 s / steps for the reference arm)")
@@ -205,6 +209,26 @@ def reference_arm(args, world, rank, w):
     print(json.dumps(line), flush=True)
 
 
+def prediction_quality(w, ctx, shape, params):
+    """How well the trained network predicts the work of the timed workload's
+    bin pairs (a profile of that workload, not seen in training), next to the
+    best the static cost can do: a least-squares line from log2(pairs) to the
+    same measured log2 cycles."""
+    from immunodbscan_gb300 import learned
+    X, T = learned.profile(w, ctx, tune=shape)
+    T = T.astype(np.float64)
+    pred = learned.forward(params, X)
+    f = X[:, 6].astype(np.float64)                 # log2(1 + pairs)
+    A = np.stack([f, np.ones_like(f)], 1)
+    coef = np.linalg.lstsq(A, T, rcond=None)[0]
+    var = float(np.var(T)) or 1.0
+    mse_mlp = float(np.mean((pred - T) ** 2))
+    mse_static = float(np.mean((A @ coef - T) ** 2))
+    return {"eval_binpairs": int(len(T)), "eval_mse_log2_cycles": mse_mlp,
+            "eval_r2": 1.0 - mse_mlp / var, "static_fit_mse_log2_cycles": mse_static,
+            "static_fit_r2": 1.0 - mse_static / var}
+
+
 def time_batch(batch, steps, warmup, world, clocks=None):
     """Warm up, then time exactly `steps` graph replays (device time per step)."""
     import torch
@@ -258,27 +282,38 @@ def main():
     admissible = int(adm.value)
 
     # autotuner: work-unit shape measured on this workload (setup, untimed)
-    tune_rec = tuning.measure(w, ctx_setup)
-    shape = (tune_rec["rx"], tune_rec["ty"])
+    if args.tile:
+        shape = tuple(int(x) for x in args.tile.split(","))
+        tune_rec = {"tried": [], "source": "--tile"}
+    else:
+        tune_rec = tuning.measure(w, ctx_setup)
+        shape = (tune_rec["rx"], tune_rec["ty"])
 
     # learned schedule: trained on a profile of a differently seeded workload of
     # the same kind (setup, untimed)
     t0 = time.time()
-    wt = synth.workload(args.workload, scale=min(args.scale, 0.1), seed=4242 + args.workload)
-    X, T = learned.profile(wt, ctx_setup, tune=shape)
-    params, loss = learned.train(X, T, ctx_setup, epochs=args.mlp_epochs)
-    learned.install(ctx_learned, params)
+    learn = not args.static_only
+    X = T = None
+    loss = float("nan")
+    if learn:
+        wt = synth.workload(args.workload, scale=min(args.scale, 0.1), seed=4242 + args.workload)
+        X, T = learned.profile(wt, ctx_setup, tune=shape)
+        params, loss = learned.train(X, T, ctx_setup, epochs=args.mlp_epochs)
+        learned.install(ctx_learned, params)
     train_s = time.time() - t0
 
     # batched graph path, static heavy-first order
     b_static = DeviceBatch(w, ctx_static, schedule=0, tune=shape)
     b_static.plan()
-    r_static = time_batch(b_static, args.steps, args.warmup, world)
-    # batched graph path, learned order (the headline value)
-    b_learned = DeviceBatch(w, ctx_learned, schedule=1, tune=shape)
-    b_learned.plan()
     clocks = ClockSampler(local)
-    r = time_batch(b_learned, args.steps, args.warmup, world, clocks)
+    r_static = time_batch(b_static, args.steps, args.warmup, world, None if learn else clocks)
+    if learn:
+        # batched graph path, learned order (the headline value)
+        b_learned = DeviceBatch(w, ctx_learned, schedule=1, tune=shape)
+        b_learned.plan()
+        r = time_batch(b_learned, args.steps, args.warmup, world, clocks)
+    else:
+        b_learned, r = b_static, r_static
     step_ms = r["step_ms"]
     value = world * admissible / (step_ms * 1e-3) / 1e9
     last = r["last"]
@@ -295,7 +330,8 @@ def main():
                       "global_batch": n * world, "seq_len": int(w.lengths().max()),
                       "parallelism": "replicas only" if world > 1 else "single GPU",
                       "l2": "inputs and working set larger than L2 (129 MB)",
-                      "schedule": "learned (2x64 MLP, BF16 inference)",
+                      "schedule": ("learned (2x64 MLP, BF16 inference)" if learn else
+                                   "static (heavy-first by pair count)"),
                       "tile": {"rx": shape[0], "ty": shape[1], "source": "autotuner"}},
            "seq_per_s": world * n / (step_ms * 1e-3), "admissible_pairs": admissible,
            "pairs_evaluated": int(last.pairs_evaluated),
@@ -309,11 +345,21 @@ def main():
            "static_schedule": {"ms_per_step": r_static["step_ms"],
                                "distance_ms": r_static["ms_dist"],
                                "learned_gain": r_static["step_ms"] / step_ms,
+                               "pairs_evaluated": int(r_static["last"].pairs_evaluated),
+                               "neighbour_pairs": int(r_static["last"].neighbour_pairs),
+                               "n_clusters": int(r_static["last"].n_clusters),
                                "identical_partitions": bool(np.array_equal(clone_s, clone_b) and
-                                                            np.array_equal(core_s, core_b))},
-           "autotune": {"tried": tune_rec["tried"]},
-           "learned_model": {"train_binpairs": int(len(T)), "mse_log2_cycles": loss,
-                             "setup_seconds": train_s}}
+                                                            np.array_equal(core_s, core_b)),
+                               "differing_rows": int(np.count_nonzero((clone_s != clone_b) |
+                                                                      (core_s != core_b)))},
+           "autotune": {"tried": tune_rec["tried"]}}
+    if learn:
+        out["learned_model"] = {"train_binpairs": int(len(T)), "train_mse_log2_cycles": loss,
+                                "setup_seconds": train_s, **prediction_quality(w, ctx_setup, shape,
+                                                                                params)}
+    else:
+        out["config"]["tile"]["source"] = tune_rec.get("source", "autotuner")
+        del out["static_schedule"]
 
     # roofline of the distance kernel: integer logic against the measured int peak
     gops = C.c_double()
@@ -339,7 +385,7 @@ def main():
     # e2e through idb_cluster (the InterlinkClass replacement) with pinned host buffers
     if not args.no_e2e:
         hin, hkeep = build_host_input(w, pinned=True)
-        prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, 1, shape)
+        prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, int(learn), shape)
         clone = torch.empty(n, dtype=torch.int32).pin_memory()
         core = torch.empty(n, dtype=torch.int32).pin_memory()
         copies = torch.empty(n, dtype=torch.int32).pin_memory()
@@ -359,7 +405,8 @@ def main():
         out["e2e"] = {"value": world * admissible / e2e_s / 1e9, "unit": UNIT,
                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * n,
                       "ms_per_step": e2e_s * 1e3, "seq_per_s": world * n / e2e_s,
-                      "api": "idb_cluster (host buffers, learned schedule)"}
+                      "api": "idb_cluster (host buffers, %s schedule)" % ("learned" if learn else
+                                                                           "static")}
         same = (np.array_equal(clone.numpy().view(np.uint32), clone_b) and
                 np.array_equal(core.numpy(), core_b))
         out["e2e"]["identical_partitions_vs_batched"] = bool(same)

@@ -623,8 +623,8 @@ static DistArgs make_args(const Plan &P, const Buffers &B) {
     a.edges = B.edges;
     a.cap_edges = P.cap_edges;
     a.ctr = B.ctr;
-    a.bp_cycles = nullptr;
-    a.bp_hits = nullptr;
+    a.bp_cycles = B.bp_cycles;   // set only while profiling
+    a.bp_hits = B.bp_hits;
     a.meta = B.ent_meta;
     a.sig_exact = P.sig_exact ? 1 : 0;
     return a;

@@ -157,8 +157,11 @@ class Table {
         Benchmark::instance().message("Deleting " + std::to_string(n) + " rows");
         for (auto &col : cols_) {
             size_t t = 0;
-            for (size_t r = 0; r < col.size(); ++r)
-                if (!del[r]) col[t++] = std::move(col[r]);
+            for (size_t r = 0; r < col.size(); ++r) {
+                if (del[r]) continue;
+                if (t != r) col[t] = std::move(col[r]);   // no self-move: it may empty the string
+                ++t;
+            }
             col.resize(t);
         }
     }

@@ -108,6 +108,45 @@ def test_psdbscan_help_and_errors(tmp_path):
     assert r.returncode == 1
 
 
+@pytest.mark.parametrize("noise", [False, True])
+def test_psdbscan_table_flow_with_stand_in_library(tmp_path, noise):
+    """The psdbscan host built against tests/cpp/fake_idb.cpp (row r of the
+    clustered table gets clone r%3, core r%2, copies 1+r%4): rows with an empty
+    sequence, V or J value are deleted before clustering, the read columns keep
+    their values in row order, the results line up with the surviving rows,
+    noise rows (clone 0) go when configured, an unread column is written empty."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from test_gpu_cli import _write_inputs
+    from immunodbscan_gb300 import synth
+    d = tmp_path / "bin"
+    d.mkdir()
+    inc = ["-I", os.path.join(ROOT, "include")]
+    subprocess.run(["g++", "-std=c++17", "-O1", "-shared", "-fPIC", *inc,
+                    os.path.join(ROOT, "tests", "cpp", "fake_idb.cpp"), "-o",
+                    str(d / "libimmunodbscan_gb300.so")], check=True)
+    subprocess.run(["g++", "-std=c++17", "-O1", *inc, "-I", os.path.join(ROOT, "immunodbscan_gb300", "host"),
+                    os.path.join(ROOT, "immunodbscan_gb300", "host", "psdbscan.cpp"), "-o",
+                    str(d / "psdbscan"), "-L" + str(d), "-limmunodbscan_gb300", "-Wl,-rpath,$ORIGIN"],
+                   check=True)
+    w = synth.workload(0, scale=0.05)
+    cf, inp, keep = _write_inputs(tmp_path, w, False, noise)
+    r = subprocess.run([str(d / "psdbscan"), "--config_file", str(cf), "--input", str(inp)],
+                       capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = (tmp_path / "output_repertoire.csv").read_text().split("\n")
+    assert lines[0].split("\t") == ["Original.Filename", "ID.code", "V_CALL", "CDR3", "Not.In.Input",
+                                    "Cores", "Copies", "Clone"]
+    assert lines[-1] == ""
+    body = [l.split("\t") for l in lines[1:-1]]
+    want = [(k, i) for k, i in enumerate(keep) if not (noise and k % 3 == 0)]
+    assert len(body) == len(want)
+    for b, (k, i) in zip(body, want):
+        assert b == [str(inp), "id%d" % i, w.vcall(i).decode(), w.seq(i).decode(), "",
+                     str(k % 2), str(1 + k % 4), str(k % 3)]
+    assert (tmp_path / "benchmark_repertoire.csv").exists()
+
+
 def test_mlp_cpu_gradient_is_exact():
     """The NumPy reference gradient (used to check the device training kernel)
     against central finite differences."""
