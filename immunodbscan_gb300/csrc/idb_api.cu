@@ -69,7 +69,7 @@ enum BufId {
     bURow, bUCopies, bULen, bURep, bBinHist, bBinCursor, bEntUid, bEntRec, bBpCount, bBp,
     bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bDeg, bGOff, bGCur, bAdj, bCnt, bUCore,
     bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
-    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bNumBufs
+    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bNumBufs
 };
 
 }  // namespace
@@ -417,6 +417,16 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
 }
 
 // Workspace for everything sized by N and the plan.
+// The call-string table of the gene-bitset phase lives in the duplicate
+// table's memory (4*tcap bytes, at most 2^20 slots of 8 bytes).
+void set_call_scratch(Buffers &B, uint64_t tcap, uint32_t *aux) {
+    B.call_tab = reinterpret_cast<unsigned long long *>(B.table);
+    B.call_mask = (uint32_t)(std::min<uint64_t>(tcap / 2, 1u << 20) - 1);
+    B.call_ref = B.slot;
+    B.call_todo = B.rep_row;
+    B.call_ntodo = aux;
+}
+
 idb_status alloc_fixed(Pipeline &pl) {
     idb_context *c = pl.c;
     Plan &P = pl.P;
@@ -468,6 +478,8 @@ idb_status alloc_fixed(Pipeline &pl) {
     B.row2uid = ptr<uint32_t>(c, bRow2Uid);
     B.table = ptr<uint32_t>(c, bTable); B.tcount = ptr<uint32_t>(c, bTCount);
     B.table_mask = tcap - 1;
+    TRY(ensure(c, bCallAux, 16));
+    set_call_scratch(B, tcap, ptr<uint32_t>(c, bCallAux));
     B.urow = ptr<uint32_t>(c, bURow); B.ucopies = ptr<uint32_t>(c, bUCopies);
     B.ulen = ptr<uint32_t>(c, bULen); B.urep = ptr<uint32_t>(c, bURep);
     B.bin_hist = ptr<uint32_t>(c, bBinHist); B.bin_cursor = ptr<uint32_t>(c, bBinCursor);
@@ -929,6 +941,15 @@ idb_status idb_diag_gene_bits(idb_context *c, const char *calls, const int64_t *
     B.vgenes = ptr<uint8_t>(c, bVGenes); B.vg_off = ptr<int32_t>(c, bVGOff);
     B.vtab = ptr<GeneEntry>(c, bVTab);
     B.vbits = ptr<uint64_t>(c, bVBits);
+    const uint64_t tcap = next_pow2(std::max<uint64_t>(2ull * n_rows, 1024));
+    TRY(ensure(c, bTable, 4 * tcap));
+    TRY(ensure(c, bSlot, 4 * (size_t)n_rows));
+    TRY(ensure(c, bRepRow, 4 * (size_t)n_rows));
+    TRY(ensure(c, bCallAux, 16));
+    B.table = ptr<uint32_t>(c, bTable);
+    B.slot = ptr<uint32_t>(c, bSlot);
+    B.rep_row = ptr<uint32_t>(c, bRepRow);
+    set_call_scratch(B, tcap, ptr<uint32_t>(c, bCallAux));
     launch_gene_bits(P, B, true, c->stream);
     TRY(check_launch());
     CU(cudaMemcpyAsync(words_out, B.vbits, sizeof(uint64_t) * n_rows * P.VW, cudaMemcpyDeviceToHost,

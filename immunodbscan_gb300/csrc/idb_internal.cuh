@@ -138,6 +138,13 @@ struct Buffers {
     // duplicate table
     uint32_t *table = nullptr, *tcount = nullptr;
     uint64_t table_mask = 0;
+    // call-string collapse of a gene column (scratch, used before the duplicate
+    // table: call_tab aliases table, call_ref slot, call_todo rep_row)
+    unsigned long long *call_tab = nullptr;         // [call_mask+1] (hash hi 32 | row)
+    uint32_t call_mask = 0;
+    uint32_t *call_ref = nullptr;                   // [N] slot of the row's string or kNone
+    uint32_t *call_todo = nullptr;                  // [N] rows that compute their own bitset
+    uint32_t *call_ntodo = nullptr;                 // [1]
     // uniques [N]
     uint32_t *urow = nullptr, *ucopies = nullptr, *ulen = nullptr, *urep = nullptr;
     // bins

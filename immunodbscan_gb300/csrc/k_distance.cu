@@ -252,6 +252,23 @@ __device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, u
     }
 }
 
+// Deferred hits: the Hamming loop only records, per lane, (y index in the staged
+// chunk, hit bits) in a small shared-memory queue; the queue is drained here when
+// a lane's queue is full or the chunk ends, with every lane taking part.
+constexpr int kHitQ = 8;   // queued (y, hits) records per lane
+
+__device__ __noinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, const uint32_t *q,
+                                        uint32_t qn, const uint4 *xm, const uint4 *ym,
+                                        uint32_t xbase, uint32_t ypos0, uint32_t same,
+                                        uint32_t v, uint32_t j, int lane) {
+    const uint32_t kmax = __reduce_max_sync(0xFFFFFFFFu, qn);
+    for (uint32_t k = 0; k < kmax; ++k) {
+        const uint32_t e = k < qn ? q[k * 32 + lane] : 0u;
+        const uint32_t hit = e & 0xFFu, t = e >> 8;
+        emit_hits_meta(a, ew, hit, xm, ym[t], xbase, ypos0 + t, same, v, j, lane);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Hamming, fast path.  BP planes x W words per record; RX x-entries per lane.
 // EM: 0 = popcount test, 1 = eps == 1 (d & (d-1)) == 0, 2 = eps == 0.
@@ -264,6 +281,8 @@ k_hamming(DistArgs a) {
     __shared__ uint4 sy[kWarps][kYB * R16];
     __shared__ uint4 sym[kWarps][kYB];            // y side records
     __shared__ uint4 sxm[kWarps][32 * RX];        // x side records
+    __shared__ uint32_t shq[kWarps][kHitQ * 32];  // deferred hits
+    static_assert(RX <= 8 && kYB < (1 << 24), "hit record layout");
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
     EdgeWriter ew;
@@ -299,12 +318,16 @@ k_hamming(DistArgs a) {
             for (uint32_t t = lane; t < nb * R16; t += 32) sy[wid][t] = __ldg(src + t);
             for (uint32_t t = lane; t < nb; t += 32) sym[wid][t] = __ldg(a.meta + yrow0 + yb + t);
             __syncwarp();
+            uint32_t qn = 0;
             for (uint32_t t = 0; t < nb; ++t) {
                 // x-entries before this y (all of them unless the bin pairs with itself)
                 const uint32_t yp = U.ybase + yb + t;
                 uint32_t nact = U.nx;
                 if (same) nact = yp > U.xbase ? min(U.nx, yp - U.xbase) : 0u;
                 if (nact == 0) continue;
+                // r-blocks in which this lane's x-entry comes before y: 32r + lane < nact
+                const uint32_t nr = nact > (uint32_t)lane ? (nact - lane + 31) >> 5 : 0u;
+                const uint32_t before = nr >= 32 ? 0xFFFFFFFFu : ((1u << nr) - 1u);
                 uint32_t y[NW];
 #pragma unroll
                 for (int q = 0; q < R16; ++q) {
@@ -340,10 +363,20 @@ k_hamming(DistArgs a) {
                         hit |= (uint32_t)h << r;
                     }
                 }
-                hit &= valid;
-                if (__any_sync(0xFFFFFFFFu, hit))
-                    emit_hits_meta(a, ew, hit, sxm[wid], sym[wid][t], U.xbase, yp, same, U.P.v,
-                                   U.P.j, lane);
+                hit &= valid & before;
+                if (hit) shq[wid][qn++ * 32 + lane] = (t << 8) | hit;
+                if (__any_sync(0xFFFFFFFFu, qn == kHitQ)) {
+                    __syncwarp();
+                    drain_hits(a, ew, shq[wid], qn, sxm[wid], sym[wid], U.xbase, U.ybase + yb, same,
+                               U.P.v, U.P.j, lane);
+                    qn = 0;
+                    __syncwarp();
+                }
+            }
+            if (__any_sync(0xFFFFFFFFu, qn)) {
+                __syncwarp();
+                drain_hits(a, ew, shq[wid], qn, sxm[wid], sym[wid], U.xbase, U.ybase + yb, same,
+                           U.P.v, U.P.j, lane);
             }
             __syncwarp();
         }

@@ -79,24 +79,35 @@ __global__ void k_const_strings(uint8_t *blob, int64_t *off, uint32_t N) {
 // ---------------------------------------------------------------------------
 // S1 -- gene bitsets.  Bit g of a row is set iff reference gene name g is a
 // byte-exact substring of the row's call (cuda/BitsetVector.inl:149-175, one
-// launch and one block per row per gene there).
+// launch and one block per row per gene there).  Empty names never match (the
+// reference launches a zero-thread block for them).
 //
-// Here a block takes 128 rows at a time and stages their call bytes in shared
-// memory with coalesced loads.  A byte that starts some gene name is a
-// candidate; candidates are collected into a queue, then each thread takes one
-// candidate and extends a rolling hash over the following bytes (up to the end
-// of the row's call), looking the hash up in the gene table at every length
-// that some name has, and verifying the bytes of every hit.  Each candidate
-// thus costs one pass over at most the longest name instead of one scan per
-// gene.  Empty names never match (the reference launches a zero-thread block
-// for them).  A chunk whose calls exceed the staging buffer, or a table with a
-// name longer than 255 bytes, falls back to one warp per row and one lane per
-// gene.
+// Calls repeat heavily (a repertoire has a few hundred distinct V calls over
+// millions of rows), so a column is collapsed by string first:
+//   k_call_slots  hashes every row's call and inserts (hash, row) into a bounded
+//                 open-addressing table; the first row of every distinct string,
+//                 and any row that finds no slot within kCallProbe probes, is
+//                 queued;
+//   k_gene_bits   computes the bitsets of the queued rows;
+//   k_call_copy   copies each representative's bitset to the rows that share
+//                 its string.
+// A bitset is a function of the string alone, so the result does not depend
+// on which row wins a slot.
+//
+// k_gene_bits: a warp takes up to 32 queued rows, gathers their call bytes into
+// its shared-memory slice, collects the bytes that start some gene name into a
+// candidate queue with ballots, and verifies one candidate per lane: a rolling
+// hash over the following bytes is looked up in the gene table at every length
+// some name has, and every hit is checked byte by byte.  A row longer than the
+// slice, or a table with a name longer than 255 bytes, takes one warp per row
+// and one lane per gene instead.
 // ---------------------------------------------------------------------------
 constexpr int kGbWarps = 8;                 // warps per block
-constexpr int kGbRows = 32;                 // rows per warp chunk
+constexpr int kGbRows = 32;                 // rows per warp window
 constexpr int kGbBytes = 2048;              // staged call bytes per warp
 constexpr int kGbNameBytes = 16384;         // gene names kept in shared memory
+constexpr uint32_t kCallProbe = 64;         // probes before a row computes its own bitset
+constexpr unsigned long long kCallEmpty = ~0ull;
 
 __device__ __forceinline__ bool name_at(const uint8_t *c, uint32_t cl, const uint8_t *name,
                                         uint32_t nl) {
@@ -135,13 +146,98 @@ __device__ void gene_bits_row_naive(const uint8_t *c, uint32_t cl, const uint8_t
         if (lane == w && (uint32_t)w < GW) out[w] = acc[w];
 }
 
-// Each warp takes 32 rows at a time: their call bytes are staged in the warp's
-// shared-memory slice with 4-byte loads, bytes that start a gene name are
-// compacted into a candidate queue with ballots, and the lanes then verify one
-// candidate each (rolling hash, table probe at every name length, byte check
-// against the names in shared memory), setting bits with shared atomics.
+// A warp's shared-memory slice: bitsets, row offsets, candidate queue, bytes.
+struct GbSlice {
+    uint64_t *bits;     // [kGbRows * GW]
+    uint32_t *roff;     // [kGbRows + 1] byte offset of each staged row
+    uint16_t *cand;     // [kGbBytes]
+    uint32_t *words;    // [kGbBytes / 4 + 1]
+    __device__ const uint8_t *bytes() const { return reinterpret_cast<const uint8_t *>(words); }
+};
+
+__host__ __device__ constexpr size_t gb_slice_bytes(uint32_t GW) {
+    return (size_t)kGbBytes + 4 + 2 * kGbBytes + 4 * (kGbRows + 1) + 8 * (size_t)kGbRows * GW + 16;
+}
+
+__device__ GbSlice gb_slice(uint8_t *base, uint32_t GW, int wid) {
+    const size_t slice = (gb_slice_bytes(GW) + 15) / 16 * 16;
+    uint8_t *w = base + slice * wid;
+    GbSlice g;
+    g.bits = reinterpret_cast<uint64_t *>(w);
+    g.roff = reinterpret_cast<uint32_t *>(g.bits + kGbRows * GW);
+    g.cand = reinterpret_cast<uint16_t *>(g.roff + kGbRows + 1);
+    g.words = reinterpret_cast<uint32_t *>(
+        (reinterpret_cast<uintptr_t>(g.cand + kGbBytes) + 3) & ~(uintptr_t)3);
+    return g;
+}
+
+// Stages the longest prefix of rows [r, end) of the window (row k is rows[k], or
+// k itself when rows is null) whose call bytes fit the slice.  Returns the
+// number of rows staged, 0 if row r alone does not fit.  *my_row receives the
+// row of lane l (entry r + l).  With rows == null the rows are contiguous and are
+// copied with aligned 4-byte loads; otherwise row by row.
+__device__ uint32_t gb_stage(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
+                             const uint32_t *__restrict__ rows, uint32_t r, uint32_t end, int lane,
+                             const GbSlice &w, uint32_t *my_row) {
+    const uint32_t k = r + lane;
+    uint32_t row = 0, len = 0;
+    int64_t st = 0;
+    if (k < end) {
+        row = rows ? rows[k] : k;
+        st = off[row];
+        len = (uint32_t)(off[row + 1] - st);
+    }
+    *my_row = row;
+    // shift: alignment slack of the contiguous copy (0 for the gather)
+    const int64_t base = __shfl_sync(0xFFFFFFFFu, st, 0);
+    const uint32_t shift = rows ? 0u : (uint32_t)(reinterpret_cast<uintptr_t>(calls + base) & 3u);
+    uint32_t incl = len;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += t;
+    }
+    const bool fit = k < end && incl + shift + 4 <= (uint32_t)kGbBytes;
+    const uint32_t nr = __popc(__ballot_sync(0xFFFFFFFFu, fit));
+    if (nr == 0) return 0;
+    const uint32_t excl = incl - len;
+    if ((uint32_t)lane < nr) w.roff[lane] = excl + shift;
+    const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, nr - 1);
+    if (lane == 0) w.roff[nr] = total + shift;
+    if (!rows) {
+        // aligned words covering [calls + base, + total); the edge words are read
+        // byte by byte where they reach outside that range
+        const uint32_t *src = reinterpret_cast<const uint32_t *>(
+            reinterpret_cast<uintptr_t>(calls + base) - shift);
+        const uint32_t qend = shift + total, nwords = (qend + 3) >> 2;
+        for (uint32_t t = lane; t < nwords; t += 32) {
+            if (4 * t >= shift && 4 * t + 4 <= qend) {
+                w.words[t] = src[t];
+            } else {
+                uint32_t v = 0;
+                for (uint32_t b = 0; b < 4; ++b) {
+                    const uint32_t q = 4 * t + b;
+                    if (q >= shift && q < qend) v |= (uint32_t)calls[base + (q - shift)] << (8 * b);
+                }
+                w.words[t] = v;
+            }
+        }
+    } else {
+        uint8_t *dst = reinterpret_cast<uint8_t *>(w.words);
+        for (uint32_t j = 0; j < nr; ++j) {
+            const int64_t sj = __shfl_sync(0xFFFFFFFFu, st, j);
+            const uint32_t lj = __shfl_sync(0xFFFFFFFFu, len, j);
+            const uint32_t oj = __shfl_sync(0xFFFFFFFFu, excl, j);
+            for (uint32_t t = lane; t < lj; t += 32) dst[oj + t] = calls[sj + t];
+        }
+    }
+    __syncwarp();
+    return nr;
+}
+
 __global__ void __launch_bounds__(kGbWarps * 32)
-k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, uint32_t N,
+k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
+            const uint32_t *__restrict__ rows, const uint32_t *__restrict__ n_dev, uint32_t n_host,
             const uint8_t *__restrict__ genes, const int32_t *__restrict__ goff, uint32_t G,
             uint32_t GW, const GeneEntry *__restrict__ tab, GeneMatcher gm,
             uint64_t *__restrict__ bits) {
@@ -151,18 +247,11 @@ k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, 
     int32_t *s_goff = reinterpret_cast<int32_t *>(s_tab + gm.ts);
     const uint32_t name_bytes = (uint32_t)goff[G] <= (uint32_t)kGbNameBytes ? (uint32_t)goff[G] : 0u;
     uint8_t *s_names = reinterpret_cast<uint8_t *>(s_goff + G + 1);
-    // per-warp slices (16-byte aligned)
-    uintptr_t wbase = (reinterpret_cast<uintptr_t>(s_names + name_bytes) + 15) & ~(uintptr_t)15;
+    uint8_t *wbase = reinterpret_cast<uint8_t *>(
+        (reinterpret_cast<uintptr_t>(s_names + name_bytes) + 15) & ~(uintptr_t)15);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const size_t slice = (size_t)kGbBytes + 4 + 2 * kGbBytes + 4 * (kGbRows + 1) +
-                         8 * (size_t)kGbRows * GW + 16;
-    uint8_t *wsm = reinterpret_cast<uint8_t *>(wbase + (slice * wid + 15) / 16 * 16);
-    uint64_t *w_bits = reinterpret_cast<uint64_t *>(wsm);                     // [32*GW]
-    uint32_t *w_roff = reinterpret_cast<uint32_t *>(w_bits + kGbRows * GW);   // [33]
-    uint16_t *w_cand = reinterpret_cast<uint16_t *>(w_roff + kGbRows + 1);    // [kGbBytes]
-    uint32_t *w_words = reinterpret_cast<uint32_t *>(
-        (reinterpret_cast<uintptr_t>(w_cand + kGbBytes) + 3) & ~(uintptr_t)3); // [kGbBytes/4+1]
-    const uint8_t *w_bytes0 = reinterpret_cast<const uint8_t *>(w_words);
+    const GbSlice w = gb_slice(wbase, GW, wid);
+    const uint8_t *wb = w.bytes();
     __shared__ uint32_t s_first[8], s_len[8];
     for (uint32_t k = threadIdx.x; k < gm.ts; k += blockDim.x) s_tab[k] = tab[k];
     for (uint32_t k = threadIdx.x; k <= G; k += blockDim.x) s_goff[k] = goff[k];
@@ -175,97 +264,177 @@ k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, 
         }
     __syncthreads();
     const uint8_t *names = name_bytes ? s_names : genes;
-    const uint32_t nchunks = (N + kGbRows - 1) / kGbRows;
+    const uint32_t n = n_dev ? *n_dev : n_host;
+    const uint32_t nchunks = (n + kGbRows - 1) / kGbRows;
     const uint32_t gwarp = blockIdx.x * kGbWarps + wid, nwarps = gridDim.x * kGbWarps;
     for (uint32_t ch = gwarp; ch < nchunks; ch += nwarps) {
-        const uint32_t r0 = ch * kGbRows, nr = min((uint32_t)kGbRows, N - r0);
-        const int64_t base = off[r0];
-        const int64_t total = off[r0 + nr] - base;
-        // 4-byte words covering [calls + base, calls + base + total), aligned on the
-        // absolute address; the first and last word are read byte by byte where they
-        // reach outside that range, so no byte outside the chunk is touched.
-        const uintptr_t a0 = reinterpret_cast<uintptr_t>(calls + base);
-        const uint32_t shift = (uint32_t)(a0 & 3u);
-        if (total + shift + 4 > kGbBytes || gm.long_names) {  // slow path: warp per row
-            for (uint32_t r = 0; r < nr; ++r) {
-                const int64_t c0 = off[r0 + r];
-                gene_bits_row_naive(calls + c0, (uint32_t)(off[r0 + r + 1] - c0), names, s_goff,
-                                    G, GW, lane, bits + (size_t)(r0 + r) * GW);
+        const uint32_t end = min(ch * kGbRows + kGbRows, n);
+        uint32_t r = ch * kGbRows;
+        while (r < end) {
+            uint32_t my_row = 0;
+            const uint32_t nr = gm.long_names ? 0u : gb_stage(calls, off, rows, r, end, lane, w, &my_row);
+            if (nr == 0) {   // one row (or every row: long names) the slow way
+                const uint32_t row = rows ? rows[r] : r;
+                const int64_t c0 = off[row];
+                gene_bits_row_naive(calls + c0, (uint32_t)(off[row + 1] - c0), names, s_goff, G,
+                                    GW, lane, bits + (size_t)row * GW);
+                ++r;
+                continue;
             }
-            continue;
-        }
-        for (uint32_t k = lane; k <= nr; k += 32) w_roff[k] = (uint32_t)(off[r0 + k] - base) + shift;
-        for (uint32_t k = lane; k < nr * GW; k += 32) w_bits[k] = 0;
-        const uint32_t nwords = (uint32_t)((total + shift + 3) >> 2);
-        const uint32_t *src = reinterpret_cast<const uint32_t *>(a0 - shift);
-        const uint32_t qend = shift + (uint32_t)total;
-        for (uint32_t k = lane; k < nwords; k += 32) {
-            if (4 * k >= shift && 4 * k + 4 <= qend) {
-                w_words[k] = src[k];
-            } else {
-                uint32_t v = 0;
-                for (uint32_t b = 0; b < 4; ++b) {
-                    const uint32_t q = 4 * k + b;
-                    if (q >= shift && q < qend) v |= (uint32_t)calls[base + (q - shift)] << (8 * b);
+            for (uint32_t k = lane; k < nr * GW; k += 32) w.bits[k] = 0;
+            // candidates: positions whose byte starts some gene name
+            uint32_t ncand = 0;
+            const uint32_t qbeg = w.roff[0], qend = w.roff[nr];
+            for (uint32_t q0 = qbeg; q0 < qend; q0 += 32) {
+                const uint32_t q = q0 + lane;
+                bool cand = false;
+                if (q < qend) {
+                    const uint32_t c = wb[q];
+                    cand = (s_first[c >> 5] >> (c & 31)) & 1u;
                 }
-                w_words[k] = v;
+                const uint32_t m = __ballot_sync(0xFFFFFFFFu, cand);
+                if (cand) w.cand[ncand + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
+                ncand += __popc(m);
             }
-        }
-        __syncwarp();
-        // candidates: positions whose byte starts some gene name
-        uint32_t ncand = 0;
-        for (uint32_t q0 = shift; q0 < qend; q0 += 32) {
-            const uint32_t q = q0 + lane;
-            bool cand = false;
-            if (q < qend) {
-                const uint32_t c = w_bytes0[q];
-                cand = (s_first[c >> 5] >> (c & 31)) & 1u;
-            }
-            const uint32_t m = __ballot_sync(0xFFFFFFFFu, cand);
-            if (cand) w_cand[ncand + __popc(m & ((1u << lane) - 1u))] = (uint16_t)q;
-            ncand += __popc(m);
-        }
-        __syncwarp();
-        for (uint32_t k = lane; k < ncand; k += 32) {
-            const uint32_t q = w_cand[k];
-            uint32_t lo = 0, hi = nr;   // row: largest r with w_roff[r] <= q
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (w_roff[mid] <= q) lo = mid; else hi = mid;
-            }
-            const uint32_t row = lo, end = w_roff[row + 1];
-            uint32_t h = 0;
-            for (uint32_t t = 0; t < gm.maxlen && q + t < end; ++t) {
-                h = h * kGeneHashMul + w_bytes0[q + t];
-                const uint32_t L = t + 1;
-                if (!((s_len[L >> 5] >> (L & 31)) & 1u)) continue;
-                uint32_t sl = h & (gm.ts - 1);
-                while (s_tab[sl].len != 0) {
-                    const GeneEntry e = s_tab[sl];
-                    if (e.h == h && e.len == L) {
-                        const uint8_t *name = names + s_goff[e.gene];
-                        uint32_t i = 0;
-                        while (i < L && name[i] == w_bytes0[q + i]) ++i;
-                        if (i == L)
-                            atomicOr(reinterpret_cast<unsigned long long *>(&w_bits[row * GW + (e.gene >> 6)]),
-                                     1ull << (e.gene & 63));
+            __syncwarp();
+            for (uint32_t k = lane; k < ncand; k += 32) {
+                const uint32_t q = w.cand[k];
+                uint32_t lo = 0, hi = nr;   // row: largest i with roff[i] <= q
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (w.roff[mid] <= q) lo = mid; else hi = mid;
+                }
+                const uint32_t ri = lo, rend = w.roff[ri + 1];
+                uint32_t h = 0;
+                for (uint32_t t = 0; t < gm.maxlen && q + t < rend; ++t) {
+                    h = h * kGeneHashMul + wb[q + t];
+                    const uint32_t L = t + 1;
+                    if (!((s_len[L >> 5] >> (L & 31)) & 1u)) continue;
+                    uint32_t sl = h & (gm.ts - 1);
+                    while (s_tab[sl].len != 0) {
+                        const GeneEntry e = s_tab[sl];
+                        if (e.h == h && e.len == L) {
+                            const uint8_t *name = names + s_goff[e.gene];
+                            uint32_t i = 0;
+                            while (i < L && name[i] == wb[q + i]) ++i;
+                            if (i == L)
+                                atomicOr(reinterpret_cast<unsigned long long *>(&w.bits[ri * GW + (e.gene >> 6)]),
+                                         1ull << (e.gene & 63));
+                        }
+                        sl = (sl + 1) & (gm.ts - 1);
                     }
-                    sl = (sl + 1) & (gm.ts - 1);
                 }
             }
+            __syncwarp();
+            if (rows) {
+                for (uint32_t k = lane; k < nr * GW; k += 32)
+                    bits[(size_t)rows[r + k / GW] * GW + k % GW] = w.bits[k];
+            } else {
+                for (uint32_t k = lane; k < nr * GW; k += 32) bits[(size_t)r * GW + k] = w.bits[k];
+            }
+            __syncwarp();
+            r += nr;
         }
-        __syncwarp();
-        for (uint32_t k = lane; k < nr * GW; k += 32) bits[(size_t)r0 * GW + k] = w_bits[k];
-        __syncwarp();
     }
 }
 
 size_t gene_bits_smem(uint32_t G, uint32_t GW, uint32_t ts, uint32_t name_bytes) {
-    const size_t slice = (size_t)kGbBytes + 4 + 2 * kGbBytes + 4 * (kGbRows + 1) +
-                         8 * (size_t)kGbRows * GW + 16;
     const size_t nb = name_bytes <= (uint32_t)kGbNameBytes ? name_bytes : 0;
     return sizeof(GeneEntry) * ts + sizeof(int32_t) * (G + 1) + nb + 16 +
-           kGbWarps * ((slice + 15) / 16 * 16);
+           kGbWarps * ((gb_slice_bytes(GW) + 15) / 16 * 16);
+}
+
+// String hash of a staged call (64-bit; equality is then checked byte by byte).
+__device__ __forceinline__ unsigned long long call_hash(const uint8_t *p, uint32_t len) {
+    unsigned long long h = 0x9E3779B97F4A7C15ull ^ len;
+    uint64_t word = 0;
+    for (uint32_t k = 0; k < len; ++k) {
+        word = (word << 8) | p[k];
+        if ((k & 7) == 7) { h = mix64(h, word); word = 0; }
+    }
+    return mix64(h, word);
+}
+
+// Collapse of a call column by string: ref[row] = slot of the row's string, or
+// kNone when the row computes its own bitset (it won the slot, or found none);
+// those rows are appended to todo.
+__global__ void __launch_bounds__(kGbWarps * 32)
+k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, uint32_t N,
+             unsigned long long *tab, uint32_t tmask, uint32_t *__restrict__ ref,
+             uint32_t *__restrict__ todo, uint32_t *n_todo) {
+    extern __shared__ __align__(16) uint8_t sm[];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const GbSlice w = gb_slice(sm, 1, wid);
+    const uint8_t *wb = w.bytes();
+    const uint32_t nchunks = (N + kGbRows - 1) / kGbRows;
+    const uint32_t gwarp = blockIdx.x * kGbWarps + wid, nwarps = gridDim.x * kGbWarps;
+    for (uint32_t ch = gwarp; ch < nchunks; ch += nwarps) {
+        const uint32_t end = min(ch * kGbRows + kGbRows, N);
+        uint32_t r = ch * kGbRows;
+        while (r < end) {
+            uint32_t my_row = 0;
+            const uint32_t nr = gb_stage(calls, off, nullptr, r, end, lane, w, &my_row);
+            bool own = false;
+            uint32_t myref = kNone;
+            if (nr == 0) {                      // too long to stage: computes its own bitset
+                own = lane == 0;
+            } else if ((uint32_t)lane < nr) {
+                const uint32_t q0 = w.roff[lane], len = w.roff[lane + 1] - q0;
+                const unsigned long long h = call_hash(wb + q0, len);
+                const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | my_row;
+                uint32_t sl = (uint32_t)h & tmask;
+                own = true;                     // unless a slot is found below
+                for (uint32_t it = 0; it < kCallProbe; ++it) {
+                    unsigned long long cur = *((volatile unsigned long long *)&tab[sl]);
+                    if (cur == kCallEmpty) {
+                        const unsigned long long prev = atomicCAS(&tab[sl], kCallEmpty, key);
+                        if (prev == kCallEmpty) break;          // representative: own bitset
+                        cur = prev;
+                    }
+                    if ((cur >> 32) == (h >> 32)) {
+                        const uint32_t other = (uint32_t)cur;
+                        const int64_t o0 = off[other];
+                        bool eq = (uint32_t)(off[other + 1] - o0) == len;
+                        if (eq) {
+                            uint32_t diff = 0;      // no early exit: the loads pipeline
+#pragma unroll 4
+                            for (uint32_t b = 0; b < len; ++b) diff |= calls[o0 + b] ^ wb[q0 + b];
+                            eq = diff == 0;
+                        }
+                        if (eq) { own = false; myref = sl; break; }
+                    }
+                    sl = (sl + 1) & tmask;
+                }
+            }
+            if (own) myref = kNone;
+            const uint32_t m = __ballot_sync(0xFFFFFFFFu, own);
+            uint32_t b0 = 0;
+            if (lane == 0 && m) b0 = atomicAdd(n_todo, (uint32_t)__popc(m));
+            b0 = __shfl_sync(0xFFFFFFFFu, b0, 0);
+            if (own) todo[b0 + __popc(m & ((1u << lane) - 1u))] = nr == 0 ? r : my_row;
+            if (nr == 0) {
+                if (lane == 0) ref[r] = kNone;
+                ++r;
+            } else {
+                if ((uint32_t)lane < nr) ref[my_row] = myref;
+                r += nr;
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Rows that share a representative's string take its bitset.
+__global__ void k_call_copy(uint32_t N, const uint32_t *__restrict__ ref,
+                            const unsigned long long *__restrict__ tab, uint32_t GW,
+                            uint64_t *__restrict__ bits) {
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+        const uint32_t s = ref[i];
+        if (s == kNone) continue;
+        const uint32_t src = (uint32_t)tab[s];
+        for (uint32_t k = 0; k < GW; ++k) bits[(size_t)i * GW + k] = bits[(size_t)src * GW + k];
+    }
 }
 
 // No gene column: every row carries bit 0 ("V" against ["V"]).
@@ -573,19 +742,30 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     const GeneEntry *tab = v_column ? B.vtab : B.jtab;
     const GeneMatcher &gm = v_column ? P.vmatch : P.jmatch;
     const uint32_t name_bytes = v_column ? P.gene_bytes_v : P.gene_bytes_j;
+    // 1. collapse the column by string
+    const size_t smem_slots = kGbWarps * ((gb_slice_bytes(1) + 15) / 16 * 16);
+    const int grid_rows = (int)std::min<uint64_t>(((uint64_t)P.N + kGbRows * kGbWarps - 1) /
+                                                      (kGbRows * kGbWarps),
+                                                  (uint64_t)sm_count() * 4);
+    cudaMemsetAsync(B.call_tab, 0xFF, sizeof(unsigned long long) * ((size_t)B.call_mask + 1), s);
+    cudaMemsetAsync(B.call_ntodo, 0, sizeof(uint32_t), s);
+    k_call_slots<<<grid_rows > 0 ? grid_rows : 1, kGbWarps * 32, smem_slots, s>>>(
+        calls, off, P.N, B.call_tab, B.call_mask, B.call_ref, B.call_todo, B.call_ntodo);
+    // 2. bitsets of the representatives
     const size_t smem = gene_bits_smem(G, GW, gm.ts, name_bytes);
     static thread_local size_t attr_set = 0;
     if (smem > 48 * 1024 && smem > attr_set) {
         cudaFuncSetAttribute(k_gene_bits, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         attr_set = smem;
     }
-    const uint32_t nchunks = (P.N + kGbRows - 1) / kGbRows;
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gene_bits, kGbWarps * 32, smem);
-    const uint64_t want = (nchunks + kGbWarps - 1) / kGbWarps;
+    const uint64_t want = ((uint64_t)P.N + kGbRows * kGbWarps - 1) / (kGbRows * kGbWarps);
     const int grid = (int)std::min<uint64_t>(want, (uint64_t)sm_count() * (per_sm > 0 ? per_sm : 1));
-    k_gene_bits<<<grid > 0 ? grid : 1, kGbWarps * 32, smem, s>>>(calls, off, P.N, genes, goff, G, GW,
-                                                                  tab, gm, bits);
+    k_gene_bits<<<grid > 0 ? grid : 1, kGbWarps * 32, smem, s>>>(
+        calls, off, B.call_todo, B.call_ntodo, P.N, genes, goff, G, GW, tab, gm, bits);
+    // 3. everybody else
+    k_call_copy<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.call_ref, B.call_tab, GW, bits);
 }
 
 void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s) {

@@ -179,14 +179,24 @@ __global__ void k_depth(uint32_t N, const uint32_t *__restrict__ row2uid, const 
         if (h[k]) atomicAdd(&hist[k], h[k]);
 }
 
+// Full compression: parent[u] = root of u for every core u.  The walk to the
+// root only reads: with path halving here, a halving step computed from a stale
+// parent could land after another thread's final root write and leave that
+// node pointing at an inner ancestor.  Each thread writes only its own node,
+// and the roots no longer change, so every write is final.
 __global__ void k_compress(const Counters *__restrict__ ctr, const uint32_t *__restrict__ ucore,
                            uint32_t *parent, uint32_t *__restrict__ rootflag) {
     const uint32_t nu = ctr->n_uniques;
     const uint32_t stride = gridDim.x * blockDim.x;
+    volatile uint32_t *vp = parent;
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
         uint32_t r = u;
         if (ucore[u]) {
-            r = uf_find(parent, u);
+            uint32_t pr = vp[r];
+            while (pr != r) {   // parent[y] <= y: strictly decreasing, terminates
+                r = pr;
+                pr = vp[r];
+            }
             parent[u] = r;
         }
         rootflag[u] = ucore[u] && r == u;

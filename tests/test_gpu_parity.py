@@ -232,19 +232,29 @@ def test_gene_bits_known_answers(gpu_ctx):
     assert got.tolist() == S1_WORDS
 
 
-@pytest.mark.parametrize("mode", ["short", "long_calls", "long_names"])
+GENE_BIT_MODES = ["short", "long_calls", "long_names", "huge_calls", "repeated"]
+
+
+@pytest.mark.parametrize("mode", GENE_BIT_MODES)
 def test_gene_bits_vs_oracle(gpu_ctx, mode):
     """Random names (incl. empty, repeated, overlapping and prefix-sharing ones)
-    against random calls.  Long calls overflow a warp's staging buffer for some
-    32-row chunks (those take the per-row path, the rest the staged path); a name
-    longer than 255 bytes sends every row through the per-row path."""
-    rng = np.random.default_rng(5 + ["short", "long_calls", "long_names"].index(mode))
+    against random calls.  Long calls fill a warp's staging slice after fewer than
+    32 rows; a call longer than the slice (huge_calls) or a name longer than 255
+    bytes takes the per-row path; repeated calls share a representative row."""
+    rng = np.random.default_rng(5 + GENE_BIT_MODES.index(mode))
     alpha = list(b"ACGT*-I0123")
     genes = [bytes(rng.choice(alpha, size=int(rng.integers(1, 7))).astype(np.uint8)) for _ in range(150)]
     genes += [b"", genes[3], genes[7] + b"*"] + ([b"A" * 300] if mode == "long_names" else [])
     calls = []
     for i in range(3000):
-        n = int(rng.integers(0, 60 if mode == "short" else (400 if i % 200 < 40 else 30)))
+        if mode == "repeated" and i >= 40:
+            calls.append(calls[int(rng.integers(0, 40))])
+            continue
+        if mode == "huge_calls":
+            n = int(rng.integers(2040, 3000)) if i % 100 == 3 else int(rng.integers(0, 60))
+        else:
+            n = int(rng.integers(0, 60 if mode in ("short", "repeated") else
+                                 (400 if i % 200 < 40 else 30)))
         s = bytearray(rng.choice(alpha, size=n).astype(np.uint8).tobytes())
         if rng.random() < 0.5 and n > 10:
             g = genes[int(rng.integers(0, len(genes)))]
@@ -254,6 +264,21 @@ def test_gene_bits_vs_oracle(gpu_ctx, mode):
     got = _as_words32(_gpu_bits(gpu_ctx, calls, genes), len(genes))
     want = oracle.gene_bitsets(calls, genes)
     assert np.array_equal(got, want)
+
+
+def test_gene_bits_call_table_overflow(gpu_ctx):
+    """More distinct calls than the call-string table holds (2^20 slots): rows
+    that find no slot compute their own bitsets."""
+    rng = np.random.default_rng(9)
+    n = 1_200_000
+    genes = [b"IGHV%d" % k for k in range(1, 70)] + [b"-1", b"*0"]
+    # distinct calls: a gene name plus a unique decimal suffix; some repeated
+    idx = rng.integers(0, 69, size=n)
+    calls = [b"IGHV%d-%d*0%d" % (idx[i] + 1, i, i % 7) for i in range(n)]
+    for i in range(0, n, 1000):
+        calls[i] = calls[i // 2]
+    got = _as_words32(_gpu_bits(gpu_ctx, calls, genes), len(genes))
+    assert np.array_equal(got, oracle.gene_bitsets(calls, genes))
 
 
 def test_gene_bits_synthetic(gpu_ctx):
