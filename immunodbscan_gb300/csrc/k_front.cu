@@ -159,6 +159,21 @@ __host__ __device__ constexpr size_t gb_slice_bytes(uint32_t GW) {
     return (size_t)kGbBytes + 4 + 2 * kGbBytes + 4 * (kGbRows + 1) + 8 * (size_t)kGbRows * GW + 16;
 }
 
+// The call-collapse kernel stages bytes only: row offsets and words.
+__host__ __device__ constexpr size_t cs_slice_bytes() {
+    return 4 * (kGbRows + 1) + (size_t)kGbBytes + 4 + 16;
+}
+
+__device__ GbSlice cs_slice(uint8_t *base, int wid) {
+    uint8_t *w = base + (cs_slice_bytes() + 15) / 16 * 16 * wid;
+    GbSlice g;
+    g.bits = nullptr;
+    g.cand = nullptr;
+    g.roff = reinterpret_cast<uint32_t *>(w);
+    g.words = g.roff + kGbRows + 1;
+    return g;
+}
+
 __device__ GbSlice gb_slice(uint8_t *base, uint32_t GW, int wid) {
     const size_t slice = (gb_slice_bytes(GW) + 15) / 16 * 16;
     uint8_t *w = base + slice * wid;
@@ -364,7 +379,7 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
              uint32_t *__restrict__ todo, uint32_t *n_todo) {
     extern __shared__ __align__(16) uint8_t sm[];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const GbSlice w = gb_slice(sm, 1, wid);
+    const GbSlice w = cs_slice(sm, wid);
     const uint8_t *wb = w.bytes();
     const uint32_t nchunks = (N + kGbRows - 1) / kGbRows;
     const uint32_t gwarp = blockIdx.x * kGbWarps + wid, nwarps = gridDim.x * kGbWarps;
@@ -426,13 +441,14 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
 
 // Rows that share a representative's string take its bitset.
 __global__ void k_call_copy(uint32_t N, const uint32_t *__restrict__ ref,
-                            const unsigned long long *__restrict__ tab, uint32_t GW,
+                            const unsigned long long *__restrict__ tab, uint32_t tmask, uint32_t GW,
                             uint64_t *__restrict__ bits) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
         const uint32_t s = ref[i];
-        if (s == kNone) continue;
+        if (s > tmask) continue;                 // kNone: the row has its own bitset
         const uint32_t src = (uint32_t)tab[s];
+        if (src >= N) continue;
         for (uint32_t k = 0; k < GW; ++k) bits[(size_t)i * GW + k] = bits[(size_t)src * GW + k];
     }
 }
@@ -743,7 +759,8 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     const GeneMatcher &gm = v_column ? P.vmatch : P.jmatch;
     const uint32_t name_bytes = v_column ? P.gene_bytes_v : P.gene_bytes_j;
     // 1. collapse the column by string
-    const size_t smem_slots = kGbWarps * ((gb_slice_bytes(1) + 15) / 16 * 16);
+    const size_t smem_slots = kGbWarps * ((cs_slice_bytes() + 15) / 16 * 16);
+    static_assert(kGbWarps * ((cs_slice_bytes() + 15) / 16 * 16) <= 48 * 1024, "default smem limit");
     const int grid_rows = (int)std::min<uint64_t>(((uint64_t)P.N + kGbRows * kGbWarps - 1) /
                                                       (kGbRows * kGbWarps),
                                                   (uint64_t)sm_count() * 4);
@@ -765,7 +782,8 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     k_gene_bits<<<grid > 0 ? grid : 1, kGbWarps * 32, smem, s>>>(
         calls, off, B.call_todo, B.call_ntodo, P.N, genes, goff, G, GW, tab, gm, bits);
     // 3. everybody else
-    k_call_copy<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.call_ref, B.call_tab, GW, bits);
+    k_call_copy<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.call_ref, B.call_tab, B.call_mask, GW,
+                                                    bits);
 }
 
 void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s) {
