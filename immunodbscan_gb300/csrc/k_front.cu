@@ -359,6 +359,29 @@ size_t gene_bits_smem(uint32_t G, uint32_t GW, uint32_t ts, uint32_t name_bytes)
            kGbWarps * ((gb_slice_bytes(GW) + 15) / 16 * 16);
 }
 
+// Byte equality of a call in global memory with a staged one.  Reads the aligned
+// 4-byte words that hold the call's bytes (each holds at least one of them, so
+// no read leaves the call's pages), independent loads without an early exit.
+__device__ __forceinline__ bool bytes_equal_global(const uint8_t *g, const uint8_t *sb,
+                                                   uint32_t len) {
+    if (len == 0) return true;
+    const uintptr_t a = reinterpret_cast<uintptr_t>(g);
+    const uint32_t sh = (uint32_t)(a & 3u);
+    const uint32_t *gw = reinterpret_cast<const uint32_t *>(a - sh);
+    const uint32_t nwords = (sh + len + 3) >> 2;
+    uint32_t diff = 0;
+#pragma unroll 4
+    for (uint32_t t = 0; t < nwords; ++t) {
+        const uint32_t x = __ldg(gw + t);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const int p = (int)(4 * t + k) - (int)sh;
+            if (p >= 0 && p < (int)len) diff |= ((x >> (8 * k)) & 0xFFu) ^ sb[p];
+        }
+    }
+    return diff == 0;
+}
+
 // String hash of a staged call (64-bit; equality is then checked byte by byte).
 __device__ __forceinline__ unsigned long long call_hash(const uint8_t *p, uint32_t len) {
     unsigned long long h = 0x9E3779B97F4A7C15ull ^ len;
@@ -393,33 +416,58 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
             uint32_t myref = kNone;
             if (nr == 0) {                      // too long to stage: computes its own bitset
                 own = lane == 0;
-            } else if ((uint32_t)lane < nr) {
-                const uint32_t q0 = w.roff[lane], len = w.roff[lane + 1] - q0;
-                const unsigned long long h = call_hash(wb + q0, len);
-                const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | my_row;
-                uint32_t sl = (uint32_t)h & tmask;
-                own = true;                     // unless a slot is found below
-                for (uint32_t it = 0; it < kCallProbe; ++it) {
-                    unsigned long long cur = *((volatile unsigned long long *)&tab[sl]);
-                    if (cur == kCallEmpty) {
-                        const unsigned long long prev = atomicCAS(&tab[sl], kCallEmpty, key);
-                        if (prev == kCallEmpty) break;          // representative: own bitset
-                        cur = prev;
-                    }
-                    if ((cur >> 32) == (h >> 32)) {
-                        const uint32_t other = (uint32_t)cur;
-                        const int64_t o0 = off[other];
-                        bool eq = (uint32_t)(off[other + 1] - o0) == len;
-                        if (eq) {
-                            uint32_t diff = 0;      // no early exit: the loads pipeline
-#pragma unroll 4
-                            for (uint32_t b = 0; b < len; ++b) diff |= calls[o0 + b] ^ wb[q0 + b];
-                            eq = diff == 0;
-                        }
-                        if (eq) { own = false; myref = sl; break; }
-                    }
-                    sl = (sl + 1) & tmask;
+            } else {
+                const bool act = (uint32_t)lane < nr;
+                uint32_t q0 = 0, len = 0;
+                unsigned long long h = 0;
+                if (act) {
+                    q0 = w.roff[lane];
+                    len = w.roff[lane + 1] - q0;
+                    h = call_hash(wb + q0, len);
                 }
+                // equal calls inside the window: the lowest lane of each hash group
+                // looks the string up, the others check their bytes against it
+                const uint32_t grp = __match_any_sync(0xFFFFFFFFu, act ? h : kCallEmpty);
+                const int leader = __ffs(grp) - 1;
+                const uint32_t lq0 = __shfl_sync(0xFFFFFFFFu, q0, leader);
+                const uint32_t llen = __shfl_sync(0xFFFFFFFFu, len, leader);
+                bool follow = false;
+                if (act && leader != lane && llen == len) {
+                    uint32_t diff = 0;
+                    for (uint32_t b = 0; b < len; ++b) diff |= wb[q0 + b] ^ wb[lq0 + b];
+                    follow = diff == 0;
+                }
+                uint32_t slot = kNone;          // the string's slot, kNone if none was found
+                if (act && !follow) {
+                    const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | my_row;
+                    uint32_t sl = (uint32_t)h & tmask;
+                    own = true;                 // unless an equal string is found below
+                    for (uint32_t it = 0; it < kCallProbe; ++it) {
+                        unsigned long long cur = *((volatile unsigned long long *)&tab[sl]);
+                        if (cur == kCallEmpty) {
+                            const unsigned long long prev = atomicCAS(&tab[sl], kCallEmpty, key);
+                            if (prev == kCallEmpty) { slot = sl; break; }   // representative
+                            cur = prev;
+                        }
+                        if ((cur >> 32) == (h >> 32)) {
+                            const uint32_t other = (uint32_t)cur;
+                            const int64_t o0 = off[other];
+                            if ((uint32_t)(off[other + 1] - o0) == len &&
+                                bytes_equal_global(calls + o0, wb + q0, len)) {
+                                own = false;
+                                slot = sl;
+                                break;
+                            }
+                        }
+                        sl = (sl + 1) & tmask;
+                    }
+                }
+                const uint32_t lslot = __shfl_sync(0xFFFFFFFFu, slot, leader);
+                if (follow) {
+                    own = lslot == kNone;       // the leader found no slot: own bitset too
+                    slot = lslot;
+                }
+                myref = slot;
             }
             if (own) myref = kNone;
             const uint32_t m = __ballot_sync(0xFFFFFFFFu, own);
@@ -763,7 +811,7 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     static_assert(kGbWarps * ((cs_slice_bytes() + 15) / 16 * 16) <= 48 * 1024, "default smem limit");
     const int grid_rows = (int)std::min<uint64_t>(((uint64_t)P.N + kGbRows * kGbWarps - 1) /
                                                       (kGbRows * kGbWarps),
-                                                  (uint64_t)sm_count() * 4);
+                                                  (uint64_t)sm_count() * 8);
     cudaMemsetAsync(B.call_tab, 0xFF, sizeof(unsigned long long) * ((size_t)B.call_mask + 1), s);
     cudaMemsetAsync(B.call_ntodo, 0, sizeof(uint32_t), s);
     k_call_slots<<<grid_rows > 0 ? grid_rows : 1, kGbWarps * 32, smem_slots, s>>>(
