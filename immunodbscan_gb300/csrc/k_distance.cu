@@ -256,8 +256,9 @@ __device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, u
 // chunk, hit bits) in a small shared-memory queue; the queue is drained here when
 // a lane's queue is full or the chunk ends, with every lane taking part.
 constexpr int kHitQ = 8;   // queued (y, hits) records per lane
+constexpr uint32_t kOff = 0x40000000u;   // score of a masked x-entry (never a hit)
 
-__device__ __noinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, const uint32_t *q,
+__device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, const uint32_t *q,
                                         uint32_t qn, const uint4 *xm, const uint4 *ym,
                                         uint32_t xbase, uint32_t ypos0, uint32_t same,
                                         uint32_t v, uint32_t j, int lane) {
@@ -274,7 +275,7 @@ __device__ __noinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, const
 // EM: 0 = popcount test, 1 = eps == 1 (d & (d-1)) == 0, 2 = eps == 0.
 // ---------------------------------------------------------------------------
 template <int BP, int W, int RX, int EM>
-__global__ void __launch_bounds__(kWarps * 32, (W == 1 ? 5 : 4))
+__global__ void __launch_bounds__(kWarps * 32, 4)
 k_hamming(DistArgs a) {
     constexpr int NW = BP * W;                 // words per record used
     constexpr int R16 = (NW + 3) / 4;          // 16-byte words per record
@@ -291,12 +292,14 @@ k_hamming(DistArgs a) {
     Unit U;
     while (next_unit(a, n_units, n_bp, lane, U)) {
         uint32_t x[RX][NW];
+        uint32_t vmask[RX];          // kOff for x-entries outside the unit
         uint32_t valid = 0;
 #pragma unroll
         for (int r = 0; r < RX; ++r) {
             const uint32_t xi = (uint32_t)r * 32 + lane;
             const bool ok = xi < U.nx;
             valid |= (uint32_t)ok << r;
+            vmask[r] = ok ? 0u : kOff;
             const uint4 *src = a.rec + (size_t)(U.P.a_start + U.xbase + (ok ? xi : 0)) * R16;
 #pragma unroll
             for (int q = 0; q < R16; ++q) {
@@ -309,10 +312,13 @@ k_hamming(DistArgs a) {
             if (ok) pairs += unit_pairs(U, U.xbase + xi);
             sxm[wid][xi] = __ldg(a.meta + U.P.a_start + U.xbase + (ok ? xi : 0));
         }
-        const int eps = U.P.eps;
+        // a pair is a hit iff its score <= thr (score: d&(d-1) for eps 1, d for
+        // eps 0, the popcount otherwise); masked entries score >= kOff
+        const uint32_t thr = EM == 0 ? (uint32_t)max(U.P.eps, 0) : 0u;
+        const bool neg = EM == 0 && U.P.eps < 0;       // no pair can be a neighbour
         const uint32_t same = U.P.same;
         const uint32_t yrow0 = (same ? U.P.a_start : U.P.b_start) + U.ybase;
-        for (uint32_t yb = 0; yb < U.ny; yb += kYB) {
+        for (uint32_t yb = 0; yb < U.ny && !neg; yb += kYB) {
             const uint32_t nb = min((uint32_t)kYB, U.ny - yb);
             const uint4 *src = a.rec + (size_t)(yrow0 + yb) * R16;
             for (uint32_t t = lane; t < nb * R16; t += 32) sy[wid][t] = __ldg(src + t);
@@ -320,14 +326,9 @@ k_hamming(DistArgs a) {
             __syncwarp();
             uint32_t qn = 0;
             for (uint32_t t = 0; t < nb; ++t) {
-                // x-entries before this y (all of them unless the bin pairs with itself)
                 const uint32_t yp = U.ybase + yb + t;
-                uint32_t nact = U.nx;
-                if (same) nact = yp > U.xbase ? min(U.nx, yp - U.xbase) : 0u;
-                if (nact == 0) continue;
-                // r-blocks in which this lane's x-entry comes before y: 32r + lane < nact
-                const uint32_t nr = nact > (uint32_t)lane ? (nact - lane + 31) >> 5 : 0u;
-                const uint32_t before = nr >= 32 ? 0xFFFFFFFFu : ((1u << nr) - 1u);
+                // same bin: only x-entries before y count; none before -> skip y
+                if (same && yp <= U.xbase) continue;
                 uint32_t y[NW];
 #pragma unroll
                 for (int q = 0; q < R16; ++q) {
@@ -337,34 +338,43 @@ k_hamming(DistArgs a) {
                     for (int e = 0; e < 4; ++e)
                         if (4 * q + e < NW) y[4 * q + e] = w4[e];
                 }
-                uint32_t hit = 0;
+                // all RX chains without branches (independent, interleaved)
+                uint32_t sc[RX];
 #pragma unroll
                 for (int r = 0; r < RX; ++r) {
-                    if ((uint32_t)r * 32 < nact) {   // warp-uniform
-                        bool h;
-                        if (W == 1) {
-                            uint32_t d = x[r][0] ^ y[0];
+                    if (W == 1) {
+                        uint32_t d = x[r][0] ^ y[0];
 #pragma unroll
-                            for (int p = 1; p < BP; ++p) d |= x[r][p] ^ y[p];
-                            if (EM == 2) h = d == 0;
-                            else if (EM == 1) h = (d & (d - 1)) == 0;
-                            else h = __popc(d) <= eps;
-                        } else {
-                            int dist = 0;
+                        for (int p = 1; p < BP; ++p) d |= x[r][p] ^ y[p];
+                        sc[r] = (EM == 2 ? d : (EM == 1 ? (d & (d - 1u)) : (uint32_t)__popc(d))) | vmask[r];
+                    } else {
+                        uint32_t dist = 0;
 #pragma unroll
-                            for (int w = 0; w < W; ++w) {
-                                uint32_t d = x[r][w] ^ y[w];
+                        for (int w = 0; w < W; ++w) {
+                            uint32_t d = x[r][w] ^ y[w];
 #pragma unroll
-                                for (int p = 1; p < BP; ++p) d |= x[r][p * W + w] ^ y[p * W + w];
-                                dist += __popc(d);
-                            }
-                            h = dist <= eps;
+                            for (int p = 1; p < BP; ++p) d |= x[r][p * W + w] ^ y[p * W + w];
+                            dist += __popc(d);
                         }
-                        hit |= (uint32_t)h << r;
+                        sc[r] = dist | vmask[r];
                     }
                 }
-                hit &= valid & before;
-                if (hit) shq[wid][qn++ * 32 + lane] = (t << 8) | hit;
+                // y inside the unit's own x range (same bin): mask x-entries not before y
+                if (same && yp < U.xbase + U.nx) {
+                    const uint32_t nact = yp - U.xbase;
+#pragma unroll
+                    for (int r = 0; r < RX; ++r)
+                        if ((uint32_t)r * 32 + lane >= nact) sc[r] |= kOff;
+                }
+                uint32_t z = sc[0];
+#pragma unroll
+                for (int r = 1; r < RX; ++r) z = min(z, sc[r]);
+                if (z <= thr) {
+                    uint32_t hit = 0;
+#pragma unroll
+                    for (int r = 0; r < RX; ++r) hit |= (uint32_t)(sc[r] <= thr) << r;
+                    shq[wid][qn++ * 32 + lane] = (t << 8) | (hit & valid);
+                }
                 if (__any_sync(0xFFFFFFFFu, qn == kHitQ)) {
                     __syncwarp();
                     drain_hits(a, ew, shq[wid], qn, sxm[wid], sym[wid], U.xbase, U.ybase + yb, same,

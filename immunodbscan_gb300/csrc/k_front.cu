@@ -359,38 +359,57 @@ size_t gene_bits_smem(uint32_t G, uint32_t GW, uint32_t ts, uint32_t name_bytes)
            kGbWarps * ((gb_slice_bytes(GW) + 15) / 16 * 16);
 }
 
-// Byte equality of a call in global memory with a staged one.  Reads the aligned
-// 4-byte words that hold the call's bytes (each holds at least one of them, so
-// no read leaves the call's pages), independent loads without an early exit.
-__device__ __forceinline__ bool bytes_equal_global(const uint8_t *g, const uint8_t *sb,
-                                                   uint32_t len) {
+// Four staged bytes from byte offset q of a warp's slice (q + 8 <= slice size).
+__device__ __forceinline__ uint32_t staged_word(const uint32_t *words, uint32_t q) {
+    return __funnelshift_r(words[q >> 2], words[(q >> 2) + 1], 8 * (q & 3));
+}
+
+// Mask of the first n (0..4) bytes of a word.
+__device__ __forceinline__ uint32_t byte_mask(uint32_t n) {
+    return n >= 4 ? 0xFFFFFFFFu : ((1u << (8 * n)) - 1u);
+}
+
+// Byte equality of a call in global memory with the staged bytes at offset q0.
+// Reads the aligned 4-byte words that hold the call's bytes (each holds at least
+// one of them, so no read leaves the call's pages); independent loads, no early
+// exit.
+__device__ __forceinline__ bool bytes_equal_global(const uint8_t *g, const uint32_t *words,
+                                                   uint32_t q0, uint32_t len) {
     if (len == 0) return true;
     const uintptr_t a = reinterpret_cast<uintptr_t>(g);
     const uint32_t sh = (uint32_t)(a & 3u);
     const uint32_t *gw = reinterpret_cast<const uint32_t *>(a - sh);
     const uint32_t nwords = (sh + len + 3) >> 2;
-    uint32_t diff = 0;
+    // word 0 holds bytes [0, 4 - sh) of the call in its upper bytes
+    uint32_t diff = (__ldg(gw) >> (8 * sh)) ^ staged_word(words, q0);
+    diff &= byte_mask(min(4u - sh, len));
 #pragma unroll 4
-    for (uint32_t t = 0; t < nwords; ++t) {
-        const uint32_t x = __ldg(gw + t);
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const int p = (int)(4 * t + k) - (int)sh;
-            if (p >= 0 && p < (int)len) diff |= ((x >> (8 * k)) & 0xFFu) ^ sb[p];
-        }
+    for (uint32_t t = 1; t < nwords; ++t) {
+        const uint32_t k = 4 * t - sh;                 // call byte at the word's start
+        diff |= (__ldg(gw + t) ^ staged_word(words, q0 + k)) & byte_mask(len - k);
     }
     return diff == 0;
 }
 
+// Equality of two staged calls of equal length.
+__device__ __forceinline__ bool staged_equal(const uint32_t *words, uint32_t qa, uint32_t qb,
+                                             uint32_t len) {
+    uint32_t diff = 0;
+    for (uint32_t k = 0; k < len; k += 4)
+        diff |= (staged_word(words, qa + k) ^ staged_word(words, qb + k)) & byte_mask(len - k);
+    return diff == 0;
+}
+
 // String hash of a staged call (64-bit; equality is then checked byte by byte).
-__device__ __forceinline__ unsigned long long call_hash(const uint8_t *p, uint32_t len) {
+__device__ __forceinline__ unsigned long long call_hash(const uint32_t *words, uint32_t q0,
+                                                        uint32_t len) {
     unsigned long long h = 0x9E3779B97F4A7C15ull ^ len;
-    uint64_t word = 0;
-    for (uint32_t k = 0; k < len; ++k) {
-        word = (word << 8) | p[k];
-        if ((k & 7) == 7) { h = mix64(h, word); word = 0; }
+    for (uint32_t k = 0; k < len; k += 8) {
+        const uint32_t lo = staged_word(words, q0 + k) & byte_mask(len - k);
+        const uint32_t hi = k + 4 < len ? staged_word(words, q0 + k + 4) & byte_mask(len - k - 4) : 0u;
+        h = mix64(h, ((unsigned long long)hi << 32) | lo);
     }
-    return mix64(h, word);
+    return h;
 }
 
 // Collapse of a call column by string: ref[row] = slot of the row's string, or
@@ -423,7 +442,7 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
                 if (act) {
                     q0 = w.roff[lane];
                     len = w.roff[lane + 1] - q0;
-                    h = call_hash(wb + q0, len);
+                    h = call_hash(w.words, q0, len);
                 }
                 // equal calls inside the window: the lowest lane of each hash group
                 // looks the string up, the others check their bytes against it
@@ -432,11 +451,7 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
                 const uint32_t lq0 = __shfl_sync(0xFFFFFFFFu, q0, leader);
                 const uint32_t llen = __shfl_sync(0xFFFFFFFFu, len, leader);
                 bool follow = false;
-                if (act && leader != lane && llen == len) {
-                    uint32_t diff = 0;
-                    for (uint32_t b = 0; b < len; ++b) diff |= wb[q0 + b] ^ wb[lq0 + b];
-                    follow = diff == 0;
-                }
+                if (act && leader != lane && llen == len) follow = staged_equal(w.words, q0, lq0, len);
                 uint32_t slot = kNone;          // the string's slot, kNone if none was found
                 if (act && !follow) {
                     const unsigned long long key = (h & 0xFFFFFFFF00000000ull) | my_row;
@@ -453,7 +468,7 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
                             const uint32_t other = (uint32_t)cur;
                             const int64_t o0 = off[other];
                             if ((uint32_t)(off[other + 1] - o0) == len &&
-                                bytes_equal_global(calls + o0, wb + q0, len)) {
+                                bytes_equal_global(calls + o0, w.words, q0, len)) {
                                 own = false;
                                 slot = sl;
                                 break;
@@ -524,19 +539,21 @@ struct DedupArgs {
     Counters *ctr;
 };
 
-__device__ bool rows_equal(const DedupArgs &a, uint32_t x, uint32_t y, uint32_t rx) {
-    const int64_t ox = a.off[x], oy = a.off[y];
-    const uint32_t lx = (uint32_t)(a.off[x + 1] - ox);
-    if ((uint32_t)(a.off[y + 1] - oy) != lx) return false;
-    if (rep_of_row(a.rep_off, a.R, y) != rx) return false;
-    for (uint32_t w = 0; w < a.VW; ++w)
-        if (a.vbits[(size_t)x * a.VW + w] != a.vbits[(size_t)y * a.VW + w]) return false;
-    for (uint32_t w = 0; w < a.JW; ++w)
-        if (a.jbits[(size_t)x * a.JW + w] != a.jbits[(size_t)y * a.JW + w]) return false;
+// Row x (repertoire rx, bytes [ox, ox+lx)) equals row y: same repertoire,
+// length, V and J bitsets and bytes.  Independent loads, no early exit.
+__device__ bool rows_equal(const DedupArgs &a, uint32_t x, uint32_t y, uint32_t rx, int64_t ox,
+                           uint32_t lx) {
+    const int64_t oy = a.off[y], oy1 = a.off[y + 1];
+    const uint32_t r0 = a.rep_off[rx], r1 = a.rep_off[rx + 1];
+    if ((uint32_t)(oy1 - oy) != lx || y < r0 || y >= r1) return false;
+    uint64_t d = 0;
+    for (uint32_t w = 0; w < a.VW; ++w) d |= a.vbits[(size_t)x * a.VW + w] ^ a.vbits[(size_t)y * a.VW + w];
+    for (uint32_t w = 0; w < a.JW; ++w) d |= a.jbits[(size_t)x * a.JW + w] ^ a.jbits[(size_t)y * a.JW + w];
     const uint8_t *px = a.seq + ox, *py = a.seq + oy;
-    for (uint32_t k = 0; k < lx; ++k)
-        if (px[k] != py[k]) return false;
-    return true;
+    uint32_t db = 0;
+#pragma unroll 8
+    for (uint32_t k = 0; k < lx; ++k) db |= px[k] ^ py[k];
+    return d == 0 && db == 0;
 }
 
 __global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
@@ -569,14 +586,17 @@ __global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
                 if (prev == kNone) break;
                 cur = prev;
             }
-            if (rows_equal(a, i, cur, r)) {
-                atomicMin(&a.table[s], i);
-                break;
-            }
+            if (rows_equal(a, i, cur, r, o, L)) break;
             s = (s + 1) & a.mask;
         }
         a.slot[i] = (uint32_t)s;
-        if (s != kNone) atomicAdd(&a.tcount[s], 1u);
+        // one class-size increment and one minimum per class among the warp's
+        // rows (lanes hold ascending rows, so the lowest lane has the smallest)
+        const uint32_t grp = __match_any_sync(__activemask(), (uint32_t)s);
+        if ((threadIdx.x & 31) == (uint32_t)(__ffs(grp) - 1) && s != kNone) {
+            atomicAdd(&a.tcount[s], (uint32_t)__popc(grp));
+            atomicMin(&a.table[s], i);
+        }
     }
 }
 
