@@ -152,79 +152,38 @@ __global__ void k_bin_hist(BinGeom g, const Counters *__restrict__ ctr,
 //  codes (Levenshtein and generic path): one code byte per residue.
 // Codes are a bijection of the byte values present, so equality of codes is
 // equality of bytes.
-// Iterator over the (V gene, J gene) pairs of one unique, V major, J minor.
-struct GenePairIt {
-    const uint64_t *vb_ptr, *jb_ptr;
-    uint32_t VW, JW, vw, jw, jw0;
-    uint64_t vb, jb, jb0;
-    bool has;
-
-    __device__ static bool next_word(const uint64_t *p, uint32_t W, uint32_t &w, uint64_t &b) {
-        while (b == 0 && ++w < W) b = p[w];
-        return b != 0;
-    }
-    __device__ void init(const uint64_t *vp, uint32_t vW, const uint64_t *jp, uint32_t jW, bool act) {
-        vb_ptr = vp; jb_ptr = jp; VW = vW; JW = jW;
-        vw = 0; jw0 = 0; vb = 0; jb0 = 0;
-        has = false;
-        if (!act) return;
-        vb = vp[0];
-        jb0 = jp[0];
-        has = next_word(vp, VW, vw, vb) && next_word(jp, JW, jw0, jb0);
-        jw = jw0;
-        jb = jb0;
-    }
-    __device__ uint32_t v() const { return vw * 64 + lowest_bit64(vb); }
-    __device__ uint32_t j() const { return jw * 64 + lowest_bit64(jb); }
-    __device__ void advance() {
-        jb &= jb - 1;
-        if (next_word(jb_ptr, JW, jw, jb)) return;
-        vb &= vb - 1;
-        if (!next_word(vb_ptr, VW, vw, vb)) { has = false; return; }
-        jw = jw0;
-        jb = jb0;
-    }
-};
-
-// Entries: every unique goes to each of its |V|*|J| bins.  The record depends
-// on the unique only and is built once (registers when it is at most 128
-// bytes, the fast paths).  The warp walks its uniques' (V, J) pairs in lock
-// step; lanes that land in the same bin in the same step share one cursor
-// increment and one signature AND (match + reduce), so a large bin costs one
-// atomic per warp step instead of one per entry.
+// RSC: record size in 16-byte words when it is a compile-time 1..8 (the fast
+// paths: the record is built once, in RSC uint4 registers), 0 for the long
+// records of the generic path (code bytes packed per entry).
+template <int RSC>
 __global__ void __launch_bounds__(256)
 k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
-           const uint32_t *__restrict__ urow, const uint32_t *__restrict__ ulen,
-           const uint32_t *__restrict__ urep, const uint32_t *__restrict__ uclass,
-           unsigned long long *__restrict__ sig_and,
-           const uint64_t *__restrict__ vbits,
-           const uint64_t *__restrict__ jbits, const uint8_t *__restrict__ seq,
-           const int64_t *__restrict__ seq_off, const uint8_t *__restrict__ codemap,
-           const uint32_t *__restrict__ bin_start, uint32_t *__restrict__ cursor,
-           uint32_t *__restrict__ ent_uid, uint4 *__restrict__ ent_rec,
-           uint4 *__restrict__ ent_meta,
-           uint32_t rs16, int planes, uint32_t W, uint64_t cap_entries,
-           uint32_t *err) {
+                           const uint32_t *__restrict__ urow, const uint32_t *__restrict__ ulen,
+                           const uint32_t *__restrict__ urep, const uint32_t *__restrict__ uclass,
+                           unsigned long long *__restrict__ sig_and,
+                           const uint64_t *__restrict__ vbits,
+                           const uint64_t *__restrict__ jbits, const uint8_t *__restrict__ seq,
+                           const int64_t *__restrict__ seq_off, const uint8_t *__restrict__ codemap,
+                           const uint32_t *__restrict__ bin_start, uint32_t *__restrict__ cursor,
+                           uint32_t *__restrict__ ent_uid, uint4 *__restrict__ ent_rec,
+                           uint4 *__restrict__ ent_meta,
+                           uint32_t rs16, int planes, uint32_t W, uint64_t cap_entries,
+                           uint32_t *err) {
     __shared__ uint8_t cm[256];
     for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
     __syncthreads();
     const uint32_t nu = ctr->n_uniques;
-    const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const bool small = rs16 <= 8;
-    for (uint32_t ub = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); ub < nu; ub += stride) {
-        const uint32_t u = ub + lane;
-        uint32_t row = 0, L = 0, r = 0, cls = 0;
-        bool act = u < nu;
-        if (act) {
-            row = urow[u]; L = ulen[u]; r = urep[u]; cls = uclass[u];
-            act = g.in_range(L);
-        }
-        const uint8_t *s = seq + (act ? seq_off[row] : 0);
-        uint4 rec[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) rec[q] = make_uint4(0, 0, 0, 0);
-        if (act && small) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t row = urow[u], L = ulen[u], r = urep[u];
+        if (!g.in_range(L)) continue;
+        const uint8_t *s = seq + seq_off[row];
+        // the record depends on the unique only: build it once (registers when it
+        // is at most 128 bytes, the fast paths), store it in every bin
+        constexpr int NR = RSC > 0 ? RSC : 1;
+        uint4 rec[NR];
+        constexpr bool small = RSC > 0;
+        if (small) {
             if (planes > 0) {
                 uint32_t wd[5][4];
 #pragma unroll
@@ -241,9 +200,9 @@ k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                     }
                 }
                 // layout: word p*W + w
-                uint32_t flat[32];
+                uint32_t flat[4 * NR];
 #pragma unroll
-                for (int k = 0; k < 32; ++k) flat[k] = 0;
+                for (int k = 0; k < 4 * NR; ++k) flat[k] = 0;
 #pragma unroll
                 for (int p = 0; p < 5; ++p)
 #pragma unroll
@@ -251,15 +210,14 @@ k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                         if (p < planes && (uint32_t)w < W) {
                             const uint32_t k = (uint32_t)p * W + w;
 #pragma unroll
-                            for (int kk = 0; kk < 32; ++kk)
+                            for (int kk = 0; kk < 4 * NR; ++kk)
                                 if ((uint32_t)kk == k) flat[kk] = wd[p][w];
                         }
 #pragma unroll
-                for (int q = 0; q < 8; ++q)
-                    rec[q] = make_uint4(flat[4 * q], flat[4 * q + 1], flat[4 * q + 2], flat[4 * q + 3]);
+                for (int q = 0; q < NR; ++q) rec[q] = make_uint4(flat[4 * q], flat[4 * q + 1], flat[4 * q + 2], flat[4 * q + 3]);
             } else {
 #pragma unroll
-                for (int q = 0; q < 8; ++q) {
+                for (int q = 0; q < NR; ++q) {
                     uint32_t wv[4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
@@ -276,45 +234,34 @@ k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                 }
             }
         }
-        GenePairIt it;
-        it.init(vbits + (size_t)row * g.VW, g.VW, jbits + (size_t)row * g.JW, g.JW, act);
-        const uint64_t v0 = act ? vbits[(size_t)row * g.VW] : 0, j0 = act ? jbits[(size_t)row * g.JW] : 0;
-        while (__any_sync(0xFFFFFFFFu, it.has)) {
-            uint32_t b = kNone, v = 0, j = 0;
-            if (it.has) {
-                v = it.v();
-                j = it.j();
-                if (v < g.Gv && j < g.Gj) b = g.bin(r, v, j, L, cls);
-            }
-            const uint32_t grp = __match_any_sync(0xFFFFFFFFu, b);
-            const uint32_t leader = (uint32_t)__ffs(grp) - 1;
-            const uint64_t sv = below(v0, v), sj = below(j0, j);
-            // AND of the group's signatures (all lanes take part, each with its group)
-            const uint32_t a0 = __reduce_and_sync(grp, (uint32_t)sv);
-            const uint32_t a1 = __reduce_and_sync(grp, (uint32_t)(sv >> 32));
-            const uint32_t a2 = __reduce_and_sync(grp, (uint32_t)sj);
-            const uint32_t a3 = __reduce_and_sync(grp, (uint32_t)(sj >> 32));
-            uint32_t base = 0;
-            if (lane == leader && b != kNone) {
-                atomicAnd(&sig_and[2 * (size_t)b], ((unsigned long long)a1 << 32) | a0);
-                atomicAnd(&sig_and[2 * (size_t)b + 1], ((unsigned long long)a3 << 32) | a2);
-                base = atomicAdd(&cursor[b], (uint32_t)__popc(grp));
-            }
-            base = __shfl_sync(0xFFFFFFFFu, base, leader);
-            if (b != kNone) {
-                const uint64_t pos = (uint64_t)bin_start[b] + base + __popc(grp & ((1u << lane) - 1u));
-                if (pos >= cap_entries) {
-                    atomicOr(err, kErrEntryOverflow);
-                } else {
-                    ent_uid[pos] = u;
-                    // side record: signature below (v, j) and the unique id
-                    ent_meta[pos] = make_uint4((uint32_t)sv, (uint32_t)(sv >> 32), (uint32_t)sj, u);
-                    uint4 *dst = ent_rec + pos * rs16;
-                    if (small) {
+        for (uint32_t vw = 0; vw < g.VW; ++vw) {
+            uint64_t vb = vbits[(size_t)row * g.VW + vw];
+            while (vb) {
+                const uint32_t v = vw * 64 + lowest_bit64(vb);
+                vb &= vb - 1;
+                if (v >= g.Gv) break;
+                for (uint32_t jw = 0; jw < g.JW; ++jw) {
+                    uint64_t jb = jbits[(size_t)row * g.JW + jw];
+                    while (jb) {
+                        const uint32_t j = jw * 64 + lowest_bit64(jb);
+                        jb &= jb - 1;
+                        if (j >= g.Gj) break;
+                        const uint32_t b = g.bin(r, v, j, L, uclass[u]);
+                        const uint64_t sv = below(vbits[(size_t)row * g.VW], v);
+                        const uint64_t sj = below(jbits[(size_t)row * g.JW], j);
+                        atomicAnd(&sig_and[2 * (size_t)b], sv);
+                        atomicAnd(&sig_and[2 * (size_t)b + 1], sj);
+                        const uint64_t pos = (uint64_t)bin_start[b] + atomicAdd(&cursor[b], 1u);
+                        if (pos >= cap_entries) { atomicOr(err, kErrEntryOverflow); continue; }
+                        ent_uid[pos] = u;
+                        // side record: signature below (v, j) and the unique id
+                        ent_meta[pos] = make_uint4((uint32_t)sv, (uint32_t)(sv >> 32), (uint32_t)sj, u);
+                        uint4 *dst = ent_rec + pos * rs16;
+                        if (small) {
 #pragma unroll
-                        for (int q = 0; q < 8; ++q)
-                            if ((uint32_t)q < rs16) dst[q] = rec[q];
-                    } else {
+                            for (int q = 0; q < NR; ++q) dst[q] = rec[q];
+                            continue;
+                        }
                         // long records (generic path): code bytes, 16 at a time
                         for (uint32_t q = 0; q < rs16; ++q) {
                             uint32_t wv[4];
@@ -333,10 +280,6 @@ k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                         }
                     }
                 }
-            }
-            if (it.has) {
-                if (b == kNone) it.has = false;   // a gene index beyond the list: stop (as before)
-                else it.advance();
             }
         }
     }
@@ -508,10 +451,21 @@ void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
     cudaMemsetAsync(B.bin_cursor, 0, sizeof(uint32_t) * P.nbins, s);
     cudaMemsetAsync(B.sig_and, 0xFF, sizeof(unsigned long long) * 2 * P.nbins, s);
     const int planes = (P.fast && P.hamming) ? (int)P.B : 0;
-    k_bin_fill<<<grid_for(P.N), kThreads, 0, s>>>(
-        g, B.ctr, B.urow, B.ulen, B.urep, B.uclass, B.sig_and, B.vbits, B.jbits, B.seq, B.seq_off,
-        B.codemap, B.bin_hist, B.bin_cursor, B.ent_uid, B.ent_rec, B.ent_meta, P.RS / 16, planes, P.W,
-        P.cap_entries, &B.ctr->error);
+    const uint32_t rs16 = P.RS / 16;
+    auto go = [&](auto kern) {
+        kern<<<grid_for(P.N), kThreads, 0, s>>>(
+            g, B.ctr, B.urow, B.ulen, B.urep, B.uclass, B.sig_and, B.vbits, B.jbits, B.seq, B.seq_off,
+            B.codemap, B.bin_hist, B.bin_cursor, B.ent_uid, B.ent_rec, B.ent_meta, rs16, planes, P.W,
+            P.cap_entries, &B.ctr->error);
+    };
+    switch (rs16) {
+        case 1: go(k_bin_fill<1>); break;
+        case 2: go(k_bin_fill<2>); break;
+        case 3: go(k_bin_fill<3>); break;
+        case 4: go(k_bin_fill<4>); break;
+        case 5: case 6: case 7: case 8: go(k_bin_fill<8>); break;
+        default: go(k_bin_fill<0>); break;
+    }
 }
 
 void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s) {

@@ -270,6 +270,100 @@ __device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, co
     }
 }
 
+// The y loop of one Hamming unit.  FULL: every r-block of the lane's x-entries
+// is inside the unit, so all RX chains run without branches; otherwise the
+// chains of r-blocks past the unit's end are skipped.
+template <int BP, int W, int RX, int EM, bool FULL>
+__device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew, const Unit &U,
+                                               const uint32_t (&x)[RX][BP * W],
+                                               const uint32_t (&vmask)[RX], uint32_t valid,
+                                               uint4 *sy, uint4 *sym, uint4 *sxm, uint32_t *shq,
+                                               int lane) {
+    constexpr int NW = BP * W;
+    constexpr int R16 = (NW + 3) / 4;
+    const uint32_t rb = (U.nx + 31) >> 5;   // r-blocks holding entries
+    // a pair is a hit iff its score <= thr (score: d&(d-1) for eps 1, d for
+    // eps 0, the popcount otherwise); masked entries score >= kOff
+    const uint32_t thr = EM == 0 ? (uint32_t)max(U.P.eps, 0) : 0u;
+    const bool neg = EM == 0 && U.P.eps < 0;       // no pair can be a neighbour
+    const uint32_t same = U.P.same;
+    const uint32_t yrow0 = (same ? U.P.a_start : U.P.b_start) + U.ybase;
+    for (uint32_t yb = 0; yb < U.ny && !neg; yb += kYB) {
+        const uint32_t nb = min((uint32_t)kYB, U.ny - yb);
+        const uint4 *src = a.rec + (size_t)(yrow0 + yb) * R16;
+        for (uint32_t t = lane; t < nb * R16; t += 32) sy[t] = __ldg(src + t);
+        for (uint32_t t = lane; t < nb; t += 32) sym[t] = __ldg(a.meta + yrow0 + yb + t);
+        __syncwarp();
+        uint32_t qn = 0;
+        for (uint32_t t = 0; t < nb; ++t) {
+            const uint32_t yp = U.ybase + yb + t;
+            // same bin: only x-entries before y count; none before -> skip y
+            if (same && yp <= U.xbase) continue;
+            uint32_t y[NW];
+#pragma unroll
+            for (int q = 0; q < R16; ++q) {
+                const uint4 v = sy[t * R16 + q];
+                const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (4 * q + e < NW) y[4 * q + e] = w4[e];
+            }
+            // FULL: all RX chains without branches (independent, interleaved);
+            // otherwise only the r-blocks that hold entries (warp-uniform test)
+            uint32_t sc[RX];
+#pragma unroll
+            for (int r = 0; r < RX; ++r) {
+                if (!FULL && r >= rb) { sc[r] = kOff; continue; }
+                if (W == 1) {
+                    uint32_t d = x[r][0] ^ y[0];
+#pragma unroll
+                    for (int p = 1; p < BP; ++p) d |= x[r][p] ^ y[p];
+                    sc[r] = (EM == 2 ? d : (EM == 1 ? (d & (d - 1u)) : (uint32_t)__popc(d))) | vmask[r];
+                } else {
+                    uint32_t dist = 0;
+#pragma unroll
+                    for (int w = 0; w < W; ++w) {
+                        uint32_t d = x[r][w] ^ y[w];
+#pragma unroll
+                        for (int p = 1; p < BP; ++p) d |= x[r][p * W + w] ^ y[p * W + w];
+                        dist += __popc(d);
+                    }
+                    sc[r] = dist | vmask[r];
+                }
+            }
+            // y inside the unit's own x range (same bin): mask x-entries not before y
+            if (same && yp < U.xbase + U.nx) {
+                const uint32_t nact = yp - U.xbase;
+#pragma unroll
+                for (int r = 0; r < RX; ++r)
+                    if ((uint32_t)r * 32 + lane >= nact) sc[r] |= kOff;
+            }
+            uint32_t z = sc[0];
+#pragma unroll
+            for (int r = 1; r < RX; ++r) z = min(z, sc[r]);
+            if (z <= thr) {
+                uint32_t hit = 0;
+#pragma unroll
+                for (int r = 0; r < RX; ++r) hit |= (uint32_t)(sc[r] <= thr) << r;
+                shq[qn++ * 32 + lane] = (t << 8) | (hit & valid);
+            }
+            if (__any_sync(0xFFFFFFFFu, qn == kHitQ)) {
+                __syncwarp();
+                drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same,
+                           U.P.v, U.P.j, lane);
+                qn = 0;
+                __syncwarp();
+            }
+        }
+        if (__any_sync(0xFFFFFFFFu, qn)) {
+            __syncwarp();
+            drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same,
+                       U.P.v, U.P.j, lane);
+        }
+        __syncwarp();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Hamming, fast path.  BP planes x W words per record; RX x-entries per lane.
 // EM: 0 = popcount test, 1 = eps == 1 (d & (d-1)) == 0, 2 = eps == 0.
@@ -312,84 +406,12 @@ k_hamming(DistArgs a) {
             if (ok) pairs += unit_pairs(U, U.xbase + xi);
             sxm[wid][xi] = __ldg(a.meta + U.P.a_start + U.xbase + (ok ? xi : 0));
         }
-        // a pair is a hit iff its score <= thr (score: d&(d-1) for eps 1, d for
-        // eps 0, the popcount otherwise); masked entries score >= kOff
-        const uint32_t thr = EM == 0 ? (uint32_t)max(U.P.eps, 0) : 0u;
-        const bool neg = EM == 0 && U.P.eps < 0;       // no pair can be a neighbour
-        const uint32_t same = U.P.same;
-        const uint32_t yrow0 = (same ? U.P.a_start : U.P.b_start) + U.ybase;
-        for (uint32_t yb = 0; yb < U.ny && !neg; yb += kYB) {
-            const uint32_t nb = min((uint32_t)kYB, U.ny - yb);
-            const uint4 *src = a.rec + (size_t)(yrow0 + yb) * R16;
-            for (uint32_t t = lane; t < nb * R16; t += 32) sy[wid][t] = __ldg(src + t);
-            for (uint32_t t = lane; t < nb; t += 32) sym[wid][t] = __ldg(a.meta + yrow0 + yb + t);
-            __syncwarp();
-            uint32_t qn = 0;
-            for (uint32_t t = 0; t < nb; ++t) {
-                const uint32_t yp = U.ybase + yb + t;
-                // same bin: only x-entries before y count; none before -> skip y
-                if (same && yp <= U.xbase) continue;
-                uint32_t y[NW];
-#pragma unroll
-                for (int q = 0; q < R16; ++q) {
-                    const uint4 v = sy[wid][t * R16 + q];
-                    const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
-#pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        if (4 * q + e < NW) y[4 * q + e] = w4[e];
-                }
-                // all RX chains without branches (independent, interleaved)
-                uint32_t sc[RX];
-#pragma unroll
-                for (int r = 0; r < RX; ++r) {
-                    if (W == 1) {
-                        uint32_t d = x[r][0] ^ y[0];
-#pragma unroll
-                        for (int p = 1; p < BP; ++p) d |= x[r][p] ^ y[p];
-                        sc[r] = (EM == 2 ? d : (EM == 1 ? (d & (d - 1u)) : (uint32_t)__popc(d))) | vmask[r];
-                    } else {
-                        uint32_t dist = 0;
-#pragma unroll
-                        for (int w = 0; w < W; ++w) {
-                            uint32_t d = x[r][w] ^ y[w];
-#pragma unroll
-                            for (int p = 1; p < BP; ++p) d |= x[r][p * W + w] ^ y[p * W + w];
-                            dist += __popc(d);
-                        }
-                        sc[r] = dist | vmask[r];
-                    }
-                }
-                // y inside the unit's own x range (same bin): mask x-entries not before y
-                if (same && yp < U.xbase + U.nx) {
-                    const uint32_t nact = yp - U.xbase;
-#pragma unroll
-                    for (int r = 0; r < RX; ++r)
-                        if ((uint32_t)r * 32 + lane >= nact) sc[r] |= kOff;
-                }
-                uint32_t z = sc[0];
-#pragma unroll
-                for (int r = 1; r < RX; ++r) z = min(z, sc[r]);
-                if (z <= thr) {
-                    uint32_t hit = 0;
-#pragma unroll
-                    for (int r = 0; r < RX; ++r) hit |= (uint32_t)(sc[r] <= thr) << r;
-                    shq[wid][qn++ * 32 + lane] = (t << 8) | (hit & valid);
-                }
-                if (__any_sync(0xFFFFFFFFu, qn == kHitQ)) {
-                    __syncwarp();
-                    drain_hits(a, ew, shq[wid], qn, sxm[wid], sym[wid], U.xbase, U.ybase + yb, same,
-                               U.P.v, U.P.j, lane);
-                    qn = 0;
-                    __syncwarp();
-                }
-            }
-            if (__any_sync(0xFFFFFFFFu, qn)) {
-                __syncwarp();
-                drain_hits(a, ew, shq[wid], qn, sxm[wid], sym[wid], U.xbase, U.ybase + yb, same,
-                           U.P.v, U.P.j, lane);
-            }
-            __syncwarp();
-        }
+        if (U.nx == (uint32_t)(32 * RX))
+            hamming_unit_y<BP, W, RX, EM, true>(a, ew, U, x, vmask, valid, sy[wid], sym[wid], sxm[wid],
+                                                shq[wid], lane);
+        else
+            hamming_unit_y<BP, W, RX, EM, false>(a, ew, U, x, vmask, valid, sy[wid], sym[wid],
+                                                 sxm[wid], shq[wid], lane);
         log_unit(a, U, lane);
     }
     finish(a, ew, pairs, lane);

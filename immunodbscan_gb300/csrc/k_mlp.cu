@@ -37,6 +37,7 @@ static_assert(kOffB3 + 1 == kMlpParams, "parameter layout");
 namespace {
 
 constexpr int kThreads = 128;
+constexpr uint32_t kLearnMinPairs = 4096;   // smaller bin pairs skip the network
 
 // Features of one bin pair (also used by the host to build training sets).
 __device__ void binpair_features(const BinPair &P, float *f) {
@@ -82,24 +83,31 @@ k_mlp_predict_bf16(const Counters *__restrict__ ctr, const BinPair *__restrict__
     const uint32_t n = ctr->n_binpairs;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        const BinPair P = bp[i];
+        // bin pairs below kLearnMinPairs are cheap whatever their order: they take
+        // the lightest class without running the network
+        if (P.cost_lo < kLearnMinPairs) { pred[i] = 1.0f; continue; }
         float f[kIn];
-        binpair_features(bp[i], f);
+        binpair_features(P, f);
         __nv_bfloat16 x[kIn];
 #pragma unroll
         for (int k = 0; k < kIn; ++k) x[k] = __float2bfloat16(f[k]);
-        __nv_bfloat16 h1[kH];
+        // fully unrolled so the activations stay in registers
+        float h1[kH];
+#pragma unroll
         for (int j = 0; j < kH; ++j) {
             float acc = __bfloat162float(w[kOffB1 + j]);
 #pragma unroll
             for (int k = 0; k < kIn; ++k)
                 acc = fmaf(__bfloat162float(x[k]), __bfloat162float(w[kOffW1 + k * kH + j]), acc);
-            h1[j] = __float2bfloat16(fmaxf(acc, 0.0f));
+            h1[j] = __bfloat162float(__float2bfloat16(fmaxf(acc, 0.0f)));
         }
         float y = __bfloat162float(w[kOffB3]);
         for (int j = 0; j < kH; ++j) {
             float acc = __bfloat162float(w[kOffB2 + j]);
+#pragma unroll
             for (int k = 0; k < kH; ++k)
-                acc = fmaf(__bfloat162float(h1[k]), __bfloat162float(w[kOffW2 + k * kH + j]), acc);
+                acc = fmaf(h1[k], __bfloat162float(w[kOffW2 + k * kH + j]), acc);
             const float h2 = __bfloat162float(__float2bfloat16(fmaxf(acc, 0.0f)));
             y = fmaf(h2, __bfloat162float(w[kOffW3 + j]), y);
         }
