@@ -69,7 +69,7 @@ enum BufId {
     bURow, bUCopies, bULen, bURep, bBinHist, bBinCursor, bEntUid, bEntRec, bBpCount, bBp,
     bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bDeg, bGOff, bGCur, bAdj, bCnt, bUCore,
     bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
-    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bNumBufs
+    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bBpSmall, bNumBufs
 };
 
 }  // namespace
@@ -512,6 +512,7 @@ idb_status alloc_binpairs(Pipeline &pl, uint64_t n_bp) {
     TRY(ensure(c, bBp, sizeof(BinPair) * pl.P.cap_binpairs));
     TRY(ensure(c, bBpSorted, sizeof(BinPair) * pl.P.cap_binpairs));
     TRY(ensure(c, bBpUnits, 4 * (pl.P.cap_binpairs + 1)));
+    TRY(ensure(c, bBpSmall, 4 * (pl.P.cap_binpairs + 1)));
     TRY(ensure(c, bPred, 4 * (pl.P.cap_binpairs + 1)));
     const uint64_t need = scan_part_needed(pl.P.cap_binpairs + 1);
     if (need > pl.B.scan_part_cap) {
@@ -522,6 +523,7 @@ idb_status alloc_binpairs(Pipeline &pl, uint64_t n_bp) {
     pl.B.bp = ptr<BinPair>(c, bBp);
     pl.B.bp_sorted = ptr<BinPair>(c, bBpSorted);
     pl.B.bp_units = ptr<uint32_t>(c, bBpUnits);
+    pl.B.bp_small = ptr<uint32_t>(c, bBpSmall);
     pl.B.pred = ptr<float>(c, bPred);
     return IDB_OK;
 }

@@ -16,6 +16,9 @@ constexpr int kGenericMaxLen = 1024;    // Levenshtein on the generic path
 constexpr int kDepthMax = 50;           // tree-depth histogram cap (cuda/PSDBSCAN.hcu:1029)
 constexpr uint32_t kEdgeChunk = 256;    // edge slots reserved per warp at a time
 constexpr uint32_t kSpinCap = 1u << 22; // bound of every device-side retry loop
+// Bin pairs with at most kSmallSide entries on each side (Hamming fast path) are
+// evaluated pair-parallel: lanes take pairs, records travel by shuffles.
+constexpr uint32_t kSmallSide = 32;
 constexpr int kMlpIn = 16;              // learned scheduler: features per bin pair
 constexpr int kMlpHidden = 64;          // two hidden layers of 64
 constexpr int kMlpParams = kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +
@@ -69,7 +72,9 @@ struct Counters {
     unsigned long long admissible_pairs;
     unsigned long long stamp[8];  // %globaltimer at the phase boundaries (ns)
     unsigned long long lev_columns;  // text columns consumed by live Levenshtein pairs
-    uint32_t pad[4];
+    uint32_t n_small;            // small bin pairs handed to the pair-parallel path
+    uint32_t small_cursor;       // their work queue head
+    uint32_t pad[2];
 };
 
 // One bucket ("bin") holds the uniques of one (repertoire, V gene, J gene,
@@ -158,6 +163,7 @@ struct Buffers {
     uint32_t *bp_count = nullptr;                   // [nbins+1]
     BinPair *bp = nullptr, *bp_sorted = nullptr;    // [cap_binpairs]
     uint32_t *bp_units = nullptr;                   // [cap_binpairs+1]
+    uint32_t *bp_small = nullptr;                   // [cap_binpairs] schedule positions of small bin pairs
     uint32_t *cls_hist = nullptr;                   // [65]
     float *pred = nullptr;                          // learned cost per bin pair
     // graph

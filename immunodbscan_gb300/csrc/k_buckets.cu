@@ -393,7 +393,9 @@ __global__ void k_cls_hist(const Counters *__restrict__ ctr, const BinPair *__re
 __global__ void k_cls_scatter(const Counters *__restrict__ ctr, const BinPair *__restrict__ bp,
                               const float *__restrict__ pred, const uint32_t *__restrict__ start,
                               uint32_t *__restrict__ cursor, BinPair *__restrict__ out,
-                              uint32_t *__restrict__ units, uint32_t TX, uint32_t TY, uint32_t q) {
+                              uint32_t *__restrict__ units, uint32_t TX, uint32_t TY, uint32_t q,
+                              int small_mode, uint32_t *__restrict__ small_list,
+                              uint32_t *__restrict__ n_small) {
     const uint32_t n = ctr->n_binpairs;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -407,7 +409,10 @@ __global__ void k_cls_scatter(const Counters *__restrict__ ctr, const BinPair *_
         P.cls = (uint8_t)cls;
         out[pos] = P;
         uint64_t nu;
-        if (P.same) {
+        if (small_mode && P.a_n <= kSmallSide && (P.same || P.b_n <= kSmallSide)) {
+            nu = 0;                               // pair-parallel path, no tiled units
+            small_list[atomicAdd(n_small, 1u)] = pos;
+        } else if (P.same) {
             const uint32_t ncy = (P.a_n + TY - 1) / TY;
             nu = tri_units(P.ncx, ncy, q);
         } else {
@@ -463,7 +468,10 @@ void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
         case 2: go(k_bin_fill<2>); break;
         case 3: go(k_bin_fill<3>); break;
         case 4: go(k_bin_fill<4>); break;
-        case 5: case 6: case 7: case 8: go(k_bin_fill<8>); break;
+        case 5: go(k_bin_fill<5>); break;
+        case 6: go(k_bin_fill<6>); break;
+        case 7: go(k_bin_fill<7>); break;
+        case 8: go(k_bin_fill<8>); break;
         default: go(k_bin_fill<0>); break;
     }
 }
@@ -491,8 +499,10 @@ void launch_schedule(const Plan &P, const Buffers &B, cudaStream_t s) {
     cudaMemsetAsync(B.cls_hist, 0, sizeof(uint32_t) * 130, s);
     k_cls_hist<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(B.ctr, B.bp, pred, B.cls_hist);
     scan_u32(B.cls_hist, B.cls_hist, 64, nullptr, nullptr, B.scan_part, B.scan_part_cap, s);
+    cudaMemsetAsync(&B.ctr->n_small, 0, 2 * sizeof(uint32_t), s);   // n_small, small_cursor
     k_cls_scatter<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(
-        B.ctr, B.bp, pred, B.cls_hist, B.cls_hist + 64, B.bp_sorted, B.bp_units, P.TX, P.TY, q);
+        B.ctr, B.bp, pred, B.cls_hist, B.cls_hist + 64, B.bp_sorted, B.bp_units, P.TX, P.TY, q,
+        (P.fast && P.hamming) ? 1 : 0, B.bp_small, &B.ctr->n_small);
     scan_u32(B.bp_units, B.bp_units, (uint32_t)P.cap_binpairs, &B.ctr->n_binpairs,
              &B.ctr->n_units, B.scan_part, B.scan_part_cap, s);
     k_set_unit_base<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(B.ctr, B.bp_sorted, B.bp_units);

@@ -52,6 +52,7 @@ struct DistArgs {
     uint32_t *bp_hits;
     const uint4 *meta;               // per entry {sigV lo, sigV hi, sigJ, uid}
     int sig_exact;                   // signatures decide canonicity exactly
+    const uint32_t *small_list;      // schedule positions of the small bin pairs
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -252,6 +253,113 @@ __device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, u
     }
 }
 
+// Pair p of a small bin pair -> (i, j).  One bin: i < j < n, ordered by j
+// (pairs of j start at j(j-1)/2).  Two bins: i = p mod n, j = p div n.
+__device__ __forceinline__ void small_pair(uint32_t p, bool same, uint32_t n, uint32_t &i,
+                                           uint32_t &j) {
+    if (same) {
+        uint32_t jj = (uint32_t)((1.0f + sqrtf(8.0f * (float)p + 1.0f)) * 0.5f);
+        while (jj > 1 && jj * (jj - 1) / 2 > p) --jj;
+        while (jj * (jj + 1) / 2 <= p) ++jj;
+        j = jj;
+        i = p - jj * (jj - 1) / 2;
+    } else {
+        j = p / n;
+        i = p - j * n;
+    }
+}
+
+// Next small bin pair for this warp (schedule position), false when none is left.
+__device__ __forceinline__ bool next_small(const DistArgs &a, uint32_t n_small, int lane,
+                                           uint32_t &idx) {
+    uint32_t s = 0;
+    if (lane == 0) s = atomicAdd(&a.ctr->small_cursor, 1u);
+    s = __shfl_sync(0xFFFFFFFFu, s, 0);
+    if (s >= n_small) return false;
+    idx = a.small_list[s];
+    return true;
+}
+
+// A small bin pair (at most kSmallSide entries a side), pair-parallel: lane l
+// holds entry l of each side; each round the lanes take 32 pairs and fetch
+// the two records by shuffles.  Canonicity of a hit is decided from the side
+// records (global loads: hits are rare).
+template <int BP, int W, int EM>
+__device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew, uint32_t idx,
+                                              int lane, uint64_t &pairs) {
+    constexpr int NW = BP * W;
+    constexpr int R16 = (NW + 3) / 4;
+    const long long t0 = a.bp_cycles ? clock64() : 0;
+    const BinPair P = a.bp[idx];
+    const bool same = P.same != 0;
+    const uint32_t n = P.a_n, m = same ? P.a_n : P.b_n;
+    const uint32_t ystart = same ? P.a_start : P.b_start;
+    uint32_t xr[NW], yr[NW];
+    {
+        const uint4 *src = a.rec + (size_t)(P.a_start + ((uint32_t)lane < n ? lane : 0)) * R16;
+        const uint4 *srcy = a.rec + (size_t)(ystart + ((uint32_t)lane < m ? lane : 0)) * R16;
+#pragma unroll
+        for (int q = 0; q < R16; ++q) {
+            const uint4 v = __ldg(src + q);
+            const uint4 u = same ? v : __ldg(srcy + q);
+            const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+            const uint32_t u4[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+                if (4 * q + e < NW) { xr[4 * q + e] = w4[e]; yr[4 * q + e] = u4[e]; }
+        }
+    }
+    const uint32_t npairs = same ? n * (n - 1) / 2 : n * m;
+    if (lane == 0) pairs += npairs;
+    const uint32_t thr = EM == 0 ? (uint32_t)max(P.eps, 0) : 0u;
+    const bool neg = EM == 0 && P.eps < 0;
+    for (uint32_t p0 = 0; p0 < npairs && !neg; p0 += 32) {
+        const uint32_t p = p0 + lane;
+        const bool act = p < npairs;
+        uint32_t i = 0, j = 0;
+        if (act) small_pair(p, same, n, i, j);
+        uint32_t sc;
+        if (W == 1) {
+            uint32_t d = __shfl_sync(0xFFFFFFFFu, xr[0], i) ^ __shfl_sync(0xFFFFFFFFu, yr[0], j);
+#pragma unroll
+            for (int q = 1; q < BP; ++q)
+                d |= __shfl_sync(0xFFFFFFFFu, xr[q], i) ^ __shfl_sync(0xFFFFFFFFu, yr[q], j);
+            sc = EM == 2 ? d : (EM == 1 ? (d & (d - 1u)) : (uint32_t)__popc(d));
+        } else {
+            uint32_t dist = 0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                uint32_t d = __shfl_sync(0xFFFFFFFFu, xr[w], i) ^ __shfl_sync(0xFFFFFFFFu, yr[w], j);
+#pragma unroll
+                for (int q = 1; q < BP; ++q)
+                    d |= __shfl_sync(0xFFFFFFFFu, xr[q * W + w], i) ^
+                         __shfl_sync(0xFFFFFFFFu, yr[q * W + w], j);
+                dist += __popc(d);
+            }
+            sc = dist;
+        }
+        const bool hit = act && sc <= thr;
+        if (__any_sync(0xFFFFFFFFu, hit)) {
+            bool ok = hit;
+            uint4 mx = make_uint4(0, 0, 0, 0), my = mx;
+            if (ok) {
+                mx = __ldg(a.meta + P.a_start + i);
+                my = __ldg(a.meta + ystart + j);
+                if (a.sig_exact) {
+                    ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
+                } else {
+                    const uint32_t rx = a.urow[mx.w], ry = a.urow[my.w];
+                    ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)P.v &&
+                         lowest_common(a.jbits, a.JW, rx, ry) == (int)P.j;
+                }
+            }
+            ew.append(a, lane, ok, min(mx.w, my.w), max(mx.w, my.w));
+        }
+    }
+    if (a.bp_cycles && lane == 0)
+        atomicAdd(&a.bp_cycles[idx], (unsigned long long)(clock64() - t0));
+}
+
 // Deferred hits: the Hamming loop only records, per lane, (y index in the staged
 // chunk, hit bits) in a small shared-memory queue; the queue is drained here when
 // a lane's queue is full or the chunk ends, with every lane taking part.
@@ -369,7 +477,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
 // EM: 0 = popcount test, 1 = eps == 1 (d & (d-1)) == 0, 2 = eps == 0.
 // ---------------------------------------------------------------------------
 template <int BP, int W, int RX, int EM>
-__global__ void __launch_bounds__(kWarps * 32, 4)
+__global__ void __launch_bounds__(kWarps * 32, (W == 1 && RX <= 4 ? 5 : 4))
 k_hamming(DistArgs a) {
     constexpr int NW = BP * W;                 // words per record used
     constexpr int R16 = (NW + 3) / 4;          // 16-byte words per record
@@ -414,6 +522,10 @@ k_hamming(DistArgs a) {
                                                  sxm[wid], shq[wid], lane);
         log_unit(a, U, lane);
     }
+    // then the small bin pairs (they also fill the tail of the tiled work)
+    const uint32_t n_small = a.ctr->n_small;
+    uint32_t sidx = 0;
+    while (next_small(a, n_small, lane, sidx)) hamming_small<BP, W, EM>(a, ew, sidx, lane, pairs);
     finish(a, ew, pairs, lane);
 }
 
@@ -643,6 +755,20 @@ k_count_admissible(DistArgs a) {
             cnt += canonical(a, U.P, ux, uy);
         }
     }
+    const uint32_t n_small = a.ctr->n_small;
+    uint32_t sidx = 0;
+    while (next_small(a, n_small, lane, sidx)) {
+        const BinPair P = a.bp[sidx];
+        if (P.eps < 0) continue;
+        const bool same = P.same != 0;
+        const uint32_t ystart = same ? P.a_start : P.b_start;
+        const uint32_t npairs = same ? P.a_n * (P.a_n - 1) / 2 : P.a_n * P.b_n;
+        for (uint32_t p = lane; p < npairs; p += 32) {
+            uint32_t i, j;
+            small_pair(p, same, P.a_n, i, j);
+            cnt += canonical(a, P, a.ent_uid[P.a_start + i], a.ent_uid[ystart + j]);
+        }
+    }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) cnt += __shfl_xor_sync(0xFFFFFFFFu, cnt, d);
     if (lane == 0 && cnt) atomicAdd(&a.ctr->admissible_pairs, cnt);
@@ -692,12 +818,14 @@ static DistArgs make_args(const Plan &P, const Buffers &B) {
     a.bp_hits = B.bp_hits;
     a.meta = B.ent_meta;
     a.sig_exact = P.sig_exact ? 1 : 0;
+    a.small_list = B.bp_small;
     return a;
 }
 
 void launch_count_admissible(const Plan &P, const Buffers &B, cudaStream_t s) {
     DistArgs a = make_args(P, B);
     cudaMemsetAsync(&B.ctr->unit_cursor, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(&B.ctr->small_cursor, 0, sizeof(uint32_t), s);
     run(k_count_admissible, a, 0, 0, s);
 }
 
@@ -708,6 +836,8 @@ const char *distance_variant_name(const Plan &P) {
 
 void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s) {
     DistArgs a = make_args(P, B);
+    cudaMemsetAsync(&B.ctr->unit_cursor, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(&B.ctr->small_cursor, 0, sizeof(uint32_t), s);
     if (!P.fast) {
         if (P.hamming) run(k_generic<true>, a, 0, grid, s);
         else run(k_generic<false>, a, 0, grid, s);
