@@ -74,7 +74,8 @@ struct Counters {
     unsigned long long lev_columns;  // text columns consumed by live Levenshtein pairs
     uint32_t n_small;            // small bin pairs handed to the pair-parallel path
     uint32_t small_cursor;       // their work queue head
-    uint32_t pad[2];
+    uint32_t n_heavy;            // bin pairs the learned predictor evaluates
+    uint32_t pad[1];
 };
 
 // One bucket ("bin") holds the uniques of one (repertoire, V gene, J gene,

@@ -12,14 +12,16 @@
 //  labels (S7)       cuda/PSDBSCAN.hcu:1263-1294 (+ tree_reduction_kernel :129-149)
 //  tree depths       cuda/PSDBSCAN.hcu:154-177, 1020-1040
 //
-// Here the neighbour pairs found by the distance kernel form an edge list that
-// is turned into a CSR graph by count / scan / fill.  Counts are accumulated
-// per edge, unions hook the larger root under the smaller one with atomicCAS
-// and find() halves paths, so every component's root is its minimum core
-// index, as in the reference.  A border unique joins the cluster of its
-// minimum-index core neighbour (deterministic; one of the outcomes the
-// reference's race allows).  Labels are 1 + the rank of the root among the
-// repertoire's core roots, found with one exclusive scan over root flags.
+// Here the neighbour pairs found by the distance kernel form an edge list.
+// Counts are accumulated per edge; core-core edges are merged by unions that
+// hook the larger root under the smaller one with atomicCAS while find()
+// halves paths, so every component's root is its minimum core index, as in the
+// reference.  The core-to-non-core edges form a CSR graph (count in the union
+// pass / scan / fill) whose row of a non-core unique lists its core
+// neighbours; the unique joins the cluster of the minimum one (deterministic;
+// one of the outcomes the reference's race allows).  Labels are 1 + the rank
+// of the root among the repertoire's core roots, found with one exclusive
+// scan over root flags.
 #include "idb_internal.cuh"
 
 namespace idb {
@@ -53,33 +55,32 @@ __global__ void k_graph_init(const Counters *__restrict__ ctr, const uint32_t *_
     }
 }
 
-// count pass: degrees for the CSR and copies-weighted neighbour counts
-__global__ void k_degree(const Counters *__restrict__ ctr, uint64_t cap, const uint2 *__restrict__ edges,
-                         const uint32_t *__restrict__ ucopies, uint32_t *__restrict__ deg,
-                         uint32_t *__restrict__ cnt) {
+// count pass: copies-weighted neighbour counts (S5)
+__global__ void k_count(const Counters *__restrict__ ctr, uint64_t cap, const uint2 *__restrict__ edges,
+                        const uint32_t *__restrict__ ucopies, uint32_t *__restrict__ cnt) {
     const uint32_t ne = edge_slots(ctr, cap);
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
         const uint2 ed = edges[e];
         if (ed.x == kNone) continue;
-        atomicAdd(&deg[ed.x], 1u);
-        atomicAdd(&deg[ed.y], 1u);
         atomicAdd(&cnt[ed.x], ucopies[ed.y]);
         atomicAdd(&cnt[ed.y], ucopies[ed.x]);
     }
 }
 
-// fill pass
+// fill pass of the border CSR: each non-core unique lists its core neighbours
 __global__ void k_fill_adj(const Counters *__restrict__ ctr, uint64_t cap, const uint2 *__restrict__ edges,
-                           const uint32_t *__restrict__ off, uint32_t *__restrict__ cursor,
-                           uint32_t *__restrict__ adj) {
+                           const uint32_t *__restrict__ ucore, const uint32_t *__restrict__ off,
+                           uint32_t *__restrict__ cursor, uint32_t *__restrict__ adj) {
     const uint32_t ne = edge_slots(ctr, cap);
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
         const uint2 ed = edges[e];
         if (ed.x == kNone) continue;
-        adj[off[ed.x] + atomicAdd(&cursor[ed.x], 1u)] = ed.y;
-        adj[off[ed.y] + atomicAdd(&cursor[ed.y], 1u)] = ed.x;
+        const uint32_t cx = ucore[ed.x], cy = ucore[ed.y];
+        if (cx == cy) continue;
+        const uint32_t nc = cx ? ed.y : ed.x, c = cx ? ed.x : ed.y;
+        adj[off[nc] + atomicAdd(&cursor[nc], 1u)] = c;
     }
 }
 
@@ -110,13 +111,19 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t *p, uint32_t x) {
     }
 }
 
+// Core-core edges are merged (S6); an edge with one core end counts towards
+// the border CSR degree of its non-core end.
 __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ edges,
-                        const uint32_t *__restrict__ ucore, uint32_t *parent) {
+                        const uint32_t *__restrict__ ucore, uint32_t *parent,
+                        uint32_t *__restrict__ deg) {
     const uint32_t ne = edge_slots(ctr, cap);
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
         const uint2 ed = edges[e];
-        if (ed.x == kNone || !ucore[ed.x] || !ucore[ed.y]) continue;
+        if (ed.x == kNone) continue;
+        const uint32_t cx = ucore[ed.x], cy = ucore[ed.y];
+        if (cx != cy) { atomicAdd(&deg[cx ? ed.y : ed.x], 1u); continue; }
+        if (!cx) continue;
         uint32_t a = ed.x, b = ed.y;
         uint32_t it = 0;
         for (; it < kSpinCap; ++it) {
@@ -132,7 +139,8 @@ __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ e
     }
 }
 
-// border rule: a non-core unique joins its minimum-index core neighbour
+// border rule: a non-core unique joins its minimum-index core neighbour (its
+// CSR row holds exactly its core neighbours)
 __global__ void k_border(const Counters *__restrict__ ctr, const uint32_t *__restrict__ off,
                          const uint32_t *__restrict__ adj, const uint32_t *__restrict__ ucore,
                          uint32_t *__restrict__ bmin) {
@@ -141,10 +149,7 @@ __global__ void k_border(const Counters *__restrict__ ctr, const uint32_t *__res
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
         if (ucore[u]) continue;
         uint32_t best = kNone;
-        for (uint32_t k = off[u]; k < off[u + 1]; ++k) {
-            const uint32_t w = adj[k];
-            if (ucore[w] && w < best) best = w;
-        }
+        for (uint32_t k = off[u]; k < off[u + 1]; ++k) best = min(best, adj[k]);
         bmin[u] = best;
     }
 }
@@ -257,11 +262,12 @@ void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s) {
     cudaMemsetAsync(B.deg, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
     cudaMemsetAsync(B.gcur, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
     k_graph_init<<<gu, kThreads, 0, s>>>(B.ctr, B.ucopies, B.cnt, B.parent, B.bmin);
-    k_degree<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucopies, B.deg, B.cnt);
-    scan_u32(B.deg, B.goff, P.N + 1, nullptr, nullptr, B.scan_part, B.scan_part_cap, s);
-    k_fill_adj<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.goff, B.gcur, B.adj);
+    k_count<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucopies, B.cnt);
     k_core<<<gu, kThreads, 0, s>>>(B.ctr, B.ctr, B.cnt, P.min_pts, B.ucore);
-    k_union<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.parent);
+    // unions, and the degrees of the border CSR (count / scan / fill)
+    k_union<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.parent, B.deg);
+    scan_u32(B.deg, B.goff, P.N + 1, nullptr, nullptr, B.scan_part, B.scan_part_cap, s);
+    k_fill_adj<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.goff, B.gcur, B.adj);
     k_border<<<gu, kThreads, 0, s>>>(B.ctr, B.goff, B.adj, B.ucore, B.bmin);
     if (trees) {
         cudaMemsetAsync(B.depth_hist, 0, sizeof(uint32_t) * (kDepthMax + 1), s);

@@ -73,20 +73,37 @@ __global__ void k_features(const Counters *__restrict__ ctr, const BinPair *__re
     }
 }
 
-// BF16 inference over the bin pairs of a call: pred[i] = 2^mlp(features)
+// Bin pairs below kLearnMinPairs are cheap whatever their order: they take the
+// lightest class without running the network; the others are listed for it.
+__global__ void k_mlp_select(Counters *ctr, const BinPair *__restrict__ bp,
+                             float *__restrict__ pred, uint32_t *__restrict__ heavy) {
+    const uint32_t n = ctr->n_binpairs;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n; i0 += stride) {
+        const uint32_t i = i0 + (threadIdx.x & 31);
+        const bool big = i < n && bp[i].cost_lo >= kLearnMinPairs;
+        if (i < n && !big) pred[i] = 1.0f;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, big);
+        uint32_t b0 = 0;
+        if ((threadIdx.x & 31) == 0 && m) b0 = atomicAdd(&ctr->n_heavy, (uint32_t)__popc(m));
+        b0 = __shfl_sync(0xFFFFFFFFu, b0, 0);
+        if (big) heavy[b0 + __popc(m & ((1u << (threadIdx.x & 31)) - 1u))] = i;
+    }
+}
+
+// BF16 inference over the listed bin pairs: pred[i] = 2^mlp(features)
 __global__ void __launch_bounds__(kThreads)
 k_mlp_predict_bf16(const Counters *__restrict__ ctr, const BinPair *__restrict__ bp,
-                   const __nv_bfloat16 *__restrict__ wq, float *__restrict__ pred) {
+                   const uint32_t *__restrict__ heavy, const __nv_bfloat16 *__restrict__ wq,
+                   float *__restrict__ pred) {
     __shared__ __nv_bfloat16 w[kMlpParams];
     for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) w[k] = wq[k];
     __syncthreads();
-    const uint32_t n = ctr->n_binpairs;
+    const uint32_t n = ctr->n_heavy;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    for (uint32_t k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += stride) {
+        const uint32_t i = heavy[k0];
         const BinPair P = bp[i];
-        // bin pairs below kLearnMinPairs are cheap whatever their order: they take
-        // the lightest class without running the network
-        if (P.cost_lo < kLearnMinPairs) { pred[i] = 1.0f; continue; }
         float f[kIn];
         binpair_features(P, f);
         __nv_bfloat16 x[kIn];
@@ -255,10 +272,14 @@ void launch_features(const Buffers &B, uint32_t cap, float *feats, cudaStream_t 
     k_features<<<grid > 0 ? grid : 1, kThreads, 0, s>>>(B.ctr, B.bp_sorted, feats);
 }
 
+// The heavy list lives in bp_small, which the schedule fills only afterwards.
 void launch_mlp_predict(const Buffers &B, uint32_t cap, const void *wq_bf16, cudaStream_t s) {
-    const int grid = (int)std::min<uint64_t>((cap + kThreads - 1) / kThreads, (uint64_t)sm_count() * 4);
+    cudaMemsetAsync(&B.ctr->n_heavy, 0, sizeof(uint32_t), s);
+    const int gsel = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sm_count() * 8);
+    k_mlp_select<<<gsel > 0 ? gsel : 1, 256, 0, s>>>(B.ctr, B.bp, B.pred, B.bp_small);
+    const int grid = (int)std::min<uint64_t>((cap + kThreads - 1) / kThreads, (uint64_t)sm_count() * 2);
     k_mlp_predict_bf16<<<grid > 0 ? grid : 1, kThreads, 0, s>>>(
-        B.ctr, B.bp, static_cast<const __nv_bfloat16 *>(wq_bf16), B.pred);
+        B.ctr, B.bp, B.bp_small, static_cast<const __nv_bfloat16 *>(wq_bf16), B.pred);
 }
 
 void launch_mlp_grad(const float *X, const float *T, uint32_t n, const float *p, float scale,
