@@ -179,6 +179,13 @@ def run_cpu(w, seconds: float, threads: int):
                 rows=sub.n, reps=len(pick), pairs=r.admissible_pairs)
 
 
+def workload_name(w):
+    eps = (f"eps={w.abs_eps}" if w.threshold != w.threshold else
+           f"threshold={w.threshold:g}" + (f" capped at {w.abs_eps}" if w.abs_eps >= 0 else ""))
+    return (f"{w.name}: {w.n_rep} repertoire(s), {w.n} rows, "
+            f"{'Hamming' if w.use_hamming else 'Levenshtein'} {eps}, minPts={w.min_pts}")
+
+
 def reference_arm(args, world, rank, w):
     if rank != 0:
         return
@@ -199,9 +206,9 @@ def reference_arm(args, world, rank, w):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u8",
         "data": "synthetic (seeded generator)",
-        "config": {"workload": f"{w.name}: {w.n_rep} aa repertoires, {w.n} rows",
-                   "global_batch": w.n, "seq_len": int(w.lengths().max()),
-                   "parallelism": "replicas only"},
+        "config": {"workload": workload_name(w), "global_batch": w.n * world,
+                   "seq_len": int(w.lengths().max()),
+                   "parallelism": f"host CPU, {threads} threads (rank 0)"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -324,9 +331,7 @@ def main():
            "warmup": args.warmup, "ms_per_step": step_ms, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "u8",
            "data": "synthetic (seeded generator, no public dataset)",
-           "config": {"workload": f"{w.name}: {w.n_rep} aa repertoires, {n} rows, "
-                                  f"{'Hamming' if w.use_hamming else 'Levenshtein'} "
-                                  f"eps={w.abs_eps}, minPts={w.min_pts}",
+           "config": {"workload": workload_name(w),
                       "global_batch": n * world, "seq_len": int(w.lengths().max()),
                       "parallelism": "replicas only" if world > 1 else "single GPU",
                       "l2": "inputs and working set larger than L2 (129 MB)",

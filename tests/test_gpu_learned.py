@@ -45,6 +45,23 @@ def test_profile_train_and_learned_partitions(gpu_ctx):
     assert np.array_equal(got.copies, base.copies)
 
 
+def test_network_predicts_better_than_static_cost(gpu_ctx):
+    """What the trained network gains over the static schedule's cost model:
+    on a profile of a workload it was not trained on, its error in log2 device
+    cycles per bin pair is below that of the best straight line from log2(pairs)
+    (fitted on that very profile, which favours the static model)."""
+    wa = synth.workload(2, scale=0.03, seed=11)
+    wb = synth.workload(2, scale=0.03, seed=12)
+    Xa, Ta = learned.profile(wa, gpu_ctx)
+    Xb, Tb = learned.profile(wb, gpu_ctx)
+    p, _ = learned.train(Xa, Ta, gpu_ctx, epochs=300)
+    mse_net = float(np.mean((learned.forward(p, Xb) - Tb) ** 2))
+    A = np.stack([Xb[:, 6].astype(np.float64), np.ones(len(Tb))], 1)
+    coef = np.linalg.lstsq(A, Tb.astype(np.float64), rcond=None)[0]
+    mse_static = float(np.mean((A @ coef - Tb) ** 2))
+    assert mse_net < mse_static, (mse_net, mse_static)
+
+
 @pytest.mark.parametrize("k,scale", [(2, 0.004), (3, 0.004)])
 def test_autotune_shapes_agree(gpu_ctx, tmp_path, k, scale):
     w = synth.workload(k, scale=scale)
