@@ -52,6 +52,35 @@ struct GeneMatcher {
     uint32_t long_names = 0;     // a name longer than 255 bytes exists
 };
 
+#ifdef __CUDACC__
+// Sequential reader of a byte string in global memory, 4 bytes per step.  It
+// loads only the aligned 4-byte words that hold bytes of the string (so no load
+// leaves the string's pages) and joins neighbours with a funnel shift; bytes
+// past the end of the string read as 0.
+struct GlobalReader {
+    const uint32_t *gw;
+    uint32_t t, last, sh, prev, rem;
+    __device__ __forceinline__ GlobalReader(const uint8_t *p, uint32_t len) {
+        const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+        sh = (uint32_t)(a & 3u);
+        gw = reinterpret_cast<const uint32_t *>(a - sh);
+        last = len ? (sh + len - 1) >> 2 : 0u;
+        t = 0;
+        rem = len;
+        prev = len ? __ldg(gw) : 0u;
+    }
+    __device__ __forceinline__ uint32_t next() {
+        const uint32_t nx = t + 1 <= last ? __ldg(gw + t + 1) : 0u;
+        uint32_t out = __funnelshift_r(prev, nx, 8 * sh);
+        if (rem < 4) out &= (1u << (8 * rem)) - 1u;
+        rem = rem < 4 ? 0u : rem - 4;
+        prev = nx;
+        ++t;
+        return out;
+    }
+};
+#endif
+
 // Device-resident counters of one clustering call (one struct, zeroed first).
 struct Counters {
     uint32_t lmax, lmin;

@@ -190,13 +190,20 @@ k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                 for (int p = 0; p < 5; ++p)
 #pragma unroll
                     for (int w = 0; w < 4; ++w) wd[p][w] = 0;
+                // residues read 4 at a time; positions past L keep code 0 (padding)
+                GlobalReader rd(s, L);
 #pragma unroll
                 for (int w = 0; w < 4; ++w) {
-                    const uint32_t i0 = 32u * w, i1 = min(L, i0 + 32u);
-                    for (uint32_t i = i0; i < i1; ++i) {
-                        const uint32_t c = cm[s[i]];
+                    for (uint32_t k = 0; k < 8; ++k) {
+                        const uint32_t i0 = 32u * w + 4u * k;
+                        if (i0 >= L) break;
+                        const uint32_t v = rd.next();
 #pragma unroll
-                        for (int p = 0; p < 5; ++p) wd[p][w] |= ((c >> p) & 1u) << (i - i0);
+                        for (int b = 0; b < 4; ++b) {
+                            const uint32_t c = i0 + b < L ? (uint32_t)cm[(v >> (8 * b)) & 0xFFu] : 0u;
+#pragma unroll
+                            for (int p = 0; p < 5; ++p) wd[p][w] |= ((c >> p) & 1u) << (4 * k + b);
+                        }
                     }
                 }
                 // layout: word p*W + w
@@ -216,16 +223,18 @@ k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
 #pragma unroll
                 for (int q = 0; q < NR; ++q) rec[q] = make_uint4(flat[4 * q], flat[4 * q + 1], flat[4 * q + 2], flat[4 * q + 3]);
             } else {
+                GlobalReader rd(s, L);
 #pragma unroll
                 for (int q = 0; q < NR; ++q) {
                     uint32_t wv[4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
+                        const uint32_t i0 = q * 16 + e * 4;
+                        const uint32_t v = i0 < L ? rd.next() : 0u;
                         uint32_t acc = 0;
 #pragma unroll
                         for (int t = 0; t < 4; ++t) {
-                            const uint32_t i = q * 16 + e * 4 + t;
-                            const uint32_t c = i < L ? cm[s[i]] : 0u;
+                            const uint32_t c = i0 + t < L ? (uint32_t)cm[(v >> (8 * t)) & 0xFFu] : 0u;
                             acc |= c << (8 * t);
                         }
                         wv[e] = acc;

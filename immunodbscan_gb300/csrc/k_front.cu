@@ -359,10 +359,21 @@ size_t gene_bits_smem(uint32_t G, uint32_t GW, uint32_t ts, uint32_t name_bytes)
            kGbWarps * ((gb_slice_bytes(GW) + 15) / 16 * 16);
 }
 
-// Four staged bytes from byte offset q of a warp's slice (q + 8 <= slice size).
-__device__ __forceinline__ uint32_t staged_word(const uint32_t *words, uint32_t q) {
-    return __funnelshift_r(words[q >> 2], words[(q >> 2) + 1], 8 * (q & 3));
-}
+// Sequential reader of a staged call: aligned 4-byte shared-memory loads
+// joined by a funnel shift, 4 call bytes per step (bytes past the call are
+// whatever the slice holds there: callers mask them).
+struct StagedReader {
+    const uint32_t *w;
+    uint32_t idx, sh, prev;
+    __device__ __forceinline__ StagedReader(const uint32_t *words, uint32_t q)
+        : w(words), idx(q >> 2), sh(8 * (q & 3)), prev(words[q >> 2]) {}
+    __device__ __forceinline__ uint32_t next() {
+        const uint32_t cur = w[++idx];
+        const uint32_t out = __funnelshift_r(prev, cur, sh);
+        prev = cur;
+        return out;
+    }
+};
 
 // Mask of the first n (0..4) bytes of a word.
 __device__ __forceinline__ uint32_t byte_mask(uint32_t n) {
@@ -370,23 +381,24 @@ __device__ __forceinline__ uint32_t byte_mask(uint32_t n) {
 }
 
 // Byte equality of a call in global memory with the staged bytes at offset q0.
-// Reads the aligned 4-byte words that hold the call's bytes (each holds at least
-// one of them, so no read leaves the call's pages); independent loads, no early
-// exit.
+// Reads only the aligned 4-byte words that hold the call's bytes (so no read
+// leaves the call's pages), joined by a funnel shift; no early exit.
 __device__ __forceinline__ bool bytes_equal_global(const uint8_t *g, const uint32_t *words,
                                                    uint32_t q0, uint32_t len) {
     if (len == 0) return true;
     const uintptr_t a = reinterpret_cast<uintptr_t>(g);
     const uint32_t sh = (uint32_t)(a & 3u);
     const uint32_t *gw = reinterpret_cast<const uint32_t *>(a - sh);
-    const uint32_t nwords = (sh + len + 3) >> 2;
-    // word 0 holds bytes [0, 4 - sh) of the call in its upper bytes
-    uint32_t diff = (__ldg(gw) >> (8 * sh)) ^ staged_word(words, q0);
-    diff &= byte_mask(min(4u - sh, len));
-#pragma unroll 4
-    for (uint32_t t = 1; t < nwords; ++t) {
-        const uint32_t k = 4 * t - sh;                 // call byte at the word's start
-        diff |= (__ldg(gw + t) ^ staged_word(words, q0 + k)) & byte_mask(len - k);
+    const uint32_t last = (sh + len - 1) >> 2;       // last word holding a call byte
+    StagedReader rd(words, q0);
+    uint32_t gprev = __ldg(gw);
+    uint32_t diff = 0;
+    for (uint32_t k = 0; k < len; k += 4) {
+        const uint32_t t = k >> 2;
+        const uint32_t gnext = t + 1 <= last ? __ldg(gw + t + 1) : 0u;
+        const uint32_t gv = __funnelshift_r(gprev, gnext, 8 * sh);
+        gprev = gnext;
+        diff |= (gv ^ rd.next()) & byte_mask(len - k);
     }
     return diff == 0;
 }
@@ -394,22 +406,25 @@ __device__ __forceinline__ bool bytes_equal_global(const uint8_t *g, const uint3
 // Equality of two staged calls of equal length.
 __device__ __forceinline__ bool staged_equal(const uint32_t *words, uint32_t qa, uint32_t qb,
                                              uint32_t len) {
+    StagedReader ra(words, qa), rb(words, qb);
     uint32_t diff = 0;
-    for (uint32_t k = 0; k < len; k += 4)
-        diff |= (staged_word(words, qa + k) ^ staged_word(words, qb + k)) & byte_mask(len - k);
+    for (uint32_t k = 0; k < len; k += 4) diff |= (ra.next() ^ rb.next()) & byte_mask(len - k);
     return diff == 0;
 }
 
-// String hash of a staged call (64-bit; equality is then checked byte by byte).
+// String hash of a staged call: two 32-bit multiplicative lanes over 4-byte
+// words, finished by mix64 (equality is then checked byte by byte).
 __device__ __forceinline__ unsigned long long call_hash(const uint32_t *words, uint32_t q0,
                                                         uint32_t len) {
-    unsigned long long h = 0x9E3779B97F4A7C15ull ^ len;
-    for (uint32_t k = 0; k < len; k += 8) {
-        const uint32_t lo = staged_word(words, q0 + k) & byte_mask(len - k);
-        const uint32_t hi = k + 4 < len ? staged_word(words, q0 + k + 4) & byte_mask(len - k - 4) : 0u;
-        h = mix64(h, ((unsigned long long)hi << 32) | lo);
+    StagedReader rd(words, q0);
+    uint32_t h1 = 0x811C9DC5u ^ len, h2 = 0x2545F491u + len;
+    for (uint32_t k = 0; k < len; k += 4) {
+        const uint32_t v = rd.next() & byte_mask(len - k);
+        h1 = (h1 ^ v) * 0x01000193u;
+        h2 = (h2 + v) * 0x9E3779B1u;
+        h2 ^= h2 >> 15;
     }
-    return h;
+    return mix64(((unsigned long long)h1 << 32) | h2, len);
 }
 
 // Collapse of a call column by string: ref[row] = slot of the row's string, or
@@ -549,29 +564,35 @@ __device__ bool rows_equal(const DedupArgs &a, uint32_t x, uint32_t y, uint32_t 
     uint64_t d = 0;
     for (uint32_t w = 0; w < a.VW; ++w) d |= a.vbits[(size_t)x * a.VW + w] ^ a.vbits[(size_t)y * a.VW + w];
     for (uint32_t w = 0; w < a.JW; ++w) d |= a.jbits[(size_t)x * a.JW + w] ^ a.jbits[(size_t)y * a.JW + w];
-    const uint8_t *px = a.seq + ox, *py = a.seq + oy;
+    GlobalReader rx_(a.seq + ox, lx), ry_(a.seq + oy, lx);
     uint32_t db = 0;
-#pragma unroll 8
-    for (uint32_t k = 0; k < lx; ++k) db |= px[k] ^ py[k];
+    for (uint32_t k = 0; k < lx; k += 4) db |= rx_.next() ^ ry_.next();   // past the end: 0 ^ 0
     return d == 0 && db == 0;
 }
 
+constexpr uint32_t kRepSmem = 2048;   // repertoire offsets kept in shared memory
+
 __global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
+    __shared__ uint32_t s_rep[kRepSmem + 1];
+    const bool rep_smem = a.R + 1 <= kRepSmem + 1;
+    if (rep_smem)
+        for (uint32_t k = threadIdx.x; k <= a.R; k += blockDim.x) s_rep[k] = a.rep_off[k];
+    __syncthreads();
+    const uint32_t *rep_off = rep_smem ? s_rep : a.rep_off;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += stride) {
-        const uint32_t r = rep_of_row(a.rep_off, a.R, i);
+        const uint32_t r = rep_of_row(rep_off, a.R, i);
         const int64_t o = a.off[i];
         const uint32_t L = (uint32_t)(a.off[i + 1] - o);
         uint64_t h = mix64(0x1234567ull + r, L);
         for (uint32_t w = 0; w < a.VW; ++w) h = mix64(h, a.vbits[(size_t)i * a.VW + w]);
         for (uint32_t w = 0; w < a.JW; ++w) h = mix64(h, a.jbits[(size_t)i * a.JW + w]);
-        const uint8_t *p = a.seq + o;
-        uint64_t word = 0;
-        for (uint32_t k = 0; k < L; ++k) {
-            word = (word << 8) | p[k];
-            if ((k & 7) == 7) { h = mix64(h, word); word = 0; }
+        GlobalReader rd(a.seq + o, L);
+        for (uint32_t k = 0; k < L; k += 8) {
+            const uint32_t lo = rd.next();
+            const uint32_t hi = k + 4 < L ? rd.next() : 0u;
+            h = mix64(h, ((uint64_t)hi << 32) | lo);
         }
-        h = mix64(h, word);
         uint64_t s = h & a.mask;
         uint32_t it = 0;
         for (;; ++it) {
