@@ -179,6 +179,14 @@ def run_cpu(w, seconds: float, threads: int):
                 rows=sub.n, reps=len(pick), pairs=r.admissible_pairs)
 
 
+def measured_hbm_peak() -> float:
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"])
+    except (OSError, ValueError, KeyError):
+        return 6800.0
+
+
 def workload_name(w):
     eps = (f"eps={w.abs_eps}" if w.threshold != w.threshold else
            f"threshold={w.threshold:g}" + (f" capped at {w.abs_eps}" if w.abs_eps >= 0 else ""))
@@ -386,6 +394,31 @@ def main():
                        "work_units": int(last.pairs_evaluated if w.use_hamming else last.lev_columns),
                        "kernel_ms": t_dist * 1e3,
                        "peak_source": "measured: idb_diag_int_peak (lop3/add chains, all SMs)"}
+
+    # graph / union-find / border / renumber phases against HBM bandwidth: the
+    # algorithmic bytes 8(n_u+1) CSR offsets + 4 n_u counts + 8 E adjacency + 8 E_cc
+    # parent loads + n_u core flags + 12 n_u parent init/compress + 8 N labels
+    n_u, E, E_cc = int(last.n_uniques), int(last.neighbour_pairs), int(last.core_edges)
+    graph_bytes = 8 * (n_u + 1) + 4 * n_u + 8 * E + 8 * E_cc + n_u + 12 * n_u + 8 * n
+    graph_ms = float(np.mean([p[3] for p in r["phases"]]))
+    hbm_peak = measured_hbm_peak()
+    out["roofline_graph"] = {"bound": "hbm", "achieved": graph_bytes / (graph_ms * 1e-3) / 1e9,
+                             "peak": hbm_peak, "unit": "GB/s",
+                             "frac": graph_bytes / (graph_ms * 1e-3) / 1e9 / hbm_peak,
+                             "traffic": None, "phase_ms": graph_ms, "bytes": graph_bytes,
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)"}
+    # the reference's own work on the same data: every unique pair of a table, plus
+    # the second sweep over cores x uniques (each repertoire is one table there)
+    rep_id = np.searchsorted(w.rep_off, np.arange(n), side="right") - 1
+    is_rep = copies_b > 0
+    nu_r = np.bincount(rep_id[is_rep], minlength=w.n_rep).astype(np.float64)
+    nc_r = np.bincount(rep_id[is_rep & (core_b > 0)], minlength=w.n_rep).astype(np.float64)
+    ref_pairs = float(np.sum(nu_r * (nu_r - 1) / 2 + nc_r * nu_r))
+    out["reference_equivalent"] = {
+        "pairs": ref_pairs, "unit": "Gpair-distances/s",
+        "value": world * ref_pairs / (step_ms * 1e-3) / 1e9,
+        "definition": "sum over repertoires of n_u(n_u-1)/2 + n_cores*n_u (the reference's "
+                      "all-pairs core sweep plus its core x unique growth sweep)"}
 
     # e2e through idb_cluster (the InterlinkClass replacement) with pinned host buffers
     if not args.no_e2e:

@@ -54,7 +54,7 @@ class Stats(C.Structure):
                 ("n_noise_rows", C.c_uint32), ("pairs_evaluated", C.c_uint64),
                 ("neighbour_pairs", C.c_uint64), ("n_entries", C.c_uint64), ("n_units", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_distance", C.c_double), ("ms_phase", C.c_double * 8),
-                ("kernel_launches", C.c_uint32), ("reserved", C.c_uint32),
+                ("kernel_launches", C.c_uint32), ("core_edges", C.c_uint32),
                 ("lev_columns", C.c_uint64)]
 
 

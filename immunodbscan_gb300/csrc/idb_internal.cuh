@@ -104,7 +104,7 @@ struct Counters {
     uint32_t n_small;            // small bin pairs handed to the pair-parallel path
     uint32_t small_cursor;       // their work queue head
     uint32_t n_heavy;            // bin pairs the learned predictor evaluates
-    uint32_t pad[1];
+    uint32_t n_core_edges;       // neighbour pairs with both ends core
 };
 
 // One bucket ("bin") holds the uniques of one (repertoire, V gene, J gene,

@@ -396,7 +396,9 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
     const bool neg = EM == 0 && U.P.eps < 0;       // no pair can be a neighbour
     const uint32_t same = U.P.same;
     const uint32_t yrow0 = (same ? U.P.a_start : U.P.b_start) + U.ybase;
-    for (uint32_t yb = 0; yb < U.ny && !neg; yb += kYB) {
+    // same bin: y-entries at or before the first x-entry pair with nothing
+    const uint32_t y0 = (same && U.xbase >= U.ybase) ? min(U.ny, U.xbase - U.ybase + 1) : 0u;
+    for (uint32_t yb = y0; yb < U.ny && !neg; yb += kYB) {
         const uint32_t nb = min((uint32_t)kYB, U.ny - yb);
         const uint4 *src = a.rec + (size_t)(yrow0 + yb) * R16;
         for (uint32_t t = lane; t < nb * R16; t += 32) sy[t] = __ldg(src + t);
@@ -450,10 +452,22 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
 #pragma unroll
             for (int r = 1; r < RX; ++r) z = min(z, sc[r]);
             if (z <= thr) {
+                // with exact signatures a hit outside its canonical bin is dropped
+                // here: sig_x & sig_y must be empty
+                const uint4 ym = sym[t];
                 uint32_t hit = 0;
 #pragma unroll
-                for (int r = 0; r < RX; ++r) hit |= (uint32_t)(sc[r] <= thr) << r;
-                shq[qn++ * 32 + lane] = (t << 8) | (hit & valid);
+                for (int r = 0; r < RX; ++r)
+                    if (sc[r] <= thr) {
+                        bool ok = true;
+                        if (a.sig_exact) {
+                            const uint4 m = sxm[32 * r + lane];
+                            ok = ((m.x & ym.x) | (m.y & ym.y) | (m.z & ym.z)) == 0;
+                        }
+                        hit |= (uint32_t)ok << r;
+                    }
+                hit &= valid;
+                if (hit) shq[qn++ * 32 + lane] = (t << 8) | hit;
             }
             if (__any_sync(0xFFFFFFFFu, qn == kHitQ)) {
                 __syncwarp();

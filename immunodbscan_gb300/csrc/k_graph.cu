@@ -118,12 +118,14 @@ __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ e
                         uint32_t *__restrict__ deg) {
     const uint32_t ne = edge_slots(ctr, cap);
     const uint32_t stride = gridDim.x * blockDim.x;
+    uint32_t n_cc = 0;
     for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
         const uint2 ed = edges[e];
         if (ed.x == kNone) continue;
         const uint32_t cx = ucore[ed.x], cy = ucore[ed.y];
         if (cx != cy) { atomicAdd(&deg[cx ? ed.y : ed.x], 1u); continue; }
         if (!cx) continue;
+        ++n_cc;
         uint32_t a = ed.x, b = ed.y;
         uint32_t it = 0;
         for (; it < kSpinCap; ++it) {
@@ -137,6 +139,9 @@ __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ e
         }
         if (it == kSpinCap) atomicOr(&ctr->error, kErrUnionStall);
     }
+#pragma unroll
+    for (int d = 16; d > 0; d >>= 1) n_cc += __shfl_xor_sync(0xFFFFFFFFu, n_cc, d);
+    if ((threadIdx.x & 31) == 0 && n_cc) atomicAdd(&ctr->n_core_edges, n_cc);
 }
 
 // border rule: a non-core unique joins its minimum-index core neighbour (its

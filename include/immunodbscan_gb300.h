@@ -104,7 +104,7 @@ typedef struct idb_stats {
                                   outputs (device time; eager calls include waits
                                   on host read-backs)                              */
     uint32_t kernel_launches;  /* kernels launched (graph replays)                 */
-    uint32_t reserved;
+    uint32_t core_edges;       /* neighbour pairs with both ends core              */
     uint64_t lev_columns;      /* text columns consumed by live Levenshtein pairs  */
 } idb_stats;
 
