@@ -179,6 +179,28 @@ def run_cpu(w, seconds: float, threads: int):
                 rows=sub.n, reps=len(pick), pairs=r.admissible_pairs)
 
 
+def profiled_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` on `workload` from the committed ncu
+    summary (a line 'traffic_bytes_per_launch <kernel> <workload> <bytes>'), or
+    None when no capture of that pair is committed."""
+    d = os.path.join(ROOT, "profiles")
+    try:
+        names = sorted(os.listdir(d))
+    except OSError:
+        return None
+    for nm in names:
+        try:
+            with open(os.path.join(d, nm)) as f:
+                for line in f:
+                    p = line.split()
+                    if len(p) == 4 and p[0] == "traffic_bytes_per_launch" and p[1] == kernel \
+                            and p[2] == workload:
+                        return int(p[3])
+        except OSError:
+            continue
+    return None
+
+
 def measured_hbm_peak() -> float:
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -388,7 +410,11 @@ def main():
     out["roofline"] = {"bound": "int", "achieved": achieved, "peak": gops.value,
                        "unit": "Gop/s (32-bit integer logic)",
                        "frac": achieved / gops.value if gops.value else None,
-                       "traffic": None, "kernel": "k_hamming" if w.use_hamming else "k_levenshtein",
+                       "traffic": (profiled_traffic("k_hamming", w.name)
+                                   if w.use_hamming and args.scale == 1.0 else None),
+                       "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
+                                         "full-size launch (profiles/)",
+                       "kernel": "k_hamming" if w.use_hamming else "k_levenshtein",
                        "ops_per_unit": ops_pair,
                        "work_unit": "pair" if w.use_hamming else "pair-column (text residue)",
                        "work_units": int(last.pairs_evaluated if w.use_hamming else last.lev_columns),
