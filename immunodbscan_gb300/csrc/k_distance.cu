@@ -556,10 +556,11 @@ k_levenshtein(DistArgs a) {
     const uint32_t peq_words = RX * A * W * 32;          // per warp
     const uint32_t ybuf_words = kYB * a.rs16 * 4;        // per warp
     const uint32_t meta_words = (kYB + 32 * RX) * 4;     // per warp
-    uint32_t *peq = smem + wid * (peq_words + ybuf_words + meta_words);
+    uint32_t *peq = smem + wid * (peq_words + ybuf_words + meta_words + kYB);
     uint4 *sy = reinterpret_cast<uint4 *>(peq + peq_words);
     uint4 *sym = sy + kYB * a.rs16;                      // y side records
     uint4 *sxm = sym + kYB;                              // x side records
+    uint32_t *spres = reinterpret_cast<uint32_t *>(sxm + 32 * RX);   // y residue sets
     const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
     EdgeWriter ew;
     ew.init();
@@ -570,6 +571,7 @@ k_levenshtein(DistArgs a) {
         const int dg = n - m;
         uint32_t xpos[RX];
         bool xval[RX];
+        uint32_t xpres[RX];        // set of residue codes of each x-entry (A <= 32)
         // Peq[r][c][w][lane]
         for (uint32_t k = 0; k < (uint32_t)RX * A * W; ++k) peq[k * 32 + lane] = 0u;
         __syncwarp();
@@ -577,6 +579,7 @@ k_levenshtein(DistArgs a) {
         for (int r = 0; r < RX; ++r) {
             xpos[r] = U.xbase + r * 32 + lane;
             xval[r] = xpos[r] < U.xbase + U.nx;
+            xpres[r] = 0;
             sxm[r * 32 + lane] = __ldg(a.meta + U.P.a_start + (xval[r] ? xpos[r] : U.xbase));
             if (xval[r]) {
                 pairs += unit_pairs(U, xpos[r]);
@@ -585,9 +588,14 @@ k_levenshtein(DistArgs a) {
                 for (int i = 0; i < m; ++i) {
                     const uint32_t c = __ldg(codes + i);
                     peq[((r * A + c) * W + (i >> 5)) * 32 + lane] |= 1u << (i & 31);
+                    xpres[r] |= 1u << c;
                 }
             }
         }
+        // An edit changes the set of residues present by at most two (a
+        // substitution drops one and adds one, an indel one), so a pair whose
+        // sets differ in more than 2*eps residues is not within eps.
+        const int pres_max = 2 * eps;
         __syncwarp();
         const uint32_t yrow0 = (U.P.same ? U.P.a_start : U.P.b_start) + U.ybase;
         for (uint32_t yb = 0; yb < U.ny; yb += kYB) {
@@ -596,14 +604,23 @@ k_levenshtein(DistArgs a) {
             for (uint32_t t = lane; t < nb * a.rs16; t += 32) sy[t] = __ldg(src + t);
             for (uint32_t t = lane; t < nb; t += 32) sym[t] = __ldg(a.meta + yrow0 + yb + t);
             __syncwarp();
+            for (uint32_t t = lane; t < nb; t += 32) {
+                const uint8_t *yc = reinterpret_cast<const uint8_t *>(sy + t * a.rs16);
+                uint32_t pr = 0;
+                for (int j = 0; j < n; ++j) pr |= 1u << yc[j];
+                spres[t] = pr;
+            }
+            __syncwarp();
             for (uint32_t t = 0; t < nb; ++t) {
                 const uint32_t ypos = U.ybase + yb + t;
                 const uint8_t *yc = reinterpret_cast<const uint8_t *>(sy + t * a.rs16);
+                const uint32_t ypres = spres[t];
                 uint32_t Pv[RX][W], Mv[RX][W];
                 bool alive[RX];
 #pragma unroll
                 for (int r = 0; r < RX; ++r) {
-                    alive[r] = xval[r] && !(U.P.same && ypos <= xpos[r]);
+                    alive[r] = xval[r] && !(U.P.same && ypos <= xpos[r]) &&
+                               __popc(xpres[r] ^ ypres) <= pres_max;
 #pragma unroll
                     for (int w = 0; w < W; ++w) { Pv[r][w] = 0xFFFFFFFFu; Mv[r][w] = 0u; }
                 }
@@ -877,7 +894,7 @@ void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s) 
         return;
     }
     const size_t smem = (size_t)kWarps * ((size_t)P.RX * P.A * P.W * 32 * 4 + (size_t)kYB * P.RS +
-                                          16 * ((size_t)kYB + 32 * P.RX));
+                                          16 * ((size_t)kYB + 32 * P.RX) + 4 * (size_t)kYB);
     switch (P.W) {
         case 1: if (P.RX == 2) run(k_levenshtein<1, 2>, a, smem, grid, s); else run(k_levenshtein<1, 1>, a, smem, grid, s); break;
         case 2: run(k_levenshtein<2, 1>, a, smem, grid, s); break;
