@@ -556,11 +556,16 @@ k_levenshtein(DistArgs a) {
     const uint32_t peq_words = RX * A * W * 32;          // per warp
     const uint32_t ybuf_words = kYB * a.rs16 * 4;        // per warp
     const uint32_t meta_words = (kYB + 32 * RX) * 4;     // per warp
-    uint32_t *peq = smem + wid * (peq_words + ybuf_words + meta_words + kYB);
+    constexpr uint32_t kCW = 8;                          // count words: 4 codes each, A <= 32
+    uint32_t *peq = smem + wid * (peq_words + ybuf_words + meta_words + kYB +
+                                  kCW * (kYB + 32 * RX));
     uint4 *sy = reinterpret_cast<uint4 *>(peq + peq_words);
     uint4 *sym = sy + kYB * a.rs16;                      // y side records
     uint4 *sxm = sym + kYB;                              // x side records
     uint32_t *spres = reinterpret_cast<uint32_t *>(sxm + 32 * RX);   // y residue sets
+    uint32_t *sycnt = spres + kYB;                       // y residue counts [kYB][kCW]
+    uint32_t *sxcnt = sycnt + kCW * kYB;                 // x residue counts [RX][kCW][32]
+    const uint32_t cw = (A + 3) / 4;                     // count words in use
     const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
     EdgeWriter ew;
     ew.init();
@@ -574,6 +579,7 @@ k_levenshtein(DistArgs a) {
         uint32_t xpres[RX];        // set of residue codes of each x-entry (A <= 32)
         // Peq[r][c][w][lane]
         for (uint32_t k = 0; k < (uint32_t)RX * A * W; ++k) peq[k * 32 + lane] = 0u;
+        for (uint32_t k = 0; k < (uint32_t)RX * kCW; ++k) sxcnt[k * 32 + lane] = 0u;
         __syncwarp();
 #pragma unroll
         for (int r = 0; r < RX; ++r) {
@@ -589,12 +595,20 @@ k_levenshtein(DistArgs a) {
                     const uint32_t c = __ldg(codes + i);
                     peq[((r * A + c) * W + (i >> 5)) * 32 + lane] |= 1u << (i & 31);
                     xpres[r] |= 1u << c;
+                    sxcnt[(r * kCW + (c >> 2)) * 32 + lane] += 1u << (8 * (c & 3));
                 }
             }
         }
+        uint32_t xcnt[RX][kCW];    // residue counts, one byte per code (lengths < 256)
+#pragma unroll
+        for (int r = 0; r < RX; ++r)
+#pragma unroll
+            for (uint32_t k = 0; k < kCW; ++k) xcnt[r][k] = sxcnt[(r * kCW + k) * 32 + lane];
         // An edit changes the set of residues present by at most two (a
         // substitution drops one and adds one, an indel one), so a pair whose
-        // sets differ in more than 2*eps residues is not within eps.
+        // sets differ in more than 2*eps residues is not within eps.  Likewise
+        // an edit changes the residue counts by at most 2 in total (sum of
+        // absolute differences), so a pair with that sum above 2*eps is not.
         const int pres_max = 2 * eps;
         __syncwarp();
         const uint32_t yrow0 = (U.P.same ? U.P.a_start : U.P.b_start) + U.ybase;
@@ -606,8 +620,15 @@ k_levenshtein(DistArgs a) {
             __syncwarp();
             for (uint32_t t = lane; t < nb; t += 32) {
                 const uint8_t *yc = reinterpret_cast<const uint8_t *>(sy + t * a.rs16);
+                uint32_t *yk = sycnt + t * kCW;
+#pragma unroll
+                for (uint32_t k = 0; k < kCW; ++k) yk[k] = 0u;
                 uint32_t pr = 0;
-                for (int j = 0; j < n; ++j) pr |= 1u << yc[j];
+                for (int j = 0; j < n; ++j) {
+                    const uint32_t c = yc[j];
+                    pr |= 1u << c;
+                    yk[c >> 2] += 1u << (8 * (c & 3));
+                }
                 spres[t] = pr;
             }
             __syncwarp();
@@ -615,12 +636,21 @@ k_levenshtein(DistArgs a) {
                 const uint32_t ypos = U.ybase + yb + t;
                 const uint8_t *yc = reinterpret_cast<const uint8_t *>(sy + t * a.rs16);
                 const uint32_t ypres = spres[t];
+                uint32_t ycnt[kCW];
+#pragma unroll
+                for (uint32_t k = 0; k < kCW; ++k) ycnt[k] = k < cw ? sycnt[t * kCW + k] : 0u;
                 uint32_t Pv[RX][W], Mv[RX][W];
                 bool alive[RX];
 #pragma unroll
                 for (int r = 0; r < RX; ++r) {
                     alive[r] = xval[r] && !(U.P.same && ypos <= xpos[r]) &&
                                __popc(xpres[r] ^ ypres) <= pres_max;
+                    if (alive[r]) {
+                        uint32_t sad = 0;
+#pragma unroll
+                        for (uint32_t k = 0; k < kCW; ++k) sad = __vsadu4(xcnt[r][k], ycnt[k]) + sad;
+                        alive[r] = (int)sad <= pres_max;
+                    }
 #pragma unroll
                     for (int w = 0; w < W; ++w) { Pv[r][w] = 0xFFFFFFFFu; Mv[r][w] = 0u; }
                 }
@@ -894,7 +924,8 @@ void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s) 
         return;
     }
     const size_t smem = (size_t)kWarps * ((size_t)P.RX * P.A * P.W * 32 * 4 + (size_t)kYB * P.RS +
-                                          16 * ((size_t)kYB + 32 * P.RX) + 4 * (size_t)kYB);
+                                          16 * ((size_t)kYB + 32 * P.RX) + 4 * (size_t)kYB +
+                                          4 * 8 * ((size_t)kYB + 32 * P.RX));
     switch (P.W) {
         case 1: if (P.RX == 2) run(k_levenshtein<1, 2>, a, smem, grid, s); else run(k_levenshtein<1, 1>, a, smem, grid, s); break;
         case 2: run(k_levenshtein<2, 1>, a, smem, grid, s); break;
