@@ -364,6 +364,7 @@ __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew,
 // chunk, hit bits) in a small shared-memory queue; the queue is drained here when
 // a lane's queue is full or the chunk ends, with every lane taking part.
 constexpr int kHitQ = 8;   // queued (y, hits) records per lane
+constexpr uint32_t kLevQ = 256;          // queued candidate pairs per warp (Levenshtein)
 constexpr uint32_t kOff = 0x40000000u;   // score of a masked x-entry (never a hit)
 
 __device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, const uint32_t *q,
@@ -558,13 +559,14 @@ k_levenshtein(DistArgs a) {
     const uint32_t meta_words = (kYB + 32 * RX) * 4;     // per warp
     constexpr uint32_t kCW = 8;                          // count words: 4 codes each, A <= 32
     uint32_t *peq = smem + wid * (peq_words + ybuf_words + meta_words + kYB +
-                                  kCW * (kYB + 32 * RX));
+                                  kCW * (kYB + 32 * RX) + kLevQ);
     uint4 *sy = reinterpret_cast<uint4 *>(peq + peq_words);
     uint4 *sym = sy + kYB * a.rs16;                      // y side records
     uint4 *sxm = sym + kYB;                              // x side records
     uint32_t *spres = reinterpret_cast<uint32_t *>(sxm + 32 * RX);   // y residue sets
     uint32_t *sycnt = spres + kYB;                       // y residue counts [kYB][kCW]
     uint32_t *sxcnt = sycnt + kCW * kYB;                 // x residue counts [RX][kCW][32]
+    uint32_t *lq = sxcnt + kCW * 32 * RX;                // queued candidate pairs [kLevQ]
     const uint32_t cw = (A + 3) / 4;                     // count words in use
     const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
     EdgeWriter ew;
@@ -632,72 +634,86 @@ k_levenshtein(DistArgs a) {
                 spres[t] = pr;
             }
             __syncwarp();
+            // 1. filters: the pairs that survive go to a warp queue as
+            //    (owner lane, r, t), so the DP below runs with every lane busy
+            uint32_t qn = 0;
             for (uint32_t t = 0; t < nb; ++t) {
                 const uint32_t ypos = U.ybase + yb + t;
-                const uint8_t *yc = reinterpret_cast<const uint8_t *>(sy + t * a.rs16);
                 const uint32_t ypres = spres[t];
                 uint32_t ycnt[kCW];
 #pragma unroll
                 for (uint32_t k = 0; k < kCW; ++k) ycnt[k] = k < cw ? sycnt[t * kCW + k] : 0u;
-                uint32_t Pv[RX][W], Mv[RX][W];
-                bool alive[RX];
 #pragma unroll
                 for (int r = 0; r < RX; ++r) {
-                    alive[r] = xval[r] && !(U.P.same && ypos <= xpos[r]) &&
-                               __popc(xpres[r] ^ ypres) <= pres_max;
-                    if (alive[r]) {
+                    bool alive = xval[r] && !(U.P.same && ypos <= xpos[r]) &&
+                                 __popc(xpres[r] ^ ypres) <= pres_max;
+                    if (alive) {
                         uint32_t sad = 0;
 #pragma unroll
                         for (uint32_t k = 0; k < kCW; ++k) sad = __vsadu4(xcnt[r][k], ycnt[k]) + sad;
-                        alive[r] = (int)sad <= pres_max;
+                        alive = (int)sad <= pres_max;
                     }
-#pragma unroll
-                    for (int w = 0; w < W; ++w) { Pv[r][w] = 0xFFFFFFFFu; Mv[r][w] = 0u; }
+                    const uint32_t mk = __ballot_sync(0xFFFFFFFFu, alive);
+                    if (alive) lq[qn + __popc(mk & lanemask_lt())] = (uint32_t)lane | ((uint32_t)r << 5) | (t << 8);
+                    qn += __popc(mk);
                 }
-                bool any = false;
+                if (qn > kLevQ - 32 * RX || t + 1 == nb) {
+                    __syncwarp();
+                    // 2. bit-parallel DP of the queued pairs, 32 at a time
+                    for (uint32_t k0 = 0; k0 < qn; k0 += 32) {
+                        const bool has = k0 + lane < qn;
+                        const uint32_t it = has ? lq[k0 + lane] : 0u;
+                        const uint32_t owner = it & 31u, r = (it >> 5) & 7u, tt = it >> 8;
+                        const uint8_t *yc = reinterpret_cast<const uint8_t *>(sy + tt * a.rs16);
+                        uint32_t Pv[W], Mv[W];
 #pragma unroll
-                for (int r = 0; r < RX; ++r) any |= alive[r];
-                if (!__any_sync(0xFFFFFFFFu, any)) continue;
-                for (int j = 0; j < n; ++j) {
-                    const uint32_t c = yc[j];
+                        for (int w = 0; w < W; ++w) { Pv[w] = 0xFFFFFFFFu; Mv[w] = 0u; }
+                        bool live = has;
+                        for (int j = 0; j < n; ++j) {
+                            const uint32_t c = yc[j];
+                            const uint32_t *pe = peq + ((r * A + c) * W) * 32 + owner;
+                            if (W == 1) {
+                                myers_step1(Pv[0], Mv[0], pe[0]);
+                            } else {
+                                int h = 1;
 #pragma unroll
-                    for (int r = 0; r < RX; ++r) {
-                        const uint32_t *pe = peq + ((r * A + c) * W) * 32 + lane;
-                        if (W == 1) {
-                            myers_step1(Pv[r][0], Mv[r][0], pe[0]);
-                        } else {
-                            int h = 1;
-#pragma unroll
-                            for (int w = 0; w < W; ++w) h = myers_block(Pv[r][w], Mv[r][w], pe[w * 32], h);
-                        }
-                    }
-                    if ((j & 3) == 3) {
-                        const int col = j + 1;
-                        const int i = col - dg;
-                        if (i >= 0 && i <= m) {
-                            bool live = false;
-#pragma unroll
-                            for (int r = 0; r < RX; ++r) {
-                                if (alive[r] && myers_value<W>(Pv[r], Mv[r], i, col) > eps) {
-                                    alive[r] = false;
-                                    cols += (uint32_t)col;
-                                }
-                                live |= alive[r];
+                                for (int w = 0; w < W; ++w) h = myers_block(Pv[w], Mv[w], pe[w * 32], h);
                             }
-                            if (!__any_sync(0xFFFFFFFFu, live)) break;
+                            if ((j & 3) == 3) {
+                                const int col = j + 1;
+                                const int i = col - dg;
+                                if (i >= 0 && i <= m) {
+                                    if (live && myers_value<W>(Pv, Mv, i, col) > eps) {
+                                        live = false;
+                                        cols += (uint32_t)col;
+                                    }
+                                    if (!__any_sync(0xFFFFFFFFu, live)) break;
+                                }
+                            }
+                        }
+                        bool hit = false;
+                        if (live) {
+                            cols += (uint32_t)n;
+                            hit = myers_value<W>(Pv, Mv, m, n) <= eps;
+                        }
+                        if (__any_sync(0xFFFFFFFFu, hit)) {
+                            bool ok = hit;
+                            const uint4 mx = sxm[r * 32 + owner], my = sym[tt];
+                            if (ok) {
+                                if (a.sig_exact) {
+                                    ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
+                                } else {
+                                    const uint32_t rx = a.urow[mx.w], ry = a.urow[my.w];
+                                    ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)U.P.v &&
+                                         lowest_common(a.jbits, a.JW, rx, ry) == (int)U.P.j;
+                                }
+                            }
+                            ew.append(a, lane, ok, min(mx.w, my.w), max(mx.w, my.w));
                         }
                     }
+                    qn = 0;
+                    __syncwarp();
                 }
-                uint32_t hit = 0;
-#pragma unroll
-                for (int r = 0; r < RX; ++r)
-                    if (alive[r]) {
-                        cols += (uint32_t)n;
-                        if (myers_value<W>(Pv[r], Mv[r], m, n) <= eps) hit |= 1u << r;
-                    }
-                if (__any_sync(0xFFFFFFFFu, hit))
-                    emit_hits_meta(a, ew, hit, sxm, sym[t], U.xbase, ypos, U.P.same, U.P.v, U.P.j,
-                                   lane);
             }
             __syncwarp();
         }
@@ -925,7 +941,7 @@ void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s) 
     }
     const size_t smem = (size_t)kWarps * ((size_t)P.RX * P.A * P.W * 32 * 4 + (size_t)kYB * P.RS +
                                           16 * ((size_t)kYB + 32 * P.RX) + 4 * (size_t)kYB +
-                                          4 * 8 * ((size_t)kYB + 32 * P.RX));
+                                          4 * 8 * ((size_t)kYB + 32 * P.RX) + 4 * (size_t)kLevQ);
     switch (P.W) {
         case 1: if (P.RX == 2) run(k_levenshtein<1, 2>, a, smem, grid, s); else run(k_levenshtein<1, 1>, a, smem, grid, s); break;
         case 2: run(k_levenshtein<2, 1>, a, smem, grid, s); break;
