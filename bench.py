@@ -55,6 +55,9 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tile", default=None,
                     help="work-unit shape RX,TY (x-entries per lane, y-chunk); skips the autotuner")
+    ap.add_argument("--no-learned-w3", action="store_true",
+                    help="skip the learned-versus-static comparison on the learned-scheduling "
+                         "workload (workload 3, 500k rows)")
     ap.add_argument("--static-only", action="store_true",
                     help="time the static schedule only (no network is trained)")
     ap.add_argument("--cpu-seconds", type=float, default=None,
@@ -501,6 +504,14 @@ def main():
                         "identical_partitions": bool(same)}
         ctx_plain.close()
 
+    # the learned-scheduling workload: 2M-row-class repertoire with V/J usage
+    # Zipf(1.8) (bin sizes 1 .. 10^5), Levenshtein eps=2; trained on a profile of
+    # a differently seeded copy, timed against the static schedule
+    if learn and not args.no_learned_w3 and args.workload == 2:
+        out["learned_schedule_workload3"] = learned_vs_static(3, 0.25, max(3, args.steps // 4),
+                                                              args.warmup, world, local,
+                                                              args.mlp_epochs)
+
     if rank == 0 and not args.no_cpu:
         res = run_cpu(w, args.cpu_seconds or 10.0, os.cpu_count() or 1)
         out["cpu_baseline"] = {"value": res["value"], "unit": UNIT, "cores": os.cpu_count(),
@@ -512,6 +523,39 @@ def main():
         print(json.dumps(out), flush=True)
     for c in (ctx_setup, ctx_static, ctx_learned):
         c.close()
+
+
+def learned_vs_static(k, scale, steps, warmup, world, local, epochs):
+    """Static and learned schedules on workload k at `scale`: step times, the gain,
+    the network's prediction error next to the static cost model's, equality."""
+    from immunodbscan_gb300 import Context, DeviceBatch, learned, synth, tuning
+    w = synth.workload(k, scale=scale)
+    ctx_s, ctx_l = Context(local), Context(local)
+    try:
+        rec = tuning.measure(w, ctx_s)
+        shape = (rec["rx"], rec["ty"])
+        wt = synth.workload(k, scale=scale, seed=4242 + k)
+        X, T = learned.profile(wt, ctx_s, tune=shape)
+        params, loss = learned.train(X, T, ctx_s, epochs=epochs)
+        learned.install(ctx_l, params)
+        bs = DeviceBatch(w, ctx_s, schedule=0, tune=shape)
+        bs.plan()
+        rs = time_batch(bs, steps, warmup, world)
+        bl = DeviceBatch(w, ctx_l, schedule=1, tune=shape)
+        bl.plan()
+        rl = time_batch(bl, steps, warmup, world)
+        cs, ks, _ = bs.results()
+        cl, kl, _ = bl.results()
+        q = prediction_quality(w, ctx_s, shape, params)
+        return {"workload": workload_name(w), "tile": {"rx": shape[0], "ty": shape[1]},
+                "static_ms_per_step": rs["step_ms"], "learned_ms_per_step": rl["step_ms"],
+                "static_distance_ms": rs["ms_dist"], "learned_distance_ms": rl["ms_dist"],
+                "learned_gain": rs["step_ms"] / rl["step_ms"],
+                "identical_partitions": bool(np.array_equal(cs, cl) and np.array_equal(ks, kl)),
+                "train_binpairs": int(len(T)), **q}
+    finally:
+        ctx_s.close()
+        ctx_l.close()
 
 
 def ops_per_pair(w, batch) -> int:
