@@ -913,6 +913,10 @@ idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
     return IDB_OK;
 }
 
+int32_t idb_diag_eps(uint32_t lx, uint32_t ly, float threshold, int32_t abs_eps) {
+    return eps_value(lx, ly, threshold, abs_eps);
+}
+
 idb_status idb_diag_gene_bits(idb_context *c, const char *calls, const int64_t *offsets,
                               uint32_t n_rows, const char *genes, const int64_t *gene_offsets,
                               uint32_t n_genes, uint64_t *words_out) {

@@ -21,6 +21,12 @@ extern "C" {
    Returns 0 on success. */
 int idb_diag_int_peak(int device, double *gops_out, double *ms_out);
 
+/* The neighbour threshold the library uses for a pair of lengths: relative
+   threshold (NaN = unused) applied as (int)truncf((float)max(lx, ly) * threshold),
+   the reference's epsilonOneFunctorClass (cuda/SpecialFunctors.hcu:245-274),
+   capped by abs_eps when abs_eps >= 0.  Host-only; needs no device. */
+int32_t idb_diag_eps(uint32_t lx, uint32_t ly, float threshold, int32_t abs_eps);
+
 /* Number of admissible unique pairs of the input: pairs of uniques (after the
    duplicate collapse) in one repertoire whose V sets and J sets overlap and
    whose length gap is admissible (equal lengths in Hamming mode, |Lx-Ly| <=

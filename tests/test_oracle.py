@@ -3,6 +3,8 @@
 These pin the oracle (the reference ships no tests or fixtures; its CUDA path
 cannot run here), which then serves as the checker for the GPU path.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -86,3 +88,46 @@ def test_invariants_workload0():
         first.setdefault(int(r.clone_id[i]), int(i))
     order = [first[k] for k in sorted(first)]
     assert order == sorted(order)
+
+
+def _eps_golden():
+    import gzip
+    import json
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "eps_reference.json.gz")
+    with gzip.open(path, "rt") as f:
+        return json.load(f)
+
+
+def test_eps_matches_reference_functor():
+    """The oracle's threshold rule against the reference's own
+    epsilonOneFunctorClass, compiled from its header (golden table made by
+    tests/golden/make_eps_golden.py): every length pair up to 64 for the
+    Levenshtein functor and equal lengths up to 1024 for the Hamming one."""
+    g = _eps_golden()
+    n = g["max_len"]
+    for k, t in enumerate(g["thresholds"]):
+        lev = g["levenshtein"][k]
+        for q in range(n + 1):
+            for s in range(n + 1):
+                assert oracle.eps(q, s, t) == lev[q][s], (t, q, s)
+        ham = g["hamming"][k]
+        for q in range(0, g["diag_len"] + 1, 7):
+            assert oracle.eps(q, q, t) == ham[q], (t, q)
+
+
+def test_library_eps_matches_reference_functor():
+    """The threshold the library tabulates for its kernels (host code, no device
+    needed) against the same reference table."""
+    import ctypes as C
+    from immunodbscan_gb300 import _lib
+    L = _lib.lib()
+    g = _eps_golden()
+    n = g["max_len"]
+    for k, t in enumerate(g["thresholds"]):
+        lev = g["levenshtein"][k]
+        for q in range(n + 1):
+            for s in range(n + 1):
+                assert L.idb_diag_eps(q, s, C.c_float(t), -1) == lev[q][s], (t, q, s)
+        ham = g["hamming"][k]
+        for q in range(g["diag_len"] + 1):
+            assert L.idb_diag_eps(q, q, C.c_float(t), -1) == ham[q], (t, q)
