@@ -77,6 +77,8 @@ enum BufId {
 struct idb_context {
     int device = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   // host->device copies of the call columns
+    cudaEvent_t ev_v = nullptr, ev_j = nullptr;   // those copies done
     DevBuf buf[bNumBufs];
     Counters *h_ctr = nullptr;        // pinned mirror of the counters
     cudaEvent_t ev[16] = {};
@@ -229,12 +231,21 @@ idb_status upload_genes(idb_context *c, const char *names, const int64_t *off, u
 }
 
 struct Pipeline {
-    idb_context *c;
+    idb_context *c = nullptr;
     Plan P;
     Buffers B;
     bool trees = false;
     bool timing = false;
     std::vector<int16_t> eps_host;
+    // host inputs: the V / J call columns arrive on the copy stream, overlapped
+    // with the sequence survey and the plan; their gene-bitset kernels wait here
+    cudaEvent_t wait_v = nullptr, wait_j = nullptr;
+    bool copies_issued = false;
+    // every return path (errors included) leaves no copy from the caller's host
+    // buffers in flight
+    ~Pipeline() {
+        if (copies_issued && c) cudaStreamSynchronize(c->copy_stream);
+    }
 };
 
 void record(Pipeline &pl, int k) {
@@ -264,7 +275,7 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
     CU(cudaMemsetAsync(B.ctr, 0, sizeof(Counters), s));
     CU(cudaMemsetAsync(&B.ctr->lmin, 0xFF, sizeof(uint32_t), s));   // min starts at max
     auto stage = [&](const char *src, const int64_t *off, BufId bid, BufId oid,
-                     const uint8_t **dst, const int64_t **doff) -> idb_status {
+                     const uint8_t **dst, const int64_t **doff, cudaStream_t cs) -> idb_status {
         if (!host_inputs) {
             *dst = reinterpret_cast<const uint8_t *>(src);
             *doff = off;
@@ -273,9 +284,9 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
         const size_t nbytes = (size_t)(P.N ? off[P.N] : 0);
         TRY(ensure(c, bid, nbytes + 16));
         TRY(ensure(c, oid, sizeof(int64_t) * ((size_t)P.N + 1)));
-        if (nbytes) CU(cudaMemcpyAsync(c->buf[bid].p, src, nbytes, cudaMemcpyHostToDevice, s));
+        if (nbytes) CU(cudaMemcpyAsync(c->buf[bid].p, src, nbytes, cudaMemcpyHostToDevice, cs));
         CU(cudaMemcpyAsync(c->buf[oid].p, off, sizeof(int64_t) * ((size_t)P.N + 1),
-                           cudaMemcpyHostToDevice, s));
+                           cudaMemcpyHostToDevice, cs));
         *dst = ptr<uint8_t>(c, bid);
         *doff = ptr<int64_t>(c, oid);
         return IDB_OK;
@@ -287,10 +298,20 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
         B.seq = ptr<uint8_t>(c, bSeq);
         B.seq_off = ptr<int64_t>(c, bSeqOff);
     } else {
-        TRY(stage(in->seqs, in->seq_offsets, bSeq, bSeqOff, &B.seq, &B.seq_off));
+        TRY(stage(in->seqs, in->seq_offsets, bSeq, bSeqOff, &B.seq, &B.seq_off, s));
     }
-    if (!P.no_v) TRY(stage(in->v_calls, in->v_offsets, bV, bVOff, &B.vcall, &B.v_off));
-    if (!P.no_j) TRY(stage(in->j_calls, in->j_offsets, bJ, bJOff, &B.jcall, &B.j_off));
+    // host inputs: the call columns go on the copy stream, behind nothing, while
+    // the main stream surveys the sequences and the host derives the plan
+    cudaStream_t cs = host_inputs ? c->copy_stream : s;
+    pl.copies_issued = host_inputs;
+    if (!P.no_v) {
+        TRY(stage(in->v_calls, in->v_offsets, bV, bVOff, &B.vcall, &B.v_off, cs));
+        if (host_inputs) { CU(cudaEventRecord(c->ev_v, cs)); pl.wait_v = c->ev_v; }
+    }
+    if (!P.no_j) {
+        TRY(stage(in->j_calls, in->j_offsets, bJ, bJOff, &B.jcall, &B.j_off, cs));
+        if (host_inputs) { CU(cudaEventRecord(c->ev_j, cs)); pl.wait_j = c->ev_j; }
+    }
     // repertoire offsets
     std::vector<uint32_t> roff(P.R + 1);
     if (in->n_repertoires > 0 && in->rep_offsets) {
@@ -564,8 +585,11 @@ idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false
     Buffers &B = pl.B;
     cudaStream_t s = c->stream;
     if (!eager) launch_check_plan(P, B, s);
+    if (pl.wait_v) CU(cudaStreamWaitEvent(s, pl.wait_v, 0));
     launch_gene_bits(P, B, true, s);
+    if (pl.wait_j) CU(cudaStreamWaitEvent(s, pl.wait_j, 0));
     launch_gene_bits(P, B, false, s);
+    pl.wait_v = pl.wait_j = nullptr;   // a later run of the phases finds the columns in place
     launch_dedupe(P, B, s);
     launch_uniques(P, B, s);
     TRY(check_launch());
@@ -775,6 +799,9 @@ idb_status idb_context_create(int device, idb_context **out) {
     idb_context *c = new idb_context();
     c->device = device;
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&c->ev_v, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&c->ev_j, cudaEventDisableTiming));
     CU(cudaMallocHost(&c->h_ctr, sizeof(Counters)));
     for (auto &e : c->ev) CU(cudaEventCreate(&e));
     *out = c;
@@ -792,6 +819,9 @@ idb_status idb_context_destroy(idb_context *c) {
         if (e) cudaEventDestroy(e);
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
     if (c->mlp_bf16) cudaFree(c->mlp_bf16);
+    if (c->ev_v) cudaEventDestroy(c->ev_v);
+    if (c->ev_j) cudaEventDestroy(c->ev_j);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c == t_default_ctx) t_default_ctx = nullptr;
     delete c;

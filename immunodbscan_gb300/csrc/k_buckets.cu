@@ -414,13 +414,25 @@ __global__ void k_cls_scatter(const Counters *__restrict__ ctr, const BinPair *_
             const float c = fmaxf(pred[i], 1.0f);
             cls = min(63u, (uint32_t)(log2f(c) * 2.0f));
         }
-        const uint32_t pos = start[63 - cls] + atomicAdd(&cursor[63 - cls], 1u);
+        // one cursor increment per class among the warp's active lanes
+        const uint32_t act = __activemask();
+        const uint32_t grp = __match_any_sync(act, cls);
+        const uint32_t lane = threadIdx.x & 31, leader = (uint32_t)__ffs(grp) - 1;
+        uint32_t base = 0;
+        if (lane == leader) base = atomicAdd(&cursor[63 - cls], (uint32_t)__popc(grp));
+        base = __shfl_sync(act, base, leader);
+        const uint32_t pos = start[63 - cls] + base + __popc(grp & ((1u << lane) - 1u));
         P.cls = (uint8_t)cls;
         out[pos] = P;
         uint64_t nu;
         if (small_mode && P.a_n <= kSmallSide && (P.same || P.b_n <= kSmallSide)) {
             nu = 0;                               // pair-parallel path, no tiled units
-            small_list[atomicAdd(n_small, 1u)] = pos;
+            const uint32_t am = __activemask();
+            const uint32_t ld = (uint32_t)__ffs(am) - 1;
+            uint32_t b0 = 0;
+            if (lane == ld) b0 = atomicAdd(n_small, (uint32_t)__popc(am));
+            b0 = __shfl_sync(am, b0, ld);
+            small_list[b0 + __popc(am & ((1u << lane) - 1u))] = pos;
         } else if (P.same) {
             const uint32_t ncy = (P.a_n + TY - 1) / TY;
             nu = tri_units(P.ncx, ncy, q);

@@ -406,10 +406,13 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
         for (uint32_t t = lane; t < nb; t += 32) sym[t] = __ldg(a.meta + yrow0 + yb + t);
         __syncwarp();
         uint32_t qn = 0;
-        for (uint32_t t = 0; t < nb; ++t) {
-            const uint32_t yp = U.ybase + yb + t;
-            // same bin: only x-entries before y count; none before -> skip y
-            if (same && yp <= U.xbase) continue;
+        // y-entries inside the unit's own x range (same bin) need the mask of the
+        // x-entries before them; they come first in the chunk (y ascending, all
+        // after xbase), the rest pair with every x-entry of the unit
+        uint32_t tdiag = 0;
+        if (same && U.ybase + yb < U.xbase + U.nx)
+            tdiag = min(nb, U.xbase + U.nx - (U.ybase + yb));
+        auto score = [&](uint32_t t, uint32_t (&sc)[RX]) {
             uint32_t y[NW];
 #pragma unroll
             for (int q = 0; q < R16; ++q) {
@@ -421,7 +424,6 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
             }
             // FULL: all RX chains without branches (independent, interleaved);
             // otherwise only the r-blocks that hold entries (warp-uniform test)
-            uint32_t sc[RX];
 #pragma unroll
             for (int r = 0; r < RX; ++r) {
                 if (!FULL && r >= rb) { sc[r] = kOff; continue; }
@@ -442,41 +444,66 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
                     sc[r] = dist | vmask[r];
                 }
             }
-            // y inside the unit's own x range (same bin): mask x-entries not before y
-            if (same && yp < U.xbase + U.nx) {
-                const uint32_t nact = yp - U.xbase;
+        };
+        auto record = [&](uint32_t t, const uint32_t (&sc)[RX]) {
+            // with exact signatures a hit outside its canonical bin is dropped
+            // here: sig_x & sig_y must be empty
+            const uint4 ym = sym[t];
+            uint32_t hit = 0;
 #pragma unroll
-                for (int r = 0; r < RX; ++r)
-                    if ((uint32_t)r * 32 + lane >= nact) sc[r] |= kOff;
-            }
-            uint32_t z = sc[0];
-#pragma unroll
-            for (int r = 1; r < RX; ++r) z = min(z, sc[r]);
-            if (z <= thr) {
-                // with exact signatures a hit outside its canonical bin is dropped
-                // here: sig_x & sig_y must be empty
-                const uint4 ym = sym[t];
-                uint32_t hit = 0;
-#pragma unroll
-                for (int r = 0; r < RX; ++r)
-                    if (sc[r] <= thr) {
-                        bool ok = true;
-                        if (a.sig_exact) {
-                            const uint4 m = sxm[32 * r + lane];
-                            ok = ((m.x & ym.x) | (m.y & ym.y) | (m.z & ym.z)) == 0;
-                        }
-                        hit |= (uint32_t)ok << r;
+            for (int r = 0; r < RX; ++r)
+                if (sc[r] <= thr) {
+                    bool ok = true;
+                    if (a.sig_exact) {
+                        const uint4 m = sxm[32 * r + lane];
+                        ok = ((m.x & ym.x) | (m.y & ym.y) | (m.z & ym.z)) == 0;
                     }
-                hit &= valid;
-                if (hit) shq[qn++ * 32 + lane] = (t << 8) | hit;
-            }
-            if (__any_sync(0xFFFFFFFFu, qn == kHitQ)) {
+                    hit |= (uint32_t)ok << r;
+                }
+            hit &= valid;
+            if (hit) shq[qn++ * 32 + lane] = (t << 8) | hit;
+        };
+        auto drain_if_full = [&](uint32_t room) {
+            if (__any_sync(0xFFFFFFFFu, qn + room > (uint32_t)kHitQ)) {
                 __syncwarp();
                 drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same,
                            U.P.v, U.P.j, lane);
                 qn = 0;
                 __syncwarp();
             }
+        };
+        for (uint32_t t = 0; t < tdiag; ++t) {
+            uint32_t sc[RX];
+            score(t, sc);
+            const uint32_t nact = U.ybase + yb + t - U.xbase;   // x-entries before y
+#pragma unroll
+            for (int r = 0; r < RX; ++r)
+                if ((uint32_t)r * 32 + lane >= nact) sc[r] |= kOff;
+            uint32_t z = sc[0];
+#pragma unroll
+            for (int r = 1; r < RX; ++r) z = min(z, sc[r]);
+            if (z <= thr) record(t, sc);
+            drain_if_full(1);
+        }
+        uint32_t t = tdiag;
+        for (; t + 1 < nb; t += 2) {      // two y-entries per step: twice the chains
+            uint32_t sa[RX], sb[RX];
+            score(t, sa);
+            score(t + 1, sb);
+            uint32_t za = sa[0], zb = sb[0];
+#pragma unroll
+            for (int r = 1; r < RX; ++r) { za = min(za, sa[r]); zb = min(zb, sb[r]); }
+            if (za <= thr) record(t, sa);
+            if (zb <= thr) record(t + 1, sb);
+            drain_if_full(2);
+        }
+        if (t < nb) {
+            uint32_t sc[RX];
+            score(t, sc);
+            uint32_t z = sc[0];
+#pragma unroll
+            for (int r = 1; r < RX; ++r) z = min(z, sc[r]);
+            if (z <= thr) record(t, sc);
         }
         if (__any_sync(0xFFFFFFFFu, qn)) {
             __syncwarp();
