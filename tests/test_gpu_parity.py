@@ -101,6 +101,30 @@ def _random_workload(rng, n, lo, hi, alphabet, hamming, eps, min_pts, n_fam=None
 
 
 @pytest.mark.parametrize("hamming", [True, False])
+def test_wide_gene_lists(gpu_ctx, hamming):
+    """More than 64 V genes and more than 32 J genes: multi-word bitsets, and a
+    neighbour's canonical bin is decided from the full bitsets (lowest common V
+    and J gene) instead of the one-word signatures; ambiguous calls of 1-4
+    genes spread each unique over many bins, small and large."""
+    rng = np.random.default_rng(21)
+    n = 6000
+    w0 = _random_workload(rng, n, 10, 16, list(b"ACDEFGHIKLMNPQRSTVWY"), hamming, 1, 2,
+                          n_fam=300)
+    vg = [b"TRBV%d-%d*" % (a, b) for a in range(1, 31) for b in range(1, 6)]     # 150
+    jg = [b"TRBJ%d-%d*" % (a, b) for a in range(1, 9) for b in range(1, 6)]      # 40
+    seqs = [w0.seq(i) for i in range(n)]
+    vc, jc = [], []
+    for s in seqs:
+        # a length-dependent gene shared by most neighbours, plus random extras
+        gv = {(len(s) // 3) * 7 % len(vg)} | set(rng.choice(len(vg), size=int(rng.integers(0, 4))).tolist())
+        gj = {(len(s) // 4) * 5 % len(jg)} | set(rng.choice(len(jg), size=int(rng.integers(0, 3))).tolist())
+        vc.append(b", or ".join(vg[g][:-1] + b"*01" for g in sorted(gv)))
+        jc.append(b", or ".join(jg[g][:-1] + b"*01" for g in sorted(gj)))
+    w = synth.from_strings(seqs, vc, jc, vg, jg, abs_eps=1, min_pts=2, use_hamming=hamming)
+    assert_same(cluster_workload(w, gpu_ctx), oracle.cluster(w), w, "wide gene lists")
+
+
+@pytest.mark.parametrize("hamming", [True, False])
 @pytest.mark.parametrize("lo,hi", [(30, 40), (60, 70), (90, 128)])
 def test_multiword_lengths(gpu_ctx, hamming, lo, hi):
     rng = np.random.default_rng(lo + hamming)
