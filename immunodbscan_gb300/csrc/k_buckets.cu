@@ -97,7 +97,9 @@ __global__ void k_group_insert(BinGeom g, Counters *ctr, const uint32_t *__restr
             sl = (sl + 1) & mask;
         }
         uslot[u] = (uint32_t)sl;
-        if (sl != kNone) atomicAdd(&tcount[sl], 1u);
+        const uint32_t grp = __match_any_sync(__activemask(), (uint32_t)sl);
+        if ((threadIdx.x & 31) == (uint32_t)__ffs(grp) - 1 && sl != kNone)
+            atomicAdd(&tcount[sl], (uint32_t)__popc(grp));
     }
 }
 
@@ -137,7 +139,11 @@ __global__ void k_bin_hist(BinGeom g, const Counters *__restrict__ ctr,
                         const uint32_t j = jw * 64 + lowest_bit64(jb);
                         jb &= jb - 1;
                         if (j >= g.Gj) break;
-                        atomicAdd(&hist[g.bin(r, v, j, L, uclass[u])], 1u);
+                        // one increment per bin among the lanes here together
+                        const uint32_t b = g.bin(r, v, j, L, uclass[u]);
+                        const uint32_t grp = __match_any_sync(__activemask(), b);
+                        if ((threadIdx.x & 31) == (uint32_t)__ffs(grp) - 1)
+                            atomicAdd(&hist[b], (uint32_t)__popc(grp));
                     }
                 }
             }
@@ -258,9 +264,21 @@ k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
                         const uint32_t b = g.bin(r, v, j, L, uclass[u]);
                         const uint64_t sv = below(vbits[(size_t)row * g.VW], v);
                         const uint64_t sj = below(jbits[(size_t)row * g.JW], j);
-                        atomicAnd(&sig_and[2 * (size_t)b], sv);
-                        atomicAnd(&sig_and[2 * (size_t)b + 1], sj);
-                        const uint64_t pos = (uint64_t)bin_start[b] + atomicAdd(&cursor[b], 1u);
+                        // the ANDs only clear bits: no atomic when nothing would change
+                        // (a stale read can only cost an unneeded atomic)
+                        const unsigned long long cv = sig_and[2 * (size_t)b];
+                        if ((cv & sv) != cv) atomicAnd(&sig_and[2 * (size_t)b], sv);
+                        const unsigned long long cj = sig_and[2 * (size_t)b + 1];
+                        if ((cj & sj) != cj) atomicAnd(&sig_and[2 * (size_t)b + 1], sj);
+                        // one cursor increment per bin among the lanes here together
+                        const uint32_t am = __activemask();
+                        const uint32_t grp = __match_any_sync(am, b);
+                        const uint32_t lane = threadIdx.x & 31, ld = (uint32_t)__ffs(grp) - 1;
+                        uint32_t base = 0;
+                        if (lane == ld) base = atomicAdd(&cursor[b], (uint32_t)__popc(grp));
+                        base = __shfl_sync(grp, base, ld);
+                        const uint64_t pos = (uint64_t)bin_start[b] + base +
+                                             __popc(grp & ((1u << lane) - 1u));
                         if (pos >= cap_entries) { atomicOr(err, kErrEntryOverflow); continue; }
                         ent_uid[pos] = u;
                         // side record: signature below (v, j) and the unique id

@@ -382,7 +382,8 @@ __device__ __forceinline__ uint32_t byte_mask(uint32_t n) {
 
 // Byte equality of a call in global memory with the staged bytes at offset q0.
 // Reads only the aligned 4-byte words that hold the call's bytes (so no read
-// leaves the call's pages), joined by a funnel shift; no early exit.
+// leaves the call's pages), joined by a funnel shift; no early exit.  Whole
+// words first, the ragged last word masked.
 __device__ __forceinline__ bool bytes_equal_global(const uint8_t *g, const uint32_t *words,
                                                    uint32_t q0, uint32_t len) {
     if (len == 0) return true;
@@ -393,12 +394,17 @@ __device__ __forceinline__ bool bytes_equal_global(const uint8_t *g, const uint3
     StagedReader rd(words, q0);
     uint32_t gprev = __ldg(gw);
     uint32_t diff = 0;
-    for (uint32_t k = 0; k < len; k += 4) {
-        const uint32_t t = k >> 2;
+    const uint32_t full = len >> 2;                  // words whose 4 bytes are all in the call
+    uint32_t t = 0;
+#pragma unroll 2
+    for (; t < full; ++t) {
         const uint32_t gnext = t + 1 <= last ? __ldg(gw + t + 1) : 0u;
-        const uint32_t gv = __funnelshift_r(gprev, gnext, 8 * sh);
+        diff |= __funnelshift_r(gprev, gnext, 8 * sh) ^ rd.next();
         gprev = gnext;
-        diff |= (gv ^ rd.next()) & byte_mask(len - k);
+    }
+    if (len & 3u) {
+        const uint32_t gnext = t + 1 <= last ? __ldg(gw + t + 1) : 0u;
+        diff |= (__funnelshift_r(gprev, gnext, 8 * sh) ^ rd.next()) & byte_mask(len & 3u);
     }
     return diff == 0;
 }
@@ -408,7 +414,10 @@ __device__ __forceinline__ bool staged_equal(const uint32_t *words, uint32_t qa,
                                              uint32_t len) {
     StagedReader ra(words, qa), rb(words, qb);
     uint32_t diff = 0;
-    for (uint32_t k = 0; k < len; k += 4) diff |= (ra.next() ^ rb.next()) & byte_mask(len - k);
+    const uint32_t full = len >> 2;
+#pragma unroll 2
+    for (uint32_t t = 0; t < full; ++t) diff |= ra.next() ^ rb.next();
+    if (len & 3u) diff |= (ra.next() ^ rb.next()) & byte_mask(len & 3u);
     return diff == 0;
 }
 
@@ -418,11 +427,17 @@ __device__ __forceinline__ unsigned long long call_hash(const uint32_t *words, u
                                                         uint32_t len) {
     StagedReader rd(words, q0);
     uint32_t h1 = 0x811C9DC5u ^ len, h2 = 0x2545F491u + len;
-    for (uint32_t k = 0; k < len; k += 4) {
-        const uint32_t v = rd.next() & byte_mask(len - k);
+    const uint32_t full = len >> 2;
+#pragma unroll 2
+    for (uint32_t t = 0; t < full; ++t) {
+        const uint32_t v = rd.next();
         h1 = (h1 ^ v) * 0x01000193u;
         h2 = (h2 + v) * 0x9E3779B1u;
-        h2 ^= h2 >> 15;
+    }
+    if (len & 3u) {
+        const uint32_t v = rd.next() & byte_mask(len & 3u);
+        h1 = (h1 ^ v) * 0x01000193u;
+        h2 = (h2 + v) * 0x9E3779B1u;
     }
     return mix64(((unsigned long long)h1 << 32) | h2, len);
 }
