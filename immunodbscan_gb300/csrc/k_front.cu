@@ -46,11 +46,42 @@ __global__ void k_survey(const uint8_t *__restrict__ seq, const int64_t *__restr
         lmax = max(lmax, L);
         lmin = min(lmin, L);
     }
+    // byte values present: 16 bytes per thread and step (aligned 16-byte loads,
+    // the ragged ends byte by byte); values 64..127 (the letters) go to a
+    // per-thread 64-bit mask, the rest straight to shared memory
     const int64_t b0 = N ? off[0] : 0, b1 = N ? off[N] : 0;
-    for (int64_t p = b0 + blockIdx.x * blockDim.x + threadIdx.x; p < b1; p += stride) {
-        uint32_t b = seq[p];
-        uint32_t bit = 1u << (b & 31);
-        if (!(used[b >> 5] & bit)) atomicOr(&used[b >> 5], bit);
+    unsigned long long m64 = 0;
+    auto note = [&](uint32_t b) {
+        if ((b & 0xC0u) == 0x40u) {
+            m64 |= 1ull << (b & 63u);
+        } else {
+            const uint32_t bit = 1u << (b & 31);
+            if (!(used[b >> 5] & bit)) atomicOr(&used[b >> 5], bit);
+        }
+    };
+    const int64_t a0 = (int64_t)((reinterpret_cast<uintptr_t>(seq + b0) + 15) & ~(uintptr_t)15) -
+                       (int64_t)reinterpret_cast<uintptr_t>(seq);   // first aligned byte
+    const int64_t head_end = a0 < b1 ? a0 : b1;
+    const uint32_t gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int64_t p = b0 + gtid; p < head_end; p += stride) note(seq[p]);
+    const int64_t nvec = b1 > head_end ? (b1 - head_end) >> 4 : 0;
+    const uint4 *vec = reinterpret_cast<const uint4 *>(seq + head_end);
+    for (int64_t k = gtid; k < nvec; k += stride) {
+        const uint4 v = __ldg(vec + k);
+        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) note((w4[e] >> (8 * q)) & 0xFFu);
+    }
+    for (int64_t p = head_end + 16 * nvec + gtid; p < b1; p += stride) note(seq[p]);
+    {
+        const uint32_t lo = __reduce_or_sync(0xFFFFFFFFu, (uint32_t)m64);
+        const uint32_t hi = __reduce_or_sync(0xFFFFFFFFu, (uint32_t)(m64 >> 32));
+        if ((threadIdx.x & 31) == 0) {
+            if (lo) atomicOr(&used[2], lo);
+            if (hi) atomicOr(&used[3], hi);
+        }
     }
     atomicMax(&smax, lmax);
     atomicMin(&smin, lmin);
