@@ -113,32 +113,6 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t *p, uint32_t x) {
 
 // Core-core edges are merged (S6); an edge with one core end counts towards
 // the border CSR degree of its non-core end.
-// Roots of a and b with path halving, the two walks interleaved so that their
-// loads are in flight together (the walks are chains of dependent loads).
-__device__ __forceinline__ void uf_find2(uint32_t *p, uint32_t a, uint32_t b, uint32_t &ra,
-                                         uint32_t &rb) {
-    volatile uint32_t *vp = p;
-    bool da = false, db = false;
-    while (!(da && db)) {    // parent[y] <= y: each walk strictly decreases, terminates
-        const uint32_t pa = da ? a : vp[a];
-        const uint32_t pb = db ? b : vp[b];
-        if (!da && pa == a) da = true;
-        if (!db && pb == b) db = true;
-        const uint32_t ppa = da ? a : vp[pa];
-        const uint32_t ppb = db ? b : vp[pb];
-        if (!da) {
-            if (ppa == pa) { a = pa; da = true; }
-            else { vp[a] = ppa; a = ppa; }
-        }
-        if (!db) {
-            if (ppb == pb) { b = pb; db = true; }
-            else { vp[b] = ppb; b = ppb; }
-        }
-    }
-    ra = a;
-    rb = b;
-}
-
 __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ edges,
                         const uint32_t *__restrict__ ucore, uint32_t *parent,
                         uint32_t *__restrict__ deg) {
@@ -155,8 +129,7 @@ __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ e
         uint32_t a = ed.x, b = ed.y;
         uint32_t it = 0;
         for (; it < kSpinCap; ++it) {
-            uint32_t ra, rb;
-            uf_find2(parent, a, b, ra, rb);
+            uint32_t ra = uf_find(parent, a), rb = uf_find(parent, b);
             if (ra == rb) break;
             if (ra < rb) { const uint32_t t = ra; ra = rb; rb = t; }
             // hook the larger root under the smaller one
