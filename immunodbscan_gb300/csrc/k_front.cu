@@ -639,35 +639,23 @@ __global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
             const uint32_t hi = k + 4 < L ? rd.next() : 0u;
             h = mix64(h, ((uint64_t)hi << 32) | lo);
         }
-        // rows of the warp with equal hashes: the lowest probes the table, the
-        // others compare themselves with it (a nearby, cached row) and, if
-        // equal, take its slot
-        const uint32_t am = __activemask();
-        const uint32_t hgrp = __match_any_sync(am, h);
-        const int hlead = __ffs(hgrp) - 1;
-        const uint32_t lrow = __shfl_sync(am, i, hlead);
-        const bool follow = (int)(threadIdx.x & 31) != hlead && rows_equal(a, i, lrow, r, o, L);
         uint64_t s = h & a.mask;
-        if (!follow) {
-            uint32_t it = 0;
-            for (;; ++it) {
-                if (it > a.mask || it >= kSpinCap) {   // table full: cannot happen at load <= 1/2
-                    atomicOr(&a.ctr->error, kErrHashStall);
-                    s = kNone;
-                    break;
-                }
-                uint32_t cur = *((volatile uint32_t *)&a.table[s]);
-                if (cur == kNone) {
-                    uint32_t prev = atomicCAS(&a.table[s], kNone, i);
-                    if (prev == kNone) break;
-                    cur = prev;
-                }
-                if (rows_equal(a, i, cur, r, o, L)) break;
-                s = (s + 1) & a.mask;
+        uint32_t it = 0;
+        for (;; ++it) {
+            if (it > a.mask || it >= kSpinCap) {   // table full: cannot happen at load <= 1/2
+                atomicOr(&a.ctr->error, kErrHashStall);
+                s = kNone;
+                break;
             }
+            uint32_t cur = *((volatile uint32_t *)&a.table[s]);
+            if (cur == kNone) {
+                uint32_t prev = atomicCAS(&a.table[s], kNone, i);
+                if (prev == kNone) break;
+                cur = prev;
+            }
+            if (rows_equal(a, i, cur, r, o, L)) break;
+            s = (s + 1) & a.mask;
         }
-        const uint64_t lslot = __shfl_sync(am, s, hlead);
-        if (follow) s = lslot;
         a.slot[i] = (uint32_t)s;
         // one class-size increment and one minimum per class among the warp's
         // rows (lanes hold ascending rows, so the lowest lane has the smallest)
