@@ -69,7 +69,8 @@ enum BufId {
     bURow, bUCopies, bULen, bURep, bBinHist, bBinCursor, bEntUid, bEntRec, bBpCount, bBp,
     bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bDeg, bGOff, bGCur, bAdj, bCnt, bUCore,
     bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
-    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bBpSmall, bNumBufs
+    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bBpSmall,
+    bJnTab, bJnCount, bJnSlotHead, bJnISlot, bJnHeadSlot, bJnStart, bJnCur, bJnBpIdx, bNumBufs
 };
 
 }  // namespace
@@ -241,6 +242,7 @@ struct Pipeline {
     // with the sequence survey and the plan; their gene-bitset kernels wait here
     cudaEvent_t wait_v = nullptr, wait_j = nullptr;
     bool copies_issued = false;
+    bool allow_join = true;   // the segment join finds neighbours, not all admissible pairs
     // every return path (errors included) leaves no copy from the caller's host
     // buffers in flight
     ~Pipeline() {
@@ -430,6 +432,11 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
     P.K = 4;
     P.big_group = 64;
     P.sig_exact = P.Gv <= 64 && P.Gj <= 32;
+    // Hamming with a small eps at every length: candidate pairs by segment join
+    // (the side records then carry the V bits and the J bits with the segment)
+    P.join = pl.allow_join && P.hamming && P.fast && emax_same <= kJoinMaxEps &&
+             P.Gv <= 64 && P.Gj <= 30;
+    P.join_smax = P.join ? (uint32_t)std::max(1, emax_same + 1) : 1u;
     P.nbins = (uint64_t)P.R * P.Gv * P.Gj * P.NL * P.K;
     if (P.nbins >= (1ull << 31))
         return fail(IDB_ERR_UNSUPPORTED, "too many buckets (repertoires x V genes x J genes x lengths = %llu)",
@@ -490,7 +497,32 @@ idb_status alloc_fixed(Pipeline &pl) {
     TRY(ensure(c, bRootFlag, 4 * N1));
     TRY(ensure(c, bUidFirst, 4 * (P.R + 1)));
     TRY(ensure(c, bDepth, 4 * (kDepthMax + 1)));
-    const uint64_t scan_n = std::max<uint64_t>(N1, P.nbins + 1);
+    uint64_t scan_n = std::max<uint64_t>(N1, P.nbins + 1);
+    if (P.join) {
+        // keys: at most join_smax per unique; the table at load <= 1/2
+        const uint64_t heads = (uint64_t)P.join_smax * N;
+        const uint64_t jcap = next_pow2(std::max<uint64_t>(2 * heads, 1024));
+        if (jcap > (1ull << 31) || 4 * N > 0xFFFFFFF0ull)
+            return fail(IDB_ERR_UNSUPPORTED, "segment join table too large");
+        TRY(ensure(c, bJnTab, 4 * jcap));
+        TRY(ensure(c, bJnCount, 4 * jcap));
+        TRY(ensure(c, bJnSlotHead, 4 * jcap));
+        TRY(ensure(c, bJnISlot, 16 * N1));
+        TRY(ensure(c, bJnHeadSlot, 4 * (heads + 1)));
+        TRY(ensure(c, bJnStart, 4 * (heads + 1)));
+        TRY(ensure(c, bJnCur, 4 * (heads + 1)));
+        TRY(ensure(c, bJnBpIdx, 4 * (heads + 1)));
+        B.jn_tab = ptr<uint32_t>(c, bJnTab);
+        B.jn_count = ptr<uint32_t>(c, bJnCount);
+        B.jn_slot_head = ptr<uint32_t>(c, bJnSlotHead);
+        B.jn_mask = jcap - 1;
+        B.jn_islot = ptr<uint32_t>(c, bJnISlot);
+        B.jn_head_slot = ptr<uint32_t>(c, bJnHeadSlot);
+        B.jn_start = ptr<uint32_t>(c, bJnStart);
+        B.jn_cur = ptr<uint32_t>(c, bJnCur);
+        B.jn_bpidx = ptr<uint32_t>(c, bJnBpIdx);
+        scan_n = std::max<uint64_t>(scan_n, heads + 1);
+    }
     B.scan_part_cap = scan_part_needed(std::max<uint64_t>(scan_n, 1u << 20));
     TRY(ensure(c, bScanPart, 4 * (size_t)B.scan_part_cap));
     B.vbits = ptr<uint64_t>(c, bVBits); B.jbits = ptr<uint64_t>(c, bJBits);
@@ -1280,6 +1312,7 @@ idb_status idb_count_admissible(idb_context *c, const idb_input *in, const idb_p
     CU(cudaSetDevice(c->device));
     Pipeline pl;
     pl.c = c;
+    pl.allow_join = false;    // every admissible pair must be enumerated here
     TRY(stage_inputs_and_survey(pl, in, true));
     TRY(derive_plan(pl, prm));
     TRY(alloc_fixed(pl));

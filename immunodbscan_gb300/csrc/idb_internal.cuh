@@ -19,6 +19,9 @@ constexpr uint32_t kSpinCap = 1u << 22; // bound of every device-side retry loop
 // Bin pairs with at most kSmallSide entries on each side (Hamming fast path) are
 // evaluated pair-parallel: lanes take pairs, records travel by shuffles.
 constexpr uint32_t kSmallSide = 32;
+// Hamming with eps <= kJoinMaxEps for every length uses the segment join: two
+// equal-length sequences within eps agree exactly on one of eps+1 segments.
+constexpr int kJoinMaxEps = 3;
 constexpr int kMlpIn = 16;              // learned scheduler: features per bin pair
 constexpr int kMlpHidden = 64;          // two hidden layers of 64
 constexpr int kMlpParams = kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +
@@ -105,6 +108,9 @@ struct Counters {
     uint32_t small_cursor;       // their work queue head
     uint32_t n_heavy;            // bin pairs the learned predictor evaluates
     uint32_t n_core_edges;       // neighbour pairs with both ends core
+    uint32_t n_heads;            // segment join: distinct segment keys
+    uint32_t n_groups;           // segment join: keys held by two or more uniques
+    uint32_t pad2[2];
 };
 
 // One bucket ("bin") holds the uniques of one (repertoire, V gene, J gene,
@@ -147,6 +153,8 @@ struct Plan {
     int schedule = 0;
     int hamming_eps_mode = 0;                     // 0 popcount, 1 eps==1, 2 eps==0
     bool sig_exact = true;                        // V genes <= 64 and J genes <= 32
+    bool join = false;                            // Hamming by segment join (eps <= kJoinMaxEps)
+    uint32_t join_smax = 1;                       // most segments of any length
     uint8_t codemap[256];
     int first_byte = -1;                          // byte value with code 0
     // capacities
@@ -194,6 +202,13 @@ struct Buffers {
     BinPair *bp = nullptr, *bp_sorted = nullptr;    // [cap_binpairs]
     uint32_t *bp_units = nullptr;                   // [cap_binpairs+1]
     uint32_t *bp_small = nullptr;                   // [cap_binpairs] schedule positions of small bin pairs
+    // segment join: table of (unique, segment) keys and the groups they form
+    uint32_t *jn_tab = nullptr, *jn_count = nullptr, *jn_slot_head = nullptr;   // [jn_mask+1]
+    uint64_t jn_mask = 0;
+    uint32_t *jn_islot = nullptr;                   // [4*N] slot of (unique, segment)
+    uint32_t *jn_head_slot = nullptr;               // [join_smax*N] slot of each key
+    uint32_t *jn_start = nullptr;                   // [join_smax*N+1] group sizes -> starts
+    uint32_t *jn_cur = nullptr, *jn_bpidx = nullptr;   // [join_smax*N]
     uint32_t *cls_hist = nullptr;                   // [65]
     float *pred = nullptr;                          // learned cost per bin pair
     // graph

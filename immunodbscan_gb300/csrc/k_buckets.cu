@@ -158,6 +158,72 @@ __global__ void k_bin_hist(BinGeom g, const Counters *__restrict__ ctr,
 //  codes (Levenshtein and generic path): one code byte per residue.
 // Codes are a bijection of the byte values present, so equality of codes is
 // equality of bytes.
+// The record of one unique (fast paths: at most NR 16-byte words): bit planes
+// (Hamming) or code bytes (Levenshtein), residues read 4 at a time.
+template <int NR>
+__device__ __forceinline__ void build_small_record(const uint8_t *s, uint32_t L,
+                                                   const uint8_t *cm, int planes, uint32_t W,
+                                                   uint4 (&rec)[NR]) {
+    if (planes > 0) {
+        uint32_t wd[5][4];
+#pragma unroll
+        for (int p = 0; p < 5; ++p)
+#pragma unroll
+            for (int w = 0; w < 4; ++w) wd[p][w] = 0;
+        // residues read 4 at a time; positions past L keep code 0 (padding)
+        GlobalReader rd(s, L);
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            for (uint32_t k = 0; k < 8; ++k) {
+                const uint32_t i0 = 32u * w + 4u * k;
+                if (i0 >= L) break;
+                const uint32_t v = rd.next();
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    const uint32_t c = i0 + b < L ? (uint32_t)cm[(v >> (8 * b)) & 0xFFu] : 0u;
+#pragma unroll
+                    for (int p = 0; p < 5; ++p) wd[p][w] |= ((c >> p) & 1u) << (4 * k + b);
+                }
+            }
+        }
+        // layout: word p*W + w
+        uint32_t flat[4 * NR];
+#pragma unroll
+        for (int k = 0; k < 4 * NR; ++k) flat[k] = 0;
+#pragma unroll
+        for (int p = 0; p < 5; ++p)
+#pragma unroll
+            for (int w = 0; w < 4; ++w)
+                if (p < planes && (uint32_t)w < W) {
+                    const uint32_t k = (uint32_t)p * W + w;
+#pragma unroll
+                    for (int kk = 0; kk < 4 * NR; ++kk)
+                        if ((uint32_t)kk == k) flat[kk] = wd[p][w];
+                }
+#pragma unroll
+        for (int q = 0; q < NR; ++q) rec[q] = make_uint4(flat[4 * q], flat[4 * q + 1], flat[4 * q + 2], flat[4 * q + 3]);
+    } else {
+        GlobalReader rd(s, L);
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+            uint32_t wv[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const uint32_t i0 = q * 16 + e * 4;
+                const uint32_t v = i0 < L ? rd.next() : 0u;
+                uint32_t acc = 0;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const uint32_t c = i0 + t < L ? (uint32_t)cm[(v >> (8 * t)) & 0xFFu] : 0u;
+                    acc |= c << (8 * t);
+                }
+                wv[e] = acc;
+            }
+            rec[q] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+        }
+    }
+}
+
 // RSC: record size in 16-byte words when it is a compile-time 1..8 (the fast
 // paths: the record is built once, in RSC uint4 registers), 0 for the long
 // records of the generic path (code bytes packed per entry).
@@ -189,66 +255,7 @@ k_bin_fill(BinGeom g, const Counters *__restrict__ ctr,
         constexpr int NR = RSC > 0 ? RSC : 1;
         uint4 rec[NR];
         constexpr bool small = RSC > 0;
-        if (small) {
-            if (planes > 0) {
-                uint32_t wd[5][4];
-#pragma unroll
-                for (int p = 0; p < 5; ++p)
-#pragma unroll
-                    for (int w = 0; w < 4; ++w) wd[p][w] = 0;
-                // residues read 4 at a time; positions past L keep code 0 (padding)
-                GlobalReader rd(s, L);
-#pragma unroll
-                for (int w = 0; w < 4; ++w) {
-                    for (uint32_t k = 0; k < 8; ++k) {
-                        const uint32_t i0 = 32u * w + 4u * k;
-                        if (i0 >= L) break;
-                        const uint32_t v = rd.next();
-#pragma unroll
-                        for (int b = 0; b < 4; ++b) {
-                            const uint32_t c = i0 + b < L ? (uint32_t)cm[(v >> (8 * b)) & 0xFFu] : 0u;
-#pragma unroll
-                            for (int p = 0; p < 5; ++p) wd[p][w] |= ((c >> p) & 1u) << (4 * k + b);
-                        }
-                    }
-                }
-                // layout: word p*W + w
-                uint32_t flat[4 * NR];
-#pragma unroll
-                for (int k = 0; k < 4 * NR; ++k) flat[k] = 0;
-#pragma unroll
-                for (int p = 0; p < 5; ++p)
-#pragma unroll
-                    for (int w = 0; w < 4; ++w)
-                        if (p < planes && (uint32_t)w < W) {
-                            const uint32_t k = (uint32_t)p * W + w;
-#pragma unroll
-                            for (int kk = 0; kk < 4 * NR; ++kk)
-                                if ((uint32_t)kk == k) flat[kk] = wd[p][w];
-                        }
-#pragma unroll
-                for (int q = 0; q < NR; ++q) rec[q] = make_uint4(flat[4 * q], flat[4 * q + 1], flat[4 * q + 2], flat[4 * q + 3]);
-            } else {
-                GlobalReader rd(s, L);
-#pragma unroll
-                for (int q = 0; q < NR; ++q) {
-                    uint32_t wv[4];
-#pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const uint32_t i0 = q * 16 + e * 4;
-                        const uint32_t v = i0 < L ? rd.next() : 0u;
-                        uint32_t acc = 0;
-#pragma unroll
-                        for (int t = 0; t < 4; ++t) {
-                            const uint32_t c = i0 + t < L ? (uint32_t)cm[(v >> (8 * t)) & 0xFFu] : 0u;
-                            acc |= c << (8 * t);
-                        }
-                        wv[e] = acc;
-                    }
-                    rec[q] = make_uint4(wv[0], wv[1], wv[2], wv[3]);
-                }
-            }
-        }
+        if (small) build_small_record<NR>(s, L, cm, planes, W, rec);
         for (uint32_t vw = 0; vw < g.VW; ++vw) {
             uint64_t vb = vbits[(size_t)row * g.VW + vw];
             while (vb) {
@@ -470,10 +477,219 @@ __global__ void k_set_unit_base(const Counters *__restrict__ ctr, BinPair *__res
         bp[i].unit_base = base[i];
 }
 
+
+// ---------------------------------------------------------------------------
+// Segment join (Hamming, eps(L,L) <= kJoinMaxEps for every length).  Split a
+// sequence of length L into S = eps+1 segments [k*L/S, (k+1)*L/S): two
+// sequences of length L within Hamming distance eps differ in at most eps
+// positions, so at least one segment is identical (pigeonhole).  Every unique
+// is entered once per segment under the key (repertoire, L, k, segment bytes);
+// the uniques that share a key form a group, and only pairs inside a group are
+// evaluated.  A pair is emitted from its lowest identical segment only, and
+// only if its V sets and J sets intersect, so each neighbour pair appears once
+// and the pairs are exactly those of the bucket path.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t seg_count(const int16_t *eps_tab, uint32_t NL, uint32_t li) {
+    const int e = eps_tab[(size_t)li * NL + li];
+    return e < 0 ? 1u : (uint32_t)e + 1u;
+}
+
+__device__ __forceinline__ bool seg_bytes_equal(const uint8_t *a, const uint8_t *b, uint32_t n) {
+    uint32_t d = 0;
+    for (uint32_t k = 0; k < n; ++k) d |= (uint32_t)(a[k] ^ b[k]);
+    return d == 0;
+}
+
+__global__ void k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
+                              const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
+                              const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
+                              const int16_t *__restrict__ eps_tab, uint32_t *tab,
+                              uint32_t *cnt, uint32_t *__restrict__ slot_head,
+                              uint32_t *__restrict__ head_slot, uint32_t *__restrict__ islot,
+                              uint64_t mask) {
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t row = urow[u], L = ulen[u], r = urep[u];
+        const uint32_t S = g.in_range(L) ? seg_count(eps_tab, g.NL, L - g.Lmin) : 0u;
+        const uint8_t *sp = seq + seq_off[row];
+        for (uint32_t k = 0; k < 4; ++k) {
+            uint32_t sl = kNone;
+            bool won = false;
+            if (k < S) {
+                const uint32_t lo = k * L / S, hi = (k + 1) * L / S;
+                unsigned long long h = mix64(0x5E6A1F00ull + r, ((unsigned long long)L << 8) | k);
+                unsigned long long word = 0;
+                for (uint32_t i = lo; i < hi; ++i) {
+                    word = (word << 8) | sp[i];
+                    if (((i - lo) & 7) == 7) { h = mix64(h, word); word = 0; }
+                }
+                h = mix64(h, word);
+                sl = (uint32_t)(h & mask);
+                uint32_t it = 0;
+                for (;; ++it) {
+                    if (it > mask || it >= kSpinCap) {
+                        atomicOr(&ctr->error, kErrHashStall);
+                        sl = kNone;
+                        break;
+                    }
+                    uint32_t cur = *((volatile uint32_t *)&tab[sl]);
+                    if (cur == kNone) {
+                        const uint32_t prev = atomicCAS(&tab[sl], kNone, u * 4 + k);
+                        if (prev == kNone) { won = true; break; }
+                        cur = prev;
+                    }
+                    const uint32_t cu = cur >> 2, ck = cur & 3u;
+                    if (ck == k && urep[cu] == r && ulen[cu] == L &&
+                        seg_bytes_equal(seq + seq_off[urow[cu]] + lo, sp + lo, hi - lo))
+                        break;
+                    sl = (sl + 1) & (uint32_t)mask;
+                }
+            }
+            islot[(size_t)u * 4 + k] = sl;
+            // a new key gets the next head index (one atomic per warp)
+            const uint32_t am = __activemask();
+            const uint32_t wm = __ballot_sync(am, won);
+            const uint32_t ld = (uint32_t)__ffs(am) - 1;
+            uint32_t base = 0;
+            if (lane == ld && wm) base = atomicAdd(&ctr->n_heads, (uint32_t)__popc(wm));
+            base = __shfl_sync(am, base, ld);
+            if (won) {
+                const uint32_t hd = base + __popc(wm & ((1u << lane) - 1u));
+                head_slot[hd] = sl;
+                slot_head[sl] = hd;
+            }
+            // one count increment per key among the lanes here together
+            const uint32_t grp = __match_any_sync(am, sl);
+            if (lane == (uint32_t)__ffs(grp) - 1 && sl != kNone) atomicAdd(&cnt[sl], (uint32_t)__popc(grp));
+        }
+    }
+}
+
+// Size of every key's group (0 for a key held by one unique) and the group
+// index of the keys that form bin pairs.
+__global__ void k_join_sizes(Counters *ctr, const uint32_t *__restrict__ head_slot,
+                             const uint32_t *__restrict__ cnt, uint32_t *__restrict__ sizes,
+                             uint32_t *__restrict__ bpidx) {
+    const uint32_t nh = ctr->n_heads;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t h0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); h0 < nh; h0 += stride) {
+        const uint32_t h = h0 + lane;
+        uint32_t c = 0;
+        if (h < nh) c = cnt[head_slot[h]];
+        const bool grp = c >= 2;
+        if (h < nh) sizes[h] = grp ? c : 0u;
+        const uint32_t m = __ballot_sync(0xFFFFFFFFu, grp);
+        uint32_t base = 0;
+        if (lane == 0 && m) base = atomicAdd(&ctr->n_groups, (uint32_t)__popc(m));
+        base = __shfl_sync(0xFFFFFFFFu, base, 0);
+        if (grp) bpidx[h] = base + __popc(m & ((1u << lane) - 1u));
+    }
+}
+
+// Entries: each unique once per segment whose key forms a group; the side
+// record carries the segment index and the unique id.
+template <int RSC>
+__global__ void __launch_bounds__(256)
+k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restrict__ urow,
+            const uint32_t *__restrict__ ulen, const uint8_t *__restrict__ seq,
+            const int64_t *__restrict__ seq_off, const uint8_t *__restrict__ codemap,
+            const int16_t *__restrict__ eps_tab, const uint32_t *__restrict__ islot,
+            const uint64_t *__restrict__ vbits, const uint64_t *__restrict__ jbits,
+            const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ slot_head,
+            const uint32_t *__restrict__ start, uint32_t *__restrict__ cursor,
+            uint32_t *__restrict__ ent_uid, uint4 *__restrict__ ent_rec,
+            uint4 *__restrict__ ent_meta, int planes, uint32_t W, uint64_t cap_entries,
+            uint32_t *err) {
+    __shared__ uint8_t cm[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
+    __syncthreads();
+    const uint32_t nu = ctr->n_uniques;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t row = urow[u], L = ulen[u];
+        if (!g.in_range(L)) continue;
+        const uint32_t S = seg_count(eps_tab, g.NL, L - g.Lmin);
+        uint4 rec[RSC];
+        build_small_record<RSC>(seq + seq_off[row], L, cm, planes, W, rec);
+        for (uint32_t k = 0; k < S; ++k) {
+            const uint32_t sl = islot[(size_t)u * 4 + k];
+            if (sl == kNone || cnt[sl] < 2) continue;
+            const uint32_t h = slot_head[sl];
+            const uint64_t pos = (uint64_t)start[h] + atomicAdd(&cursor[h], 1u);
+            if (pos >= cap_entries) { atomicOr(err, kErrEntryOverflow); continue; }
+            ent_uid[pos] = u;
+            // side record: V bits, J bits with the segment index in the top two bits
+            const uint64_t vb = vbits[(size_t)row * g.VW];
+            const uint32_t jb = (uint32_t)jbits[(size_t)row * g.JW];
+            ent_meta[pos] = make_uint4((uint32_t)vb, (uint32_t)(vb >> 32), jb | (k << 30), u);
+            uint4 *dst = ent_rec + pos * RSC;
+#pragma unroll
+            for (int q = 0; q < RSC; ++q) dst[q] = rec[q];
+        }
+        (void)lane;
+    }
+}
+
+__global__ void k_join_nbp(Counters *ctr) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) ctr->n_binpairs = ctr->n_groups;
+}
+
+// One bin pair (a group against itself) per key held by two or more uniques.
+__global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
+                               const uint32_t *__restrict__ head_slot, const uint32_t *__restrict__ tab,
+                               const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ start,
+                               const uint32_t *__restrict__ bpidx, const uint32_t *__restrict__ ulen,
+                               const int16_t *__restrict__ eps_tab, uint32_t TX, uint64_t cap_bp,
+                               BinPair *__restrict__ out, uint32_t *err) {
+    const uint32_t nh = ctr->n_heads;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += stride) {
+        const uint32_t sl = head_slot[h];
+        const uint32_t c = cnt[sl];
+        if (c < 2) continue;
+        const uint32_t k = bpidx[h];
+        if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); continue; }
+        const uint32_t item = tab[sl];
+        const uint32_t L = ulen[item >> 2];
+        const uint32_t li = L - g.Lmin;
+        BinPair P;
+        P.a_start = start[h]; P.a_n = c; P.b_start = start[h]; P.b_n = c;
+        P.unit_base = 0;
+        P.ncx = (c + TX - 1) / TX;
+        P.la = (uint16_t)L; P.lb = (uint16_t)L;
+        P.v = (uint16_t)(item & 3u);                          // segment of the group
+        P.j = (uint16_t)seg_count(eps_tab, g.NL, li);         // segments of length L
+        P.eps = eps_tab[(size_t)li * g.NL + li];
+        P.same = 1;
+        const uint64_t cost = (uint64_t)c * (c - 1) / 2;
+        P.cls = (uint8_t)(cost ? 63 - __clzll((long long)cost) : 0);
+        P.cost_lo = (uint32_t)min(cost, (uint64_t)0xFFFFFFFFu);
+        out[k] = P;
+    }
+}
 }  // namespace
 
 void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
     BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
+    if (P.join) {
+        const uint64_t heads = (uint64_t)P.join_smax * P.N;
+        cudaMemsetAsync(B.jn_tab, 0xFF, sizeof(uint32_t) * (B.jn_mask + 1), s);
+        cudaMemsetAsync(B.jn_count, 0, sizeof(uint32_t) * (B.jn_mask + 1), s);
+        cudaMemsetAsync(&B.ctr->n_heads, 0, 2 * sizeof(uint32_t), s);   // n_heads, n_groups
+        k_join_insert<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
+                                                          B.seq_off, B.eps_tab, B.jn_tab, B.jn_count,
+                                                          B.jn_slot_head, B.jn_head_slot, B.jn_islot,
+                                                          B.jn_mask);
+        k_join_sizes<<<grid_for(heads), kThreads, 0, s>>>(B.ctr, B.jn_head_slot, B.jn_count, B.jn_start,
+                                                           B.jn_bpidx);
+        scan_u32(B.jn_start, B.jn_start, (uint32_t)heads, &B.ctr->n_heads, &B.ctr->n_entries,
+                 B.scan_part, B.scan_part_cap, s);
+        return;
+    }
     const uint32_t nb = (uint32_t)P.nbins;
     // call groups (the duplicate table is free again once the uniques exist)
     cudaMemsetAsync(B.table, 0xFF, sizeof(uint32_t) * (B.table_mask + 1), s);
@@ -491,6 +707,30 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
 }
 
 void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
+    if (P.join) {
+        BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
+        cudaMemsetAsync(B.jn_cur, 0, sizeof(uint32_t) * (size_t)P.join_smax * P.N, s);
+        const int planes = (int)P.B;
+        auto go = [&](auto kern) {
+            kern<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.seq, B.seq_off,
+                                                     B.codemap, B.eps_tab, B.jn_islot, B.vbits,
+                                                     B.jbits, B.jn_count,
+                                                     B.jn_slot_head, B.jn_start, B.jn_cur, B.ent_uid,
+                                                     B.ent_rec, B.ent_meta, planes, P.W,
+                                                     P.cap_entries, &B.ctr->error);
+        };
+        switch (P.RS / 16) {   // Hamming fast path: 1..8 words of bit planes
+            case 1: go(k_join_fill<1>); break;
+            case 2: go(k_join_fill<2>); break;
+            case 3: go(k_join_fill<3>); break;
+            case 4: go(k_join_fill<4>); break;
+            case 5: go(k_join_fill<5>); break;
+            case 6: go(k_join_fill<6>); break;
+            case 7: go(k_join_fill<7>); break;
+            default: go(k_join_fill<8>); break;
+        }
+        return;
+    }
     BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
     cudaMemsetAsync(B.bin_cursor, 0, sizeof(uint32_t) * P.nbins, s);
     cudaMemsetAsync(B.sig_and, 0xFF, sizeof(unsigned long long) * 2 * P.nbins, s);
@@ -516,6 +756,10 @@ void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
 }
 
 void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s) {
+    if (P.join) {
+        k_join_nbp<<<1, 32, 0, s>>>(B.ctr);
+        return;
+    }
     PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.K, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
     const uint32_t nb = (uint32_t)P.nbins;
     k_binpairs_count<<<grid_for(nb), kThreads, 0, s>>>(nb, pg, B.eps_tab, B.bin_hist, B.sig_and,
@@ -525,6 +769,14 @@ void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s) {
 }
 
 void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
+    if (P.join) {
+        BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
+        const uint64_t heads = (uint64_t)P.join_smax * P.N;
+        k_join_bp_fill<<<grid_for(heads), kThreads, 0, s>>>(
+            g, B.ctr, B.jn_head_slot, B.jn_tab, B.jn_count, B.jn_start, B.jn_bpidx, B.ulen, B.eps_tab, P.TX,
+            P.cap_binpairs, B.bp, &B.ctr->error);
+        return;
+    }
     PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.K, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
     const uint32_t nb = (uint32_t)P.nbins;
     k_binpairs_fill<<<grid_for(nb), kThreads, 0, s>>>(nb, pg, B.eps_tab, B.bin_hist, B.sig_and,

@@ -53,6 +53,9 @@ struct DistArgs {
     const uint4 *meta;               // per entry {sigV lo, sigV hi, sigJ, uid}
     int sig_exact;                   // signatures decide canonicity exactly
     const uint32_t *small_list;      // schedule positions of the small bin pairs
+    // segment join: a hit is a neighbour pair if the V and J sets intersect and
+    // no lower segment is identical (that segment's group emits it)
+    int join;
 };
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -197,6 +200,32 @@ __device__ __forceinline__ void finish(const DistArgs &a, EdgeWriter &ew, uint64
     }
 }
 
+// Segment join with the gene bits in the side records: V and J sets intersect,
+// and no lower segment of the pair is identical, read from the difference
+// words d[w] (bit i of word w: residue 32w+i differs) of the length-L pair
+// split into S segments; k is the group's segment.
+template <int W>
+__device__ __forceinline__ bool join_meta_ok(const uint4 &mx, const uint4 &my, const uint32_t (&d)[W],
+                                             uint32_t L, uint32_t S, uint32_t k) {
+    if (((mx.x & my.x) | (mx.y & my.y)) == 0) return false;
+    if ((mx.z & my.z & 0x3FFFFFFFu) == 0) return false;
+    for (uint32_t kk = 0; kk < k; ++kk) {
+        const uint32_t lo = kk * L / S, hi = (kk + 1) * L / S;
+        uint32_t any = 0;
+#pragma unroll
+        for (int w = 0; w < W; ++w) {
+            const uint32_t a0 = max(lo, 32u * w), a1 = min(hi, 32u * w + 32u);
+            if (a0 < a1) {
+                const uint32_t n = a1 - a0;
+                const uint32_t m = (n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u)) << (a0 - 32u * w);
+                any |= d[w] & m;
+            }
+        }
+        if (any == 0) return false;   // identical (or empty) lower segment: emitted there
+    }
+    return true;
+}
+
 // ---------------------------------------------------------------------------
 // Neighbour hits of one y against the calling lane's x-entries (bit r of `hit`
 // = x-entry xbase + 32*r + lane).  Kept out of line: hits are rare, and the
@@ -228,10 +257,16 @@ __device__ __noinline__ void emit_hits(const DistArgs &a, EdgeWriter &ew, uint32
 // Same, with the entries' side records in shared memory: the canonical test is
 // (sig_x & sig_y) == 0 over the genes below the bin's V and J gene, and the
 // unique ids come with the records, so a hit reads no global memory.
+// In the segment join, the x record is read
+// back (it was loaded for the unit, so from L1) and the y record is in shared
+// memory: the lowest-identical-segment test needs no other memory.
+template <int BP, int W>
 __device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, uint32_t hit,
                                             const uint4 *xm, uint4 ym, uint32_t xbase,
                                             uint32_t ypos, uint32_t same, uint32_t v, uint32_t j,
+                                            const uint4 *xrec, const uint4 *yrec, uint32_t L,
                                             int lane) {
+    constexpr int NW = BP * W, R16 = (NW + 3) / 4;
     uint32_t any = __reduce_or_sync(0xFFFFFFFFu, hit);
     while (any) {
         const int r = __ffs(any) - 1;
@@ -241,7 +276,24 @@ __device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, u
         if (ok && same && ypos <= xpos) ok = false;
         const uint4 m = xm[32 * r + lane];
         if (ok) {
-            if (a.sig_exact) {
+            if (a.join) {
+                uint32_t xw[R16 * 4], yw[R16 * 4];
+                const uint4 *xs = xrec + (size_t)(32u * r + lane) * R16;
+#pragma unroll
+                for (int q = 0; q < R16; ++q) {
+                    const uint4 p = __ldg(xs + q), o = yrec[q];
+                    xw[4 * q] = p.x; xw[4 * q + 1] = p.y; xw[4 * q + 2] = p.z; xw[4 * q + 3] = p.w;
+                    yw[4 * q] = o.x; yw[4 * q + 1] = o.y; yw[4 * q + 2] = o.z; yw[4 * q + 3] = o.w;
+                }
+                uint32_t d[W];
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    d[w] = xw[w] ^ yw[w];
+#pragma unroll
+                    for (int q = 1; q < BP; ++q) d[w] |= xw[q * W + w] ^ yw[q * W + w];
+                }
+                ok = join_meta_ok<W>(m, ym, d, L, j, v);
+            } else if (a.sig_exact) {
                 ok = ((m.x & ym.x) | (m.y & ym.y) | (m.z & ym.z)) == 0;
             } else {
                 const uint32_t rx = a.urow[m.w], ry = a.urow[ym.w];
@@ -319,11 +371,13 @@ __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew,
         uint32_t i = 0, j = 0;
         if (act) small_pair(p, same, n, i, j);
         uint32_t sc;
+        uint32_t dw[W];
         if (W == 1) {
             uint32_t d = __shfl_sync(0xFFFFFFFFu, xr[0], i) ^ __shfl_sync(0xFFFFFFFFu, yr[0], j);
 #pragma unroll
             for (int q = 1; q < BP; ++q)
                 d |= __shfl_sync(0xFFFFFFFFu, xr[q], i) ^ __shfl_sync(0xFFFFFFFFu, yr[q], j);
+            dw[0] = d;
             sc = EM == 2 ? d : (EM == 1 ? (d & (d - 1u)) : (uint32_t)__popc(d));
         } else {
             uint32_t dist = 0;
@@ -334,6 +388,7 @@ __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew,
                 for (int q = 1; q < BP; ++q)
                     d |= __shfl_sync(0xFFFFFFFFu, xr[q * W + w], i) ^
                          __shfl_sync(0xFFFFFFFFu, yr[q * W + w], j);
+                dw[w] = d;
                 dist += __popc(d);
             }
             sc = dist;
@@ -345,7 +400,9 @@ __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew,
             if (ok) {
                 mx = __ldg(a.meta + P.a_start + i);
                 my = __ldg(a.meta + ystart + j);
-                if (a.sig_exact) {
+                if (a.join) {
+                    ok = join_meta_ok<W>(mx, my, dw, P.la, P.j, P.v);
+                } else if (a.sig_exact) {
                     ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
                 } else {
                     const uint32_t rx = a.urow[mx.w], ry = a.urow[my.w];
@@ -367,15 +424,19 @@ constexpr int kHitQ = 8;   // queued (y, hits) records per lane
 constexpr uint32_t kLevQ = 256;          // queued candidate pairs per warp (Levenshtein)
 constexpr uint32_t kOff = 0x40000000u;   // score of a masked x-entry (never a hit)
 
+template <int BP, int W>
 __device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, const uint32_t *q,
                                         uint32_t qn, const uint4 *xm, const uint4 *ym,
-                                        uint32_t xbase, uint32_t ypos0, uint32_t same,
-                                        uint32_t v, uint32_t j, int lane) {
+                                        const uint4 *sy, const Unit &U, uint32_t ypos0,
+                                        uint32_t same, int lane) {
+    constexpr int R16 = (BP * W + 3) / 4;
+    const uint4 *xrec = a.rec + (size_t)(U.P.a_start + U.xbase) * R16;
     const uint32_t kmax = __reduce_max_sync(0xFFFFFFFFu, qn);
     for (uint32_t k = 0; k < kmax; ++k) {
         const uint32_t e = k < qn ? q[k * 32 + lane] : 0u;
         const uint32_t hit = e & 0xFFu, t = e >> 8;
-        emit_hits_meta(a, ew, hit, xm, ym[t], xbase, ypos0 + t, same, v, j, lane);
+        emit_hits_meta<BP, W>(a, ew, hit, xm, ym[t], U.xbase, ypos0 + t, same, U.P.v, U.P.j,
+                              xrec, sy + t * R16, U.P.la, lane);
     }
 }
 
@@ -466,8 +527,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
         auto drain_if_full = [&](uint32_t room) {
             if (__any_sync(0xFFFFFFFFu, qn + room > (uint32_t)kHitQ)) {
                 __syncwarp();
-                drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same,
-                           U.P.v, U.P.j, lane);
+                drain_hits<BP, W>(a, ew, shq, qn, sxm, sym, sy, U, U.ybase + yb, same, lane);
                 qn = 0;
                 __syncwarp();
             }
@@ -507,8 +567,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
         }
         if (__any_sync(0xFFFFFFFFu, qn)) {
             __syncwarp();
-            drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same,
-                       U.P.v, U.P.j, lane);
+            drain_hits<BP, W>(a, ew, shq, qn, sxm, sym, sy, U, U.ybase + yb, same, lane);
         }
         __syncwarp();
     }
@@ -921,8 +980,9 @@ static DistArgs make_args(const Plan &P, const Buffers &B) {
     a.bp_cycles = B.bp_cycles;   // set only while profiling
     a.bp_hits = B.bp_hits;
     a.meta = B.ent_meta;
-    a.sig_exact = P.sig_exact ? 1 : 0;
+    a.sig_exact = (P.sig_exact && !P.join) ? 1 : 0;
     a.small_list = B.bp_small;
+    a.join = P.join ? 1 : 0;
     return a;
 }
 
