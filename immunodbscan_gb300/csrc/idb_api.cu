@@ -13,6 +13,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -433,9 +434,11 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
     P.big_group = 64;
     P.sig_exact = P.Gv <= 64 && P.Gj <= 32;
     // Hamming with a small eps at every length: candidate pairs by segment join
-    // (the side records then carry the V bits and the J bits with the segment)
+    // (the side records then carry the V bits and the J bits with the segment;
+    // a key holds the repertoire in 24 bits and the table at most 2^31 slots)
     P.join = pl.allow_join && P.hamming && P.fast && emax_same <= kJoinMaxEps &&
-             P.Gv <= 64 && P.Gj <= 30;
+             P.Gv <= 64 && P.Gj <= 30 && P.R < (1u << 24) - 1 &&
+             2ull * (uint64_t)(emax_same + 1) * P.N <= (1ull << 30);
     P.join_smax = P.join ? (uint32_t)std::max(1, emax_same + 1) : 1u;
     P.nbins = (uint64_t)P.R * P.Gv * P.Gj * P.NL * P.K;
     if (P.nbins >= (1ull << 31))
@@ -502,9 +505,7 @@ idb_status alloc_fixed(Pipeline &pl) {
         // keys: at most join_smax per unique; the table at load <= 1/2
         const uint64_t heads = (uint64_t)P.join_smax * N;
         const uint64_t jcap = next_pow2(std::max<uint64_t>(2 * heads, 1024));
-        if (jcap > (1ull << 31) || 4 * N > 0xFFFFFFF0ull)
-            return fail(IDB_ERR_UNSUPPORTED, "segment join table too large");
-        TRY(ensure(c, bJnTab, 4 * jcap));
+        TRY(ensure(c, bJnTab, 8 * jcap));
         TRY(ensure(c, bJnCount, 4 * jcap));
         TRY(ensure(c, bJnSlotHead, 4 * jcap));
         TRY(ensure(c, bJnISlot, 16 * N1));
@@ -512,7 +513,7 @@ idb_status alloc_fixed(Pipeline &pl) {
         TRY(ensure(c, bJnStart, 4 * (heads + 1)));
         TRY(ensure(c, bJnCur, 4 * (heads + 1)));
         TRY(ensure(c, bJnBpIdx, 4 * (heads + 1)));
-        B.jn_tab = ptr<uint32_t>(c, bJnTab);
+        B.jn_tab = ptr<unsigned long long>(c, bJnTab);
         B.jn_count = ptr<uint32_t>(c, bJnCount);
         B.jn_slot_head = ptr<uint32_t>(c, bJnSlotHead);
         B.jn_mask = jcap - 1;
@@ -771,6 +772,23 @@ idb_status get_ctx(idb_context **pc) {
 
 namespace idb {
 void set_last_error(const char *msg) { g_err = msg ? msg : ""; }
+
+int resident_blocks(const void *kern, int threads, size_t smem) {
+    struct Entry { const void *k; int threads; size_t smem; int dev; int blocks; };
+    static std::mutex mu;
+    static std::vector<Entry> cache;
+    int d = 0;
+    cudaGetDevice(&d);
+    std::lock_guard<std::mutex> lock(mu);
+    for (const Entry &e : cache)
+        if (e.k == kern && e.threads == threads && e.smem == smem && e.dev == d) return e.blocks;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess)
+        per_sm = 0;
+    if (per_sm <= 0) per_sm = 1;
+    cache.push_back(Entry{kern, threads, smem, d, per_sm});
+    return per_sm;
+}
 
 int sm_count() {
     static thread_local int dev = -1, n = 0;

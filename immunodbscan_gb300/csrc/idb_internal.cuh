@@ -19,6 +19,9 @@ constexpr uint32_t kSpinCap = 1u << 22; // bound of every device-side retry loop
 // Bin pairs with at most kSmallSide entries on each side (Hamming fast path) are
 // evaluated pair-parallel: lanes take pairs, records travel by shuffles.
 constexpr uint32_t kSmallSide = 32;
+// A bin paired with itself with at most kTinySide entries is a tiny bin pair:
+// one lane takes all of its pairs, 32 tiny bin pairs per warp at once.
+constexpr uint32_t kTinySide = 8;
 // Hamming with eps <= kJoinMaxEps for every length uses the segment join: two
 // equal-length sequences within eps agree exactly on one of eps+1 segments.
 constexpr int kJoinMaxEps = 3;
@@ -110,7 +113,8 @@ struct Counters {
     uint32_t n_core_edges;       // neighbour pairs with both ends core
     uint32_t n_heads;            // segment join: distinct segment keys
     uint32_t n_groups;           // segment join: keys held by two or more uniques
-    uint32_t pad2[2];
+    uint32_t n_tiny;             // tiny bin pairs (one lane each), listed from the small list's end
+    uint32_t tiny_cursor;        // their work queue head
 };
 
 // One bucket ("bin") holds the uniques of one (repertoire, V gene, J gene,
@@ -203,7 +207,8 @@ struct Buffers {
     uint32_t *bp_units = nullptr;                   // [cap_binpairs+1]
     uint32_t *bp_small = nullptr;                   // [cap_binpairs] schedule positions of small bin pairs
     // segment join: table of (unique, segment) keys and the groups they form
-    uint32_t *jn_tab = nullptr, *jn_count = nullptr, *jn_slot_head = nullptr;   // [jn_mask+1]
+    unsigned long long *jn_tab = nullptr;           // [jn_mask+1] segment keys
+    uint32_t *jn_count = nullptr, *jn_slot_head = nullptr;   // [jn_mask+1]
     uint64_t jn_mask = 0;
     uint32_t *jn_islot = nullptr;                   // [4*N] slot of (unique, segment)
     uint32_t *jn_head_slot = nullptr;               // [join_smax*N] slot of each key
@@ -268,5 +273,22 @@ void launch_to_bf16(const float *p, void *q, cudaStream_t s);
 
 int sm_count();
 const char *distance_variant_name(const Plan &P);
+
+// Blocks of a kernel resident on one SM at once (threads per block, dynamic
+// shared memory), from the occupancy calculator; cached per kernel and device.
+int resident_blocks(const void *kern, int threads, size_t smem);
+
+// Grid of a grid-stride kernel over n items: one block per `threads` items, at
+// most one full wave of resident blocks, so that no block starts in a second
+// wave after the first has drained.
+template <typename F>
+inline int grid_wave(F *kern, uint64_t n, int threads, size_t smem = 0) {
+    uint64_t g = (n + (uint64_t)threads - 1) / (uint64_t)threads;
+    const uint64_t cap = (uint64_t)sm_count() *
+                         (uint64_t)resident_blocks(reinterpret_cast<const void *>(kern), threads, smem);
+    if (g > cap) g = cap;
+    if (g < 1) g = 1;
+    return (int)g;
+}
 
 }  // namespace idb

@@ -160,32 +160,39 @@ __global__ void k_bin_hist(BinGeom g, const Counters *__restrict__ ctr,
 // equality of bytes.
 // The record of one unique (fast paths: at most NR 16-byte words): bit planes
 // (Hamming) or code bytes (Levenshtein), residues read 4 at a time.
+// Bit planes of one sequence (L <= 128): bit i of wd[p][w] is bit p of the
+// code of residue 32w + i; positions past L keep code 0.  Residues are read 4
+// at a time.
+__device__ __forceinline__ void build_planes(const uint8_t *s, uint32_t L, const uint8_t *cm,
+                                             uint32_t (&wd)[5][4]) {
+#pragma unroll
+    for (int p = 0; p < 5; ++p)
+#pragma unroll
+        for (int w = 0; w < 4; ++w) wd[p][w] = 0;
+    GlobalReader rd(s, L);
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        for (uint32_t k = 0; k < 8; ++k) {
+            const uint32_t i0 = 32u * w + 4u * k;
+            if (i0 >= L) break;
+            const uint32_t v = rd.next();
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const uint32_t c = i0 + b < L ? (uint32_t)cm[(v >> (8 * b)) & 0xFFu] : 0u;
+#pragma unroll
+                for (int p = 0; p < 5; ++p) wd[p][w] |= ((c >> p) & 1u) << (4 * k + b);
+            }
+        }
+    }
+}
+
 template <int NR>
 __device__ __forceinline__ void build_small_record(const uint8_t *s, uint32_t L,
                                                    const uint8_t *cm, int planes, uint32_t W,
                                                    uint4 (&rec)[NR]) {
     if (planes > 0) {
         uint32_t wd[5][4];
-#pragma unroll
-        for (int p = 0; p < 5; ++p)
-#pragma unroll
-            for (int w = 0; w < 4; ++w) wd[p][w] = 0;
-        // residues read 4 at a time; positions past L keep code 0 (padding)
-        GlobalReader rd(s, L);
-#pragma unroll
-        for (int w = 0; w < 4; ++w) {
-            for (uint32_t k = 0; k < 8; ++k) {
-                const uint32_t i0 = 32u * w + 4u * k;
-                if (i0 >= L) break;
-                const uint32_t v = rd.next();
-#pragma unroll
-                for (int b = 0; b < 4; ++b) {
-                    const uint32_t c = i0 + b < L ? (uint32_t)cm[(v >> (8 * b)) & 0xFFu] : 0u;
-#pragma unroll
-                    for (int p = 0; p < 5; ++p) wd[p][w] |= ((c >> p) & 1u) << (4 * k + b);
-                }
-            }
-        }
+        build_planes(s, L, cm, wd);
         // layout: word p*W + w
         uint32_t flat[4 * NR];
 #pragma unroll
@@ -429,7 +436,8 @@ __global__ void k_cls_scatter(const Counters *__restrict__ ctr, const BinPair *_
                               uint32_t *__restrict__ cursor, BinPair *__restrict__ out,
                               uint32_t *__restrict__ units, uint32_t TX, uint32_t TY, uint32_t q,
                               int small_mode, uint32_t *__restrict__ small_list,
-                              uint32_t *__restrict__ n_small) {
+                              uint32_t *__restrict__ n_small, uint32_t *__restrict__ n_tiny,
+                              uint32_t small_cap) {
     const uint32_t n = ctr->n_binpairs;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
@@ -452,12 +460,21 @@ __global__ void k_cls_scatter(const Counters *__restrict__ ctr, const BinPair *_
         uint64_t nu;
         if (small_mode && P.a_n <= kSmallSide && (P.same || P.b_n <= kSmallSide)) {
             nu = 0;                               // pair-parallel path, no tiled units
+            // small bin pairs from the front of the list, tiny ones from its end
+            const bool tiny = P.same && P.a_n <= kTinySide;
             const uint32_t am = __activemask();
+            const uint32_t tm = __ballot_sync(am, tiny), sm = am & ~tm;
             const uint32_t ld = (uint32_t)__ffs(am) - 1;
-            uint32_t b0 = 0;
-            if (lane == ld) b0 = atomicAdd(n_small, (uint32_t)__popc(am));
+            uint32_t b0 = 0, t0 = 0;
+            if (lane == ld) {
+                if (sm) b0 = atomicAdd(n_small, (uint32_t)__popc(sm));
+                if (tm) t0 = atomicAdd(n_tiny, (uint32_t)__popc(tm));
+            }
             b0 = __shfl_sync(am, b0, ld);
-            small_list[b0 + __popc(am & ((1u << lane) - 1u))] = pos;
+            t0 = __shfl_sync(am, t0, ld);
+            const uint32_t below = (1u << lane) - 1u;
+            if (tiny) small_list[small_cap - 1u - (t0 + __popc(tm & below))] = pos;
+            else small_list[b0 + __popc(sm & below)] = pos;
         } else if (P.same) {
             const uint32_t ncy = (P.a_n + TY - 1) / TY;
             nu = tri_units(P.ncx, ncy, q);
@@ -494,56 +511,67 @@ __device__ __forceinline__ uint32_t seg_count(const int16_t *eps_tab, uint32_t N
     return e < 0 ? 1u : (uint32_t)e + 1u;
 }
 
-__device__ __forceinline__ bool seg_bytes_equal(const uint8_t *a, const uint8_t *b, uint32_t n) {
-    uint32_t d = 0;
-    for (uint32_t k = 0; k < n; ++k) d |= (uint32_t)(a[k] ^ b[k]);
-    return d == 0;
+// Key of segment k of a unique: repertoire (24 bits), length (8), segment (2)
+// and 30 bits of a hash of the segment's residue codes.  Codes are a bijection
+// of the bytes, so identical segments always share a key; two different
+// segments that share one only make a group larger (the distance kernel
+// checks that segment k is identical before it emits a pair).
+__device__ __forceinline__ unsigned long long seg_key(const uint32_t (&wd)[5][4], uint32_t r,
+                                                      uint32_t L, uint32_t k, uint32_t lo,
+                                                      uint32_t hi) {
+    unsigned long long h = mix64(0x5E6A1F00ull, ((unsigned long long)r << 16) | (L << 2) | k);
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const uint32_t a0 = max(lo, 32u * w), a1 = min(hi, 32u * w + 32u);
+        if (a0 < a1) {
+            const uint32_t n = a1 - a0;
+            const uint32_t m = (n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u)) << (a0 - 32u * w);
+            unsigned long long acc = 0;
+#pragma unroll
+            for (int p = 0; p < 5; ++p) acc = acc * 0x9E3779B97F4A7C15ull + (wd[p][w] & m);
+            h = mix64(h, acc);
+        }
+    }
+    return ((unsigned long long)r << 40) | ((unsigned long long)L << 32) |
+           ((unsigned long long)k << 30) | (h >> 34);
 }
 
-__global__ void k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
-                              const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
-                              const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
-                              const int16_t *__restrict__ eps_tab, uint32_t *tab,
-                              uint32_t *cnt, uint32_t *__restrict__ slot_head,
-                              uint32_t *__restrict__ head_slot, uint32_t *__restrict__ islot,
-                              uint64_t mask) {
+__global__ void __launch_bounds__(256)
+k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
+              const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
+              const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
+              const uint8_t *__restrict__ codemap, const int16_t *__restrict__ eps_tab,
+              unsigned long long *tab, uint32_t *cnt, uint32_t *__restrict__ slot_head,
+              uint32_t *__restrict__ head_slot, uint32_t *__restrict__ islot, uint64_t mask) {
+    __shared__ uint8_t cm[256];
+    for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
+    __syncthreads();
     const uint32_t nu = ctr->n_uniques;
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
         const uint32_t row = urow[u], L = ulen[u], r = urep[u];
         const uint32_t S = g.in_range(L) ? seg_count(eps_tab, g.NL, L - g.Lmin) : 0u;
-        const uint8_t *sp = seq + seq_off[row];
+        uint32_t wd[5][4];
+        build_planes(seq + seq_off[row], S ? L : 0u, cm, wd);
         for (uint32_t k = 0; k < 4; ++k) {
             uint32_t sl = kNone;
             bool won = false;
             if (k < S) {
-                const uint32_t lo = k * L / S, hi = (k + 1) * L / S;
-                unsigned long long h = mix64(0x5E6A1F00ull + r, ((unsigned long long)L << 8) | k);
-                unsigned long long word = 0;
-                for (uint32_t i = lo; i < hi; ++i) {
-                    word = (word << 8) | sp[i];
-                    if (((i - lo) & 7) == 7) { h = mix64(h, word); word = 0; }
-                }
-                h = mix64(h, word);
-                sl = (uint32_t)(h & mask);
-                uint32_t it = 0;
-                for (;; ++it) {
+                const unsigned long long key = seg_key(wd, r, L, k, k * L / S, (k + 1) * L / S);
+                sl = (uint32_t)(mix64(key, 0x51ull) & mask);
+                for (uint32_t it = 0;; ++it) {
                     if (it > mask || it >= kSpinCap) {
                         atomicOr(&ctr->error, kErrHashStall);
                         sl = kNone;
                         break;
                     }
-                    uint32_t cur = *((volatile uint32_t *)&tab[sl]);
-                    if (cur == kNone) {
-                        const uint32_t prev = atomicCAS(&tab[sl], kNone, u * 4 + k);
-                        if (prev == kNone) { won = true; break; }
-                        cur = prev;
+                    unsigned long long cur = *((volatile unsigned long long *)&tab[sl]);
+                    if (cur == ~0ull) {
+                        cur = atomicCAS(&tab[sl], ~0ull, key);
+                        if (cur == ~0ull) { won = true; break; }
                     }
-                    const uint32_t cu = cur >> 2, ck = cur & 3u;
-                    if (ck == k && urep[cu] == r && ulen[cu] == L &&
-                        seg_bytes_equal(seq + seq_off[urow[cu]] + lo, sp + lo, hi - lo))
-                        break;
+                    if (cur == key) break;
                     sl = (sl + 1) & (uint32_t)mask;
                 }
             }
@@ -640,10 +668,10 @@ __global__ void k_join_nbp(Counters *ctr) {
 
 // One bin pair (a group against itself) per key held by two or more uniques.
 __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
-                               const uint32_t *__restrict__ head_slot, const uint32_t *__restrict__ tab,
+                               const uint32_t *__restrict__ head_slot,
+                               const unsigned long long *__restrict__ tab,
                                const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ start,
-                               const uint32_t *__restrict__ bpidx, const uint32_t *__restrict__ ulen,
-                               const int16_t *__restrict__ eps_tab, uint32_t TX, uint64_t cap_bp,
+                               const uint32_t *__restrict__ bpidx, const int16_t *__restrict__ eps_tab, uint32_t TX, uint64_t cap_bp,
                                BinPair *__restrict__ out, uint32_t *err) {
     const uint32_t nh = ctr->n_heads;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -653,15 +681,15 @@ __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
         if (c < 2) continue;
         const uint32_t k = bpidx[h];
         if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); continue; }
-        const uint32_t item = tab[sl];
-        const uint32_t L = ulen[item >> 2];
+        const unsigned long long key = tab[sl];
+        const uint32_t L = (uint32_t)(key >> 32) & 0xFFu;
         const uint32_t li = L - g.Lmin;
         BinPair P;
         P.a_start = start[h]; P.a_n = c; P.b_start = start[h]; P.b_n = c;
         P.unit_base = 0;
         P.ncx = (c + TX - 1) / TX;
         P.la = (uint16_t)L; P.lb = (uint16_t)L;
-        P.v = (uint16_t)(item & 3u);                          // segment of the group
+        P.v = (uint16_t)((key >> 30) & 3u);                   // segment of the group
         P.j = (uint16_t)seg_count(eps_tab, g.NL, li);         // segments of length L
         P.eps = eps_tab[(size_t)li * g.NL + li];
         P.same = 1;
@@ -677,14 +705,15 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
     BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
     if (P.join) {
         const uint64_t heads = (uint64_t)P.join_smax * P.N;
-        cudaMemsetAsync(B.jn_tab, 0xFF, sizeof(uint32_t) * (B.jn_mask + 1), s);
+        cudaMemsetAsync(B.jn_tab, 0xFF, sizeof(unsigned long long) * (B.jn_mask + 1), s);
         cudaMemsetAsync(B.jn_count, 0, sizeof(uint32_t) * (B.jn_mask + 1), s);
         cudaMemsetAsync(&B.ctr->n_heads, 0, 2 * sizeof(uint32_t), s);   // n_heads, n_groups
-        k_join_insert<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
-                                                          B.seq_off, B.eps_tab, B.jn_tab, B.jn_count,
+        k_join_insert<<<grid_wave(k_join_insert, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
+                                                          B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
+                                                          B.jn_count,
                                                           B.jn_slot_head, B.jn_head_slot, B.jn_islot,
                                                           B.jn_mask);
-        k_join_sizes<<<grid_for(heads), kThreads, 0, s>>>(B.ctr, B.jn_head_slot, B.jn_count, B.jn_start,
+        k_join_sizes<<<grid_wave(k_join_sizes, heads, kThreads), kThreads, 0, s>>>(B.ctr, B.jn_head_slot, B.jn_count, B.jn_start,
                                                            B.jn_bpidx);
         scan_u32(B.jn_start, B.jn_start, (uint32_t)heads, &B.ctr->n_heads, &B.ctr->n_entries,
                  B.scan_part, B.scan_part_cap, s);
@@ -694,13 +723,13 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
     // call groups (the duplicate table is free again once the uniques exist)
     cudaMemsetAsync(B.table, 0xFF, sizeof(uint32_t) * (B.table_mask + 1), s);
     cudaMemsetAsync(B.tcount, 0, sizeof(uint32_t) * (B.table_mask + 1), s);
-    k_group_insert<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.vbits,
+    k_group_insert<<<grid_wave(k_group_insert, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.vbits,
                                                        B.jbits, B.table, B.tcount, B.slot,
                                                        B.table_mask);
-    k_group_class<<<grid_for(P.N), kThreads, 0, s>>>(B.ctr, B.slot, B.tcount, P.K, P.big_group,
+    k_group_class<<<grid_wave(k_group_class, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.slot, B.tcount, P.K, P.big_group,
                                                       B.uclass);
     cudaMemsetAsync(B.bin_hist, 0, sizeof(uint32_t) * (P.nbins + 1), s);
-    k_bin_hist<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.uclass,
+    k_bin_hist<<<grid_wave(k_bin_hist, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.uclass,
                                                     B.vbits, B.jbits, B.bin_hist);
     scan_u32(B.bin_hist, B.bin_hist, nb + 1, nullptr, &B.ctr->n_entries, B.scan_part,
              B.scan_part_cap, s);
@@ -712,7 +741,7 @@ void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
         cudaMemsetAsync(B.jn_cur, 0, sizeof(uint32_t) * (size_t)P.join_smax * P.N, s);
         const int planes = (int)P.B;
         auto go = [&](auto kern) {
-            kern<<<grid_for(P.N), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.seq, B.seq_off,
+            kern<<<grid_wave(kern, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.seq, B.seq_off,
                                                      B.codemap, B.eps_tab, B.jn_islot, B.vbits,
                                                      B.jbits, B.jn_count,
                                                      B.jn_slot_head, B.jn_start, B.jn_cur, B.ent_uid,
@@ -737,7 +766,7 @@ void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
     const int planes = (P.fast && P.hamming) ? (int)P.B : 0;
     const uint32_t rs16 = P.RS / 16;
     auto go = [&](auto kern) {
-        kern<<<grid_for(P.N), kThreads, 0, s>>>(
+        kern<<<grid_wave(kern, P.N, kThreads), kThreads, 0, s>>>(
             g, B.ctr, B.urow, B.ulen, B.urep, B.uclass, B.sig_and, B.vbits, B.jbits, B.seq, B.seq_off,
             B.codemap, B.bin_hist, B.bin_cursor, B.ent_uid, B.ent_rec, B.ent_meta, rs16, planes, P.W,
             P.cap_entries, &B.ctr->error);
@@ -772,8 +801,8 @@ void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
     if (P.join) {
         BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
         const uint64_t heads = (uint64_t)P.join_smax * P.N;
-        k_join_bp_fill<<<grid_for(heads), kThreads, 0, s>>>(
-            g, B.ctr, B.jn_head_slot, B.jn_tab, B.jn_count, B.jn_start, B.jn_bpidx, B.ulen, B.eps_tab, P.TX,
+        k_join_bp_fill<<<grid_wave(k_join_bp_fill, heads, kThreads), kThreads, 0, s>>>(
+            g, B.ctr, B.jn_head_slot, B.jn_tab, B.jn_count, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX,
             P.cap_binpairs, B.bp, &B.ctr->error);
         return;
     }
@@ -791,9 +820,11 @@ void launch_schedule(const Plan &P, const Buffers &B, cudaStream_t s) {
     k_cls_hist<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(B.ctr, B.bp, pred, B.cls_hist);
     scan_u32(B.cls_hist, B.cls_hist, 64, nullptr, nullptr, B.scan_part, B.scan_part_cap, s);
     cudaMemsetAsync(&B.ctr->n_small, 0, 2 * sizeof(uint32_t), s);   // n_small, small_cursor
+    cudaMemsetAsync(&B.ctr->n_tiny, 0, 2 * sizeof(uint32_t), s);    // n_tiny, tiny_cursor
     k_cls_scatter<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(
         B.ctr, B.bp, pred, B.cls_hist, B.cls_hist + 64, B.bp_sorted, B.bp_units, P.TX, P.TY, q,
-        (P.fast && P.hamming) ? 1 : 0, B.bp_small, &B.ctr->n_small);
+        (P.fast && P.hamming) ? 1 : 0, B.bp_small, &B.ctr->n_small, &B.ctr->n_tiny,
+        (uint32_t)P.cap_binpairs + 1u);
     scan_u32(B.bp_units, B.bp_units, (uint32_t)P.cap_binpairs, &B.ctr->n_binpairs,
              &B.ctr->n_units, B.scan_part, B.scan_part_cap, s);
     k_set_unit_base<<<grid_for(P.cap_binpairs), kThreads, 0, s>>>(B.ctr, B.bp_sorted, B.bp_units);

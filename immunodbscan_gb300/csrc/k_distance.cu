@@ -52,7 +52,9 @@ struct DistArgs {
     uint32_t *bp_hits;
     const uint4 *meta;               // per entry {sigV lo, sigV hi, sigJ, uid}
     int sig_exact;                   // signatures decide canonicity exactly
-    const uint32_t *small_list;      // schedule positions of the small bin pairs
+    const uint32_t *small_list;      // schedule positions of the small bin pairs (from the
+                                     // front) and of the tiny ones (from small_cap - 1 down)
+    uint32_t small_cap;
     // segment join: a hit is a neighbour pair if the V and J sets intersect and
     // no lower segment is identical (that segment's group emits it)
     int join;
@@ -201,15 +203,17 @@ __device__ __forceinline__ void finish(const DistArgs &a, EdgeWriter &ew, uint64
 }
 
 // Segment join with the gene bits in the side records: V and J sets intersect,
-// and no lower segment of the pair is identical, read from the difference
-// words d[w] (bit i of word w: residue 32w+i differs) of the length-L pair
-// split into S segments; k is the group's segment.
+// segment k (the group's) is identical and no lower segment is, read from the
+// difference words d[w] (bit i of word w: residue 32w+i differs) of the
+// length-L pair split into S segments.  Groups are keyed by a hash of the
+// segment, so the test on segment k itself keeps a shared key of two different
+// segments from emitting a pair twice.
 template <int W>
 __device__ __forceinline__ bool join_meta_ok(const uint4 &mx, const uint4 &my, const uint32_t (&d)[W],
                                              uint32_t L, uint32_t S, uint32_t k) {
     if (((mx.x & my.x) | (mx.y & my.y)) == 0) return false;
     if ((mx.z & my.z & 0x3FFFFFFFu) == 0) return false;
-    for (uint32_t kk = 0; kk < k; ++kk) {
+    for (uint32_t kk = 0; kk <= k; ++kk) {
         const uint32_t lo = kk * L / S, hi = (kk + 1) * L / S;
         uint32_t any = 0;
 #pragma unroll
@@ -221,7 +225,8 @@ __device__ __forceinline__ bool join_meta_ok(const uint4 &mx, const uint4 &my, c
                 any |= d[w] & m;
             }
         }
-        if (any == 0) return false;   // identical (or empty) lower segment: emitted there
+        if (kk < k && any == 0) return false;   // identical (or empty) lower segment: emitted there
+        if (kk == k && any != 0) return false;  // segment k differs: a shared key only
     }
     return true;
 }
@@ -257,16 +262,10 @@ __device__ __noinline__ void emit_hits(const DistArgs &a, EdgeWriter &ew, uint32
 // Same, with the entries' side records in shared memory: the canonical test is
 // (sig_x & sig_y) == 0 over the genes below the bin's V and J gene, and the
 // unique ids come with the records, so a hit reads no global memory.
-// In the segment join, the x record is read
-// back (it was loaded for the unit, so from L1) and the y record is in shared
-// memory: the lowest-identical-segment test needs no other memory.
-template <int BP, int W>
 __device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, uint32_t hit,
                                             const uint4 *xm, uint4 ym, uint32_t xbase,
                                             uint32_t ypos, uint32_t same, uint32_t v, uint32_t j,
-                                            const uint4 *xrec, const uint4 *yrec, uint32_t L,
                                             int lane) {
-    constexpr int NW = BP * W, R16 = (NW + 3) / 4;
     uint32_t any = __reduce_or_sync(0xFFFFFFFFu, hit);
     while (any) {
         const int r = __ffs(any) - 1;
@@ -277,22 +276,7 @@ __device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, u
         const uint4 m = xm[32 * r + lane];
         if (ok) {
             if (a.join) {
-                uint32_t xw[R16 * 4], yw[R16 * 4];
-                const uint4 *xs = xrec + (size_t)(32u * r + lane) * R16;
-#pragma unroll
-                for (int q = 0; q < R16; ++q) {
-                    const uint4 p = __ldg(xs + q), o = yrec[q];
-                    xw[4 * q] = p.x; xw[4 * q + 1] = p.y; xw[4 * q + 2] = p.z; xw[4 * q + 3] = p.w;
-                    yw[4 * q] = o.x; yw[4 * q + 1] = o.y; yw[4 * q + 2] = o.z; yw[4 * q + 3] = o.w;
-                }
-                uint32_t d[W];
-#pragma unroll
-                for (int w = 0; w < W; ++w) {
-                    d[w] = xw[w] ^ yw[w];
-#pragma unroll
-                    for (int q = 1; q < BP; ++q) d[w] |= xw[q * W + w] ^ yw[q * W + w];
-                }
-                ok = join_meta_ok<W>(m, ym, d, L, j, v);
+                // segment join: checked when the hit was queued
             } else if (a.sig_exact) {
                 ok = ((m.x & ym.x) | (m.y & ym.y) | (m.z & ym.z)) == 0;
             } else {
@@ -321,28 +305,16 @@ __device__ __forceinline__ void small_pair(uint32_t p, bool same, uint32_t n, ui
     }
 }
 
-// Next small bin pair for this warp (schedule position), false when none is left.
-__device__ __forceinline__ bool next_small(const DistArgs &a, uint32_t n_small, int lane,
-                                           uint32_t &idx) {
-    uint32_t s = 0;
-    if (lane == 0) s = atomicAdd(&a.ctr->small_cursor, 1u);
-    s = __shfl_sync(0xFFFFFFFFu, s, 0);
-    if (s >= n_small) return false;
-    idx = a.small_list[s];
-    return true;
-}
-
 // A small bin pair (at most kSmallSide entries a side), pair-parallel: lane l
 // holds entry l of each side; each round the lanes take 32 pairs and fetch
 // the two records by shuffles.  Canonicity of a hit is decided from the side
 // records (global loads: hits are rare).
 template <int BP, int W, int EM>
-__device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew, uint32_t idx,
-                                              int lane, uint64_t &pairs) {
+__device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew, const BinPair &P,
+                                              uint32_t idx, int lane, uint64_t &pairs) {
     constexpr int NW = BP * W;
     constexpr int R16 = (NW + 3) / 4;
     const long long t0 = a.bp_cycles ? clock64() : 0;
-    const BinPair P = a.bp[idx];
     const bool same = P.same != 0;
     const uint32_t n = P.a_n, m = same ? P.a_n : P.b_n;
     const uint32_t ystart = same ? P.a_start : P.b_start;
@@ -417,6 +389,149 @@ __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew,
         atomicAdd(&a.bp_cycles[idx], (unsigned long long)(clock64() - t0));
 }
 
+// Small bin pairs of a warp: the warp claims kSmallBatch schedule positions
+// with one atomic, each lane loads one of their bin pairs, and while one bin
+// pair is scored the next one's records are prefetched into L1 (a small bin
+// pair is otherwise a chain of dependent loads: position, bin pair, records).
+constexpr uint32_t kSmallBatch = 16;
+
+__device__ __forceinline__ BinPair shfl_binpair(const BinPair &p, int src) {
+    static_assert(sizeof(BinPair) % 4 == 0, "BinPair words");
+    constexpr int NWD = (int)(sizeof(BinPair) / 4);
+    uint32_t w[NWD];
+    memcpy(w, &p, sizeof(BinPair));
+#pragma unroll
+    for (int k = 0; k < NWD; ++k) w[k] = __shfl_sync(0xFFFFFFFFu, w[k], src);
+    BinPair q;
+    memcpy(&q, w, sizeof(BinPair));
+    return q;
+}
+
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+    asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+template <int BP, int W, int EM>
+__device__ __forceinline__ void hamming_small_all(const DistArgs &a, EdgeWriter &ew, int lane,
+                                                  uint64_t &pairs) {
+    constexpr int R16 = (BP * W + 3) / 4;
+    const uint32_t n_small = a.ctr->n_small;
+    for (;;) {
+        uint32_t s0 = 0;
+        if (lane == 0) s0 = atomicAdd(&a.ctr->small_cursor, kSmallBatch);
+        s0 = __shfl_sync(0xFFFFFFFFu, s0, 0);
+        if (s0 >= n_small) break;
+        const uint32_t cnt = min(kSmallBatch, n_small - s0);
+        uint32_t myidx = 0;
+        BinPair myP;
+        memset(&myP, 0, sizeof(BinPair));
+        if ((uint32_t)lane < cnt) {
+            myidx = a.small_list[s0 + lane];
+            myP = a.bp[myidx];
+        }
+        for (uint32_t g = 0; g < cnt; ++g) {
+            if (g + 1 < cnt) {
+                const uint32_t na = __shfl_sync(0xFFFFFFFFu, myP.a_start, g + 1);
+                const uint32_t nn = __shfl_sync(0xFFFFFFFFu, myP.a_n, g + 1);
+                const uint32_t nb = __shfl_sync(0xFFFFFFFFu, myP.b_start, g + 1);
+                const uint32_t nm = __shfl_sync(0xFFFFFFFFu, myP.b_n, g + 1);
+                const uint32_t ns = __shfl_sync(0xFFFFFFFFu, (uint32_t)myP.same, g + 1);
+                if ((uint32_t)lane < nn) prefetch_l1(a.rec + (size_t)(na + lane) * R16);
+                if (!ns && (uint32_t)lane < nm) prefetch_l1(a.rec + (size_t)(nb + lane) * R16);
+            }
+            const BinPair P = shfl_binpair(myP, (int)g);
+            hamming_small<BP, W, EM>(a, ew, P, __shfl_sync(0xFFFFFFFFu, myidx, g), lane, pairs);
+        }
+    }
+}
+
+// Tiny bin pairs (a bin with itself, at most kTinySide entries): lane l takes
+// every pair of the l-th bin pair of a batch of 32, so the latency of loading
+// a bin pair and its records is paid once per 32 bin pairs.  Records are read
+// per pair from L1 (a tiny bin's records share one or two cache lines).
+template <int BP, int W, int EM>
+__device__ __forceinline__ void hamming_tiny_all(const DistArgs &a, EdgeWriter &ew, int lane,
+                                                 uint64_t &pairs) {
+    constexpr int NW = BP * W;
+    constexpr int R16 = (NW + 3) / 4;
+    const uint32_t n_tiny = a.ctr->n_tiny;
+    for (;;) {
+        uint32_t s0 = 0;
+        if (lane == 0) s0 = atomicAdd(&a.ctr->tiny_cursor, 32u);
+        s0 = __shfl_sync(0xFFFFFFFFu, s0, 0);
+        if (s0 >= n_tiny) break;
+        const long long t0 = a.bp_cycles ? clock64() : 0;
+        const bool act = s0 + (uint32_t)lane < n_tiny;
+        uint32_t idx = 0;
+        BinPair P;
+        memset(&P, 0, sizeof(BinPair));
+        if (act) {
+            idx = a.small_list[a.small_cap - 1u - (s0 + (uint32_t)lane)];
+            P = a.bp[idx];
+        }
+        const uint32_t n = P.a_n;
+        const uint32_t np = (EM == 0 && P.eps < 0) ? 0u : n * (n - 1) / 2;
+        pairs += n * (n - 1) / 2;
+        const uint32_t thr = EM == 0 ? (uint32_t)max((int)P.eps, 0) : 0u;
+        const uint4 *rec = a.rec + (size_t)P.a_start * R16;
+        const uint32_t maxp = __reduce_max_sync(0xFFFFFFFFu, np);
+        for (uint32_t p = 0; p < maxp; ++p) {
+            bool hit = false;
+            uint32_t i = 0, j = 0;
+            uint32_t dw[W];
+#pragma unroll
+            for (int w = 0; w < W; ++w) dw[w] = 0;
+            if (p < np) {
+                small_pair(p, true, n, i, j);
+                uint32_t xw[4 * R16], yw[4 * R16];
+#pragma unroll
+                for (int q = 0; q < R16; ++q) {
+                    const uint4 u = __ldg(rec + (size_t)i * R16 + q), v = __ldg(rec + (size_t)j * R16 + q);
+                    xw[4 * q] = u.x; xw[4 * q + 1] = u.y; xw[4 * q + 2] = u.z; xw[4 * q + 3] = u.w;
+                    yw[4 * q] = v.x; yw[4 * q + 1] = v.y; yw[4 * q + 2] = v.z; yw[4 * q + 3] = v.w;
+                }
+                uint32_t dist = 0;
+#pragma unroll
+                for (int w = 0; w < W; ++w) {
+                    uint32_t d = xw[w] ^ yw[w];
+#pragma unroll
+                    for (int q = 1; q < BP; ++q) d |= xw[q * W + w] ^ yw[q * W + w];
+                    dw[w] = d;
+                    dist += __popc(d);
+                }
+                const uint32_t sc = EM == 2 ? dw[0] : (EM == 1 ? (dw[0] & (dw[0] - 1u)) : dist);
+                hit = sc <= thr;
+            }
+            if (__any_sync(0xFFFFFFFFu, hit)) {
+                bool ok = hit;
+                uint4 mx = make_uint4(0, 0, 0, 0), my = mx;
+                if (ok) {
+                    mx = __ldg(a.meta + P.a_start + i);
+                    my = __ldg(a.meta + P.a_start + j);
+                    if (a.join) {
+                        ok = join_meta_ok<W>(mx, my, dw, P.la, P.j, P.v);
+                    } else if (a.sig_exact) {
+                        ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
+                    } else {
+                        const uint32_t rx = a.urow[mx.w], ry = a.urow[my.w];
+                        ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)P.v &&
+                             lowest_common(a.jbits, a.JW, rx, ry) == (int)P.j;
+                    }
+                }
+                ew.append(a, lane, ok, min(mx.w, my.w), max(mx.w, my.w));
+            }
+        }
+        if (a.bp_cycles) {
+            // the batch's cycles, shared out by pairs (every lane takes part in
+            // the reduction; lanes past the list's end hold n = 0)
+            const uint32_t mine = n * (n - 1) / 2;
+            const uint32_t tot = __reduce_add_sync(0xFFFFFFFFu, mine);
+            const unsigned long long dt = (unsigned long long)(clock64() - t0);
+            if (act) atomicAdd(&a.bp_cycles[idx], dt * mine / (tot ? tot : 1u));
+        }
+    }
+}
+
 // Deferred hits: the Hamming loop only records, per lane, (y index in the staged
 // chunk, hit bits) in a small shared-memory queue; the queue is drained here when
 // a lane's queue is full or the chunk ends, with every lane taking part.
@@ -424,19 +539,15 @@ constexpr int kHitQ = 8;   // queued (y, hits) records per lane
 constexpr uint32_t kLevQ = 256;          // queued candidate pairs per warp (Levenshtein)
 constexpr uint32_t kOff = 0x40000000u;   // score of a masked x-entry (never a hit)
 
-template <int BP, int W>
 __device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, const uint32_t *q,
                                         uint32_t qn, const uint4 *xm, const uint4 *ym,
-                                        const uint4 *sy, const Unit &U, uint32_t ypos0,
-                                        uint32_t same, int lane) {
-    constexpr int R16 = (BP * W + 3) / 4;
-    const uint4 *xrec = a.rec + (size_t)(U.P.a_start + U.xbase) * R16;
+                                        uint32_t xbase, uint32_t ypos0, uint32_t same,
+                                        uint32_t v, uint32_t j, int lane) {
     const uint32_t kmax = __reduce_max_sync(0xFFFFFFFFu, qn);
     for (uint32_t k = 0; k < kmax; ++k) {
         const uint32_t e = k < qn ? q[k * 32 + lane] : 0u;
         const uint32_t hit = e & 0xFFu, t = e >> 8;
-        emit_hits_meta<BP, W>(a, ew, hit, xm, ym[t], U.xbase, ypos0 + t, same, U.P.v, U.P.j,
-                              xrec, sy + t * R16, U.P.la, lane);
+        emit_hits_meta(a, ew, hit, xm, ym[t], xbase, ypos0 + t, same, v, j, lane);
     }
 }
 
@@ -448,10 +559,11 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
                                                const uint32_t (&x)[RX][BP * W],
                                                const uint32_t (&vmask)[RX], uint32_t valid,
                                                uint4 *sy, uint4 *sym, uint4 *sxm, uint32_t *shq,
-                                               int lane) {
+                                               const uint32_t *sseg, int lane) {
     constexpr int NW = BP * W;
     constexpr int R16 = (NW + 3) / 4;
     const uint32_t rb = (U.nx + 31) >> 5;   // r-blocks holding entries
+    const uint32_t jk = U.P.v;              // segment join: the group's segment
     // a pair is a hit iff its score <= thr (score: d&(d-1) for eps 1, d for
     // eps 0, the popcount otherwise); masked entries score >= kOff
     const uint32_t thr = EM == 0 ? (uint32_t)max(U.P.eps, 0) : 0u;
@@ -515,7 +627,29 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
             for (int r = 0; r < RX; ++r)
                 if (sc[r] <= thr) {
                     bool ok = true;
-                    if (a.sig_exact) {
+                    if (a.join) {
+                        // segment join: V and J sets intersect, the group's
+                        // segment is identical and no lower one is (masks of
+                        // segment kk, word w at sseg[4 kk + w])
+                        const uint4 m = sxm[32 * r + lane];
+                        ok = ((m.x & ym.x) | (m.y & ym.y)) != 0 && (m.z & ym.z & 0x3FFFFFFFu) != 0;
+                        if (ok) {
+                            const uint32_t *yw = reinterpret_cast<const uint32_t *>(sy + t * R16);
+                            uint32_t dk = 0, l0 = 0, l1 = 0, l2 = 0;
+#pragma unroll
+                            for (int w = 0; w < W; ++w) {
+                                uint32_t d = x[r][w] ^ yw[w];
+#pragma unroll
+                                for (int p = 1; p < BP; ++p) d |= x[r][p * W + w] ^ yw[p * W + w];
+                                dk |= d & sseg[4 * jk + w];
+                                l0 |= d & sseg[w];
+                                l1 |= d & sseg[4 + w];
+                                l2 |= d & sseg[8 + w];
+                            }
+                            ok = dk == 0 && (jk < 1 || l0 != 0) && (jk < 2 || l1 != 0) &&
+                                 (jk < 3 || l2 != 0);
+                        }
+                    } else if (a.sig_exact) {
                         const uint4 m = sxm[32 * r + lane];
                         ok = ((m.x & ym.x) | (m.y & ym.y) | (m.z & ym.z)) == 0;
                     }
@@ -527,7 +661,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
         auto drain_if_full = [&](uint32_t room) {
             if (__any_sync(0xFFFFFFFFu, qn + room > (uint32_t)kHitQ)) {
                 __syncwarp();
-                drain_hits<BP, W>(a, ew, shq, qn, sxm, sym, sy, U, U.ybase + yb, same, lane);
+                drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same, U.P.v, U.P.j, lane);
                 qn = 0;
                 __syncwarp();
             }
@@ -567,7 +701,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
         }
         if (__any_sync(0xFFFFFFFFu, qn)) {
             __syncwarp();
-            drain_hits<BP, W>(a, ew, shq, qn, sxm, sym, sy, U, U.ybase + yb, same, lane);
+            drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same, U.P.v, U.P.j, lane);
         }
         __syncwarp();
     }
@@ -586,6 +720,7 @@ k_hamming(DistArgs a) {
     __shared__ uint4 sym[kWarps][kYB];            // y side records
     __shared__ uint4 sxm[kWarps][32 * RX];        // x side records
     __shared__ uint32_t shq[kWarps][kHitQ * 32];  // deferred hits
+    __shared__ uint32_t sseg[kWarps][16];         // segment join: masks of segment kk, word w
     static_assert(RX <= 8 && kYB < (1 << 24), "hit record layout");
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t n_units = a.ctr->n_units, n_bp = a.ctr->n_binpairs;
@@ -615,18 +750,31 @@ k_hamming(DistArgs a) {
             if (ok) pairs += unit_pairs(U, U.xbase + xi);
             sxm[wid][xi] = __ldg(a.meta + U.P.a_start + U.xbase + (ok ? xi : 0));
         }
+        if (a.join && lane < 16) {
+            // segment kk = lane / 4 of length la split into j segments, word w = lane % 4
+            const uint32_t kk = (uint32_t)lane >> 2, w = (uint32_t)lane & 3u;
+            const uint32_t L = U.P.la, S = U.P.j;
+            const uint32_t lo = kk < S ? kk * L / S : 0u, hi = kk < S ? (kk + 1) * L / S : 0u;
+            const uint32_t a0 = max(lo, 32u * w), a1 = min(hi, 32u * w + 32u);
+            uint32_t m = 0;
+            if (a0 < a1) {
+                const uint32_t n = a1 - a0;
+                m = (n >= 32 ? 0xFFFFFFFFu : ((1u << n) - 1u)) << (a0 - 32u * w);
+            }
+            sseg[wid][lane] = m;
+        }
+        __syncwarp();
         if (U.nx == (uint32_t)(32 * RX))
             hamming_unit_y<BP, W, RX, EM, true>(a, ew, U, x, vmask, valid, sy[wid], sym[wid], sxm[wid],
-                                                shq[wid], lane);
+                                                shq[wid], sseg[wid], lane);
         else
             hamming_unit_y<BP, W, RX, EM, false>(a, ew, U, x, vmask, valid, sy[wid], sym[wid],
-                                                 sxm[wid], shq[wid], lane);
+                                                 sxm[wid], shq[wid], sseg[wid], lane);
         log_unit(a, U, lane);
     }
     // then the small bin pairs (they also fill the tail of the tiled work)
-    const uint32_t n_small = a.ctr->n_small;
-    uint32_t sidx = 0;
-    while (next_small(a, n_small, lane, sidx)) hamming_small<BP, W, EM>(a, ew, sidx, lane, pairs);
+    hamming_small_all<BP, W, EM>(a, ew, lane, pairs);
+    hamming_tiny_all<BP, W, EM>(a, ew, lane, pairs);
     finish(a, ew, pairs, lane);
 }
 
@@ -918,9 +1066,13 @@ k_count_admissible(DistArgs a) {
             cnt += canonical(a, U.P, ux, uy);
         }
     }
-    const uint32_t n_small = a.ctr->n_small;
-    uint32_t sidx = 0;
-    while (next_small(a, n_small, lane, sidx)) {
+    const uint32_t n_small = a.ctr->n_small, n_tiny = a.ctr->n_tiny;
+    for (;;) {
+        uint32_t s = 0;
+        if (lane == 0) s = atomicAdd(&a.ctr->small_cursor, 1u);
+        s = __shfl_sync(0xFFFFFFFFu, s, 0);
+        if (s >= n_small + n_tiny) break;
+        const uint32_t sidx = s < n_small ? a.small_list[s] : a.small_list[a.small_cap - 1u - (s - n_small)];
         const BinPair P = a.bp[sidx];
         if (P.eps < 0) continue;
         const bool same = P.same != 0;
@@ -982,6 +1134,7 @@ static DistArgs make_args(const Plan &P, const Buffers &B) {
     a.meta = B.ent_meta;
     a.sig_exact = (P.sig_exact && !P.join) ? 1 : 0;
     a.small_list = B.bp_small;
+    a.small_cap = (uint32_t)P.cap_binpairs + 1u;
     a.join = P.join ? 1 : 0;
     return a;
 }
@@ -990,6 +1143,7 @@ void launch_count_admissible(const Plan &P, const Buffers &B, cudaStream_t s) {
     DistArgs a = make_args(P, B);
     cudaMemsetAsync(&B.ctr->unit_cursor, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(&B.ctr->small_cursor, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(&B.ctr->tiny_cursor, 0, sizeof(uint32_t), s);
     run(k_count_admissible, a, 0, 0, s);
 }
 
@@ -1002,6 +1156,7 @@ void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s) 
     DistArgs a = make_args(P, B);
     cudaMemsetAsync(&B.ctr->unit_cursor, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(&B.ctr->small_cursor, 0, sizeof(uint32_t), s);
+    cudaMemsetAsync(&B.ctr->tiny_cursor, 0, sizeof(uint32_t), s);
     if (!P.fast) {
         if (P.hamming) run(k_generic<true>, a, 0, grid, s);
         else run(k_generic<false>, a, 0, grid, s);

@@ -870,7 +870,7 @@ void launch_check_plan(const Plan &P, const Buffers &B, cudaStream_t s) {
 }
 
 void launch_survey(const Plan &P, const Buffers &B, cudaStream_t s) {
-    k_survey<<<grid_for(P.N), kThreads, 0, s>>>(B.seq, B.seq_off, P.N, B.ctr);
+    k_survey<<<grid_wave(k_survey, P.N, kThreads), kThreads, 0, s>>>(B.seq, B.seq_off, P.N, B.ctr);
 }
 
 void launch_const_strings(uint8_t *blob, int64_t *off, uint32_t N, cudaStream_t s) {
@@ -896,9 +896,8 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     // 1. collapse the column by string
     const size_t smem_slots = kGbWarps * ((cs_slice_bytes() + 15) / 16 * 16);
     static_assert(kGbWarps * ((cs_slice_bytes() + 15) / 16 * 16) <= 48 * 1024, "default smem limit");
-    const int grid_rows = (int)std::min<uint64_t>(((uint64_t)P.N + kGbRows * kGbWarps - 1) /
-                                                      (kGbRows * kGbWarps),
-                                                  (uint64_t)sm_count() * 8);
+    const int grid_rows = grid_wave(k_call_slots, ((uint64_t)P.N + kGbRows - 1) / kGbRows * 32,
+                                    kGbWarps * 32, smem_slots);
     cudaMemsetAsync(B.call_tab, 0xFF, sizeof(unsigned long long) * ((size_t)B.call_mask + 1), s);
     cudaMemsetAsync(B.call_ntodo, 0, sizeof(uint32_t), s);
     k_call_slots<<<grid_rows > 0 ? grid_rows : 1, kGbWarps * 32, smem_slots, s>>>(
@@ -917,7 +916,7 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     k_gene_bits<<<grid > 0 ? grid : 1, kGbWarps * 32, smem, s>>>(
         calls, off, B.call_todo, B.call_ntodo, P.N, genes, goff, G, GW, tab, gm, bits);
     // 3. everybody else
-    k_call_copy<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.call_ref, B.call_tab, B.call_mask, GW,
+    k_call_copy<<<grid_wave(k_call_copy, P.N, kThreads), kThreads, 0, s>>>(P.N, B.call_ref, B.call_tab, B.call_mask, GW,
                                                     bits);
 }
 
@@ -930,14 +929,14 @@ void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s) {
     a.mask = B.table_mask; a.ctr = B.ctr;
     cudaMemsetAsync(B.table, 0xFF, sizeof(uint32_t) * (B.table_mask + 1), s);
     cudaMemsetAsync(B.tcount, 0, sizeof(uint32_t) * (B.table_mask + 1), s);
-    k_dedupe_insert<<<grid_for(P.N), kThreads, 0, s>>>(a);
-    k_dedupe_final<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.slot, B.table, B.rep_row, B.flag);
+    k_dedupe_insert<<<grid_wave(k_dedupe_insert, P.N, kThreads), kThreads, 0, s>>>(a);
+    k_dedupe_final<<<grid_wave(k_dedupe_final, P.N, kThreads), kThreads, 0, s>>>(P.N, B.slot, B.table, B.rep_row, B.flag);
 }
 
 void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s) {
     scan_u32(B.flag, B.uid_of_row, P.N, nullptr, &B.ctr->n_uniques, B.scan_part,
              B.scan_part_cap, s);
-    k_uniques<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.seq_off, B.rep_off, P.R, B.slot, B.tcount,
+    k_uniques<<<grid_wave(k_uniques, P.N, kThreads), kThreads, 0, s>>>(P.N, B.seq_off, B.rep_off, P.R, B.slot, B.tcount,
                                                    B.rep_row, B.uid_of_row, B.urow, B.ucopies,
                                                    B.ulen, B.urep, B.row2uid);
     k_uid_first<<<(P.R + 1 + 255) / 256, 256, 0, s>>>(P.N, P.R, B.rep_off, B.uid_of_row, B.ctr,

@@ -262,34 +262,33 @@ __global__ void k_uniques_out(const Counters *__restrict__ ctr, const uint32_t *
 
 void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s) {
     const uint64_t ecap = P.cap_edges;
-    const int ge = grid_for(ecap);
     const int gu = grid_for(P.N);
     cudaMemsetAsync(B.deg, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
     cudaMemsetAsync(B.gcur, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
-    k_graph_init<<<gu, kThreads, 0, s>>>(B.ctr, B.ucopies, B.cnt, B.parent, B.bmin);
-    k_count<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucopies, B.cnt);
-    k_core<<<gu, kThreads, 0, s>>>(B.ctr, B.ctr, B.cnt, P.min_pts, B.ucore);
+    k_graph_init<<<grid_wave(k_graph_init, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ucopies, B.cnt, B.parent, B.bmin);
+    k_count<<<grid_wave(k_count, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucopies, B.cnt);
+    k_core<<<grid_wave(k_core, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ctr, B.cnt, P.min_pts, B.ucore);
     // unions, and the degrees of the border CSR (count / scan / fill)
-    k_union<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.parent, B.deg);
+    k_union<<<grid_wave(k_union, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.parent, B.deg);
     scan_u32(B.deg, B.goff, P.N + 1, nullptr, nullptr, B.scan_part, B.scan_part_cap, s);
-    k_fill_adj<<<ge, kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.goff, B.gcur, B.adj);
-    k_border<<<gu, kThreads, 0, s>>>(B.ctr, B.goff, B.adj, B.ucore, B.bmin);
+    k_fill_adj<<<grid_wave(k_fill_adj, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.goff, B.gcur, B.adj);
+    k_border<<<grid_wave(k_border, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.goff, B.adj, B.ucore, B.bmin);
     if (trees) {
         cudaMemsetAsync(B.depth_hist, 0, sizeof(uint32_t) * (kDepthMax + 1), s);
         k_depth<<<gu, kThreads, 0, s>>>(P.N, B.row2uid, B.urow, B.ucore, B.bmin, B.parent,
                                          B.depth_hist);
     }
     cudaMemsetAsync(B.rootflag, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
-    k_compress<<<gu, kThreads, 0, s>>>(B.ctr, B.ucore, B.parent, B.rootflag);
+    k_compress<<<grid_wave(k_compress, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ucore, B.parent, B.rootflag);
     scan_u32(B.rootflag, B.rootflag, P.N + 1, nullptr, &B.ctr->n_clusters, B.scan_part,
              B.scan_part_cap, s);
-    k_labels<<<gu, kThreads, 0, s>>>(B.ctr, B.ucore, B.parent, B.bmin, B.rootflag, B.urep,
+    k_labels<<<grid_wave(k_labels, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ucore, B.parent, B.bmin, B.rootflag, B.urep,
                                       B.uid_first, B.cnt);
 }
 
 void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s) {
     const int gu = grid_for(P.N);
-    k_rows_out<<<gu, kThreads, 0, s>>>(P.N, P.min_pts, B.row2uid, B.urow, B.ucopies, B.ucore,
+    k_rows_out<<<grid_wave(k_rows_out, P.N, kThreads), kThreads, 0, s>>>(P.N, P.min_pts, B.row2uid, B.urow, B.ucopies, B.ucore,
                                         B.cnt, B.clone_id, B.core, B.copies, B.ctr);
     if (B.uniques) k_uniques_out<<<gu, kThreads, 0, s>>>(B.ctr, B.urow, B.uniques);
 }

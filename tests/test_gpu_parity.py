@@ -154,6 +154,30 @@ def test_generic_long(gpu_ctx, hamming):
     assert_same(g, o, w, "generic long")
 
 
+@pytest.mark.parametrize("eps", [0, 1, 2, 3])
+@pytest.mark.parametrize("lo,hi", [(1, 7), (6, 24), (40, 70)])
+def test_segment_join(gpu_ctx, eps, lo, hi):
+    """Hamming with eps <= 3 at every length: candidates come from the segment
+    join.  Short sequences (fewer residues than segments: empty segments),
+    identical sequences under different gene calls (identical in every
+    segment, emitted from the lowest), disjoint V or J sets (rejected at the
+    hit) and a small alphabet (large groups) against the oracle."""
+    rng = np.random.default_rng(100 * eps + lo)
+    w0 = _random_workload(rng, 3000, lo, hi, list(b"ACGT"), True, eps, 2, n_fam=120)
+    seqs = [w0.seq(i) for i in range(w0.n)]
+    seqs += [seqs[int(i)] for i in rng.integers(0, len(seqs), size=600)]
+    vg = [b"IGHV%d*" % g for g in range(1, 9)]
+    jg = [b"IGHJ%d*" % g for g in range(1, 4)]
+    vc = [b"IGHV%d*01" % (1 + rng.integers(0, 8)) for _ in seqs]
+    jc = [b"IGHJ%d*02, or IGHJ%d*01" % (1 + rng.integers(0, 3), 1 + rng.integers(0, 3))
+          for _ in seqs]
+    w = synth.from_strings(seqs, vc, jc, vg, jg, abs_eps=eps, min_pts=2, use_hamming=True)
+    g = cluster_workload(w, gpu_ctx)
+    o = oracle.cluster(w)
+    assert_same(g, o, w, f"segment join eps={eps} L={lo}-{hi}")
+    assert g.stats.neighbour_pairs == o.neighbour_pairs
+
+
 def test_nucleotide_two_planes(gpu_ctx):
     w = synth.workload(1, scale=0.02)
     w.use_hamming = True
