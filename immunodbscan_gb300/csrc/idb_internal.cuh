@@ -87,6 +87,29 @@ struct GlobalReader {
 };
 #endif
 
+// Bytes [32c, 32c + 32) of a string p[0..L) as 8 little-endian words, bytes
+// past L zero.  The aligned 4-byte words that hold those bytes are read with
+// independent loads (all in flight at once), then shifted into place.
+__device__ __forceinline__ void load_chunk32(const uint8_t *p, uint32_t L, uint32_t c,
+                                             uint32_t (&w)[8]) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(p) + 32u * c;
+    const uint32_t sh = (uint32_t)(a & 3u);
+    const uint32_t *gw = reinterpret_cast<const uint32_t *>(a - sh);
+    const uint32_t rem = L > 32u * c ? min(L - 32u * c, 32u) : 0u;
+    const uint32_t nw = (sh + rem + 3u) >> 2;
+    uint32_t v[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) v[k] = (uint32_t)k < nw ? __ldg(gw + k) : 0u;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        uint32_t o = __funnelshift_r(v[k], v[k + 1], 8u * sh);
+        const uint32_t b = 4u * (uint32_t)k;
+        if (b >= rem) o = 0u;
+        else if (rem - b < 4u) o &= (1u << (8u * (rem - b))) - 1u;
+        w[k] = o;
+    }
+}
+
 // Device-resident counters of one clustering call (one struct, zeroed first).
 struct Counters {
     uint32_t lmax, lmin;

@@ -169,13 +169,15 @@ __device__ __forceinline__ void build_planes(const uint8_t *s, uint32_t L, const
     for (int p = 0; p < 5; ++p)
 #pragma unroll
         for (int w = 0; w < 4; ++w) wd[p][w] = 0;
-    GlobalReader rd(s, L);
 #pragma unroll
     for (int w = 0; w < 4; ++w) {
-        for (uint32_t k = 0; k < 8; ++k) {
+        if (32u * w >= L) break;
+        uint32_t cw[8];
+        load_chunk32(s, L, (uint32_t)w, cw);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
             const uint32_t i0 = 32u * w + 4u * k;
-            if (i0 >= L) break;
-            const uint32_t v = rd.next();
+            const uint32_t v = cw[k];
 #pragma unroll
             for (int b = 0; b < 4; ++b) {
                 const uint32_t c = i0 + b < L ? (uint32_t)cm[(v >> (8 * b)) & 0xFFu] : 0u;
@@ -536,17 +538,40 @@ __device__ __forceinline__ unsigned long long seg_key(const uint32_t (&wd)[5][4]
            ((unsigned long long)k << 30) | (h >> 34);
 }
 
+// Slots of the join table in use: about 1.5 slots per possible key (join_smax
+// per unique), a power of two, at most the allocation.  The allocation is sized
+// for every row being unique; the uniques are counted on the device, so the
+// table a call probes (and clears) is the smaller one they need.
+__device__ __forceinline__ uint32_t join_mask(uint32_t nu, uint32_t smax, uint64_t cap_mask) {
+    const uint64_t want = max((3ull * smax * nu + 1) / 2, 1024ull);
+    uint64_t c = 1024;
+    while (c < want) c <<= 1;
+    return (uint32_t)min(c - 1, cap_mask);
+}
+
+__global__ void k_join_clear(const Counters *__restrict__ ctr, uint32_t smax, uint64_t cap_mask,
+                             unsigned long long *__restrict__ tab, uint32_t *__restrict__ cnt) {
+    const uint32_t n = join_mask(ctr->n_uniques, smax, cap_mask) + 1u;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        tab[i] = ~0ull;
+        cnt[i] = 0u;
+    }
+}
+
 __global__ void __launch_bounds__(256)
 k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
               const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
               const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
               const uint8_t *__restrict__ codemap, const int16_t *__restrict__ eps_tab,
               unsigned long long *tab, uint32_t *cnt, uint32_t *__restrict__ slot_head,
-              uint32_t *__restrict__ head_slot, uint32_t *__restrict__ islot, uint64_t mask) {
+              uint32_t *__restrict__ head_slot, uint32_t *__restrict__ islot, uint32_t smax,
+              uint64_t cap_mask) {
     __shared__ uint8_t cm[256];
     for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
     __syncthreads();
     const uint32_t nu = ctr->n_uniques;
+    const uint32_t mask = join_mask(nu, smax, cap_mask);
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
@@ -705,14 +730,14 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
     BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
     if (P.join) {
         const uint64_t heads = (uint64_t)P.join_smax * P.N;
-        cudaMemsetAsync(B.jn_tab, 0xFF, sizeof(unsigned long long) * (B.jn_mask + 1), s);
-        cudaMemsetAsync(B.jn_count, 0, sizeof(uint32_t) * (B.jn_mask + 1), s);
+        k_join_clear<<<grid_wave(k_join_clear, B.jn_mask + 1, kThreads), kThreads, 0, s>>>(
+            B.ctr, P.join_smax, B.jn_mask, B.jn_tab, B.jn_count);
         cudaMemsetAsync(&B.ctr->n_heads, 0, 2 * sizeof(uint32_t), s);   // n_heads, n_groups
         k_join_insert<<<grid_wave(k_join_insert, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
                                                           B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
                                                           B.jn_count,
                                                           B.jn_slot_head, B.jn_head_slot, B.jn_islot,
-                                                          B.jn_mask);
+                                                          P.join_smax, B.jn_mask);
         k_join_sizes<<<grid_wave(k_join_sizes, heads, kThreads), kThreads, 0, s>>>(B.ctr, B.jn_head_slot, B.jn_count, B.jn_start,
                                                            B.jn_bpidx);
         scan_u32(B.jn_start, B.jn_start, (uint32_t)heads, &B.ctr->n_heads, &B.ctr->n_entries,
