@@ -24,7 +24,10 @@ constexpr uint32_t kSmallSide = 32;
 constexpr uint32_t kTinySide = 8;
 // Hamming with eps <= kJoinMaxEps for every length uses the segment join: two
 // equal-length sequences within eps agree exactly on one of eps+1 segments.
-constexpr int kJoinMaxEps = 3;
+// At eps 3 the quarter-length segments make groups large enough that the
+// buckets evaluate their pairs faster (64 repertoires, 1M rows: 2.92 against
+// 3.09 ms per call; eps 1: 1.25 against 0.99 ms for the join).
+constexpr int kJoinMaxEps = 2;
 constexpr int kMlpIn = 16;              // learned scheduler: features per bin pair
 constexpr int kMlpHidden = 64;          // two hidden layers of 64
 constexpr int kMlpParams = kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +

@@ -157,11 +157,12 @@ def test_generic_long(gpu_ctx, hamming):
 @pytest.mark.parametrize("eps", [0, 1, 2, 3])
 @pytest.mark.parametrize("lo,hi", [(1, 7), (6, 24), (40, 70)])
 def test_segment_join(gpu_ctx, eps, lo, hi):
-    """Hamming with eps <= 3 at every length: candidates come from the segment
-    join.  Short sequences (fewer residues than segments: empty segments),
-    identical sequences under different gene calls (identical in every
-    segment, emitted from the lowest), disjoint V or J sets (rejected at the
-    hit) and a small alphabet (large groups) against the oracle."""
+    """Hamming with eps <= 2 at every length: candidates come from the segment
+    join (eps 3: the buckets, same answers).  Short sequences (fewer residues
+    than segments: empty segments), identical sequences under different gene
+    calls (identical in every segment, emitted from the lowest), disjoint V or
+    J sets (rejected at the hit) and a small alphabet (large groups) against
+    the oracle."""
     rng = np.random.default_rng(100 * eps + lo)
     w0 = _random_workload(rng, 3000, lo, hi, list(b"ACGT"), True, eps, 2, n_fam=120)
     seqs = [w0.seq(i) for i in range(w0.n)]
