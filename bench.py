@@ -372,6 +372,7 @@ def main():
                                    "static (heavy-first by pair count)"),
                       "tile": {"rx": shape[0], "ty": shape[1], "source": "autotuner"}},
            "seq_per_s": world * n / (step_ms * 1e-3), "admissible_pairs": admissible,
+           "candidates": "segment join" if last.candidates == 1 else "buckets (every admissible pair)",
            "pairs_evaluated": int(last.pairs_evaluated),
            "neighbour_pairs": int(last.neighbour_pairs), "n_uniques": int(last.n_uniques),
            "n_clusters": int(last.n_clusters), "gpu_launches": int(r["launches"]),
@@ -422,6 +423,8 @@ def main():
                        "work_unit": "pair" if w.use_hamming else "pair-column (text residue)",
                        "work_units": int(last.pairs_evaluated if w.use_hamming else last.lev_columns),
                        "kernel_ms": t_dist * 1e3,
+                       "hit_fraction": (float(last.neighbour_pairs) / float(last.pairs_evaluated)
+                                        if w.use_hamming and last.pairs_evaluated else None),
                        "peak_source": "measured: idb_diag_int_peak (lop3/add chains, all SMs)"}
 
     # graph / union-find / border / renumber phases against HBM bandwidth: the

@@ -55,7 +55,7 @@ class Stats(C.Structure):
                 ("neighbour_pairs", C.c_uint64), ("n_entries", C.c_uint64), ("n_units", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_distance", C.c_double), ("ms_phase", C.c_double * 8),
                 ("kernel_launches", C.c_uint32), ("core_edges", C.c_uint32),
-                ("lev_columns", C.c_uint64)]
+                ("lev_columns", C.c_uint64), ("candidates", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class Output(C.Structure):

@@ -689,6 +689,7 @@ idb_status fill_stats(Pipeline &pl, idb_stats *st) {
     st->n_units = h.n_units;
     st->lev_columns = h.lev_columns;
     st->core_edges = h.n_core_edges;
+    st->candidates = pl.P.join ? 1u : 0u;
     if (pl.timing) {
         phase_times(h, st);
         st->ms_total = h.stamp[5] > h.stamp[0] ? 1e-6 * (double)(h.stamp[5] - h.stamp[0]) : 0.0;
@@ -984,6 +985,7 @@ idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
         stats->n_units = h.n_units;
         stats->lev_columns = h.lev_columns;
         stats->core_edges = h.n_core_edges;
+        stats->candidates = c->plan.join ? 1u : 0u;
         float ms = 0;
         CU(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
         stats->ms_total = ms;

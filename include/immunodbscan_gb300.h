@@ -106,6 +106,10 @@ typedef struct idb_stats {
     uint32_t kernel_launches;  /* kernels launched (graph replays)                 */
     uint32_t core_edges;       /* neighbour pairs with both ends core              */
     uint64_t lev_columns;      /* text columns consumed by live Levenshtein pairs  */
+    uint32_t candidates;       /* 0: every admissible pair of the buckets scored;
+                                  1: Hamming segment join (eps <= 2 at every
+                                  length): only pairs sharing a whole segment    */
+    uint32_t reserved;
 } idb_stats;
 
 /* Outputs (cuda/Interlink.hpp:59-67).  clone_id/core/copies are required. */
