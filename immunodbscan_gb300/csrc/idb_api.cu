@@ -71,7 +71,7 @@ enum BufId {
     bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bDeg, bGOff, bGCur, bAdj, bCnt, bUCore,
     bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
     bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bBpSmall,
-    bJnTab, bJnCount, bJnSlotHead, bJnISlot, bJnHeadSlot, bJnStart, bJnCur, bJnBpIdx, bNumBufs
+    bJnTab, bJnISlot, bJnHeadSlot, bJnStart, bJnCur, bJnBpIdx, bNumBufs
 };
 
 }  // namespace
@@ -478,7 +478,7 @@ idb_status alloc_fixed(Pipeline &pl) {
     TRY(ensure(c, bUidOfRow, 4 * N1));
     TRY(ensure(c, bRow2Uid, 4 * N));
     const uint64_t tcap = next_pow2(std::max<uint64_t>(2 * N, 1024));
-    TRY(ensure(c, bTable, 4 * tcap));
+    TRY(ensure(c, bTable, 8 * tcap));     // duplicate table: {row, ~size} per slot
     TRY(ensure(c, bTCount, 4 * tcap));
     TRY(ensure(c, bURow, 4 * N1));
     TRY(ensure(c, bUCopies, 4 * N1));
@@ -505,17 +505,13 @@ idb_status alloc_fixed(Pipeline &pl) {
         // keys: at most join_smax per unique; the table at load <= 1/2
         const uint64_t heads = (uint64_t)P.join_smax * N;
         const uint64_t jcap = next_pow2(std::max<uint64_t>(2 * heads, 1024));
-        TRY(ensure(c, bJnTab, 8 * jcap));
-        TRY(ensure(c, bJnCount, 4 * jcap));
-        TRY(ensure(c, bJnSlotHead, 4 * jcap));
+        TRY(ensure(c, bJnTab, sizeof(JSlot) * jcap));
         TRY(ensure(c, bJnISlot, 16 * N1));
         TRY(ensure(c, bJnHeadSlot, 4 * (heads + 1)));
         TRY(ensure(c, bJnStart, 4 * (heads + 1)));
         TRY(ensure(c, bJnCur, 4 * (heads + 1)));
         TRY(ensure(c, bJnBpIdx, 4 * (heads + 1)));
-        B.jn_tab = ptr<unsigned long long>(c, bJnTab);
-        B.jn_count = ptr<uint32_t>(c, bJnCount);
-        B.jn_slot_head = ptr<uint32_t>(c, bJnSlotHead);
+        B.jn_tab = ptr<JSlot>(c, bJnTab);
         B.jn_mask = jcap - 1;
         B.jn_islot = ptr<uint32_t>(c, bJnISlot);
         B.jn_head_slot = ptr<uint32_t>(c, bJnHeadSlot);

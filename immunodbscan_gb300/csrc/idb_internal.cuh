@@ -113,6 +113,15 @@ __device__ __forceinline__ void load_chunk32(const uint8_t *p, uint32_t L, uint3
     }
 }
 
+// One slot of the segment-join table: the segment key, how many (unique,
+// segment) entries hold it, and its head index.  16 bytes: a probe and the
+// updates that follow it touch one sector.
+struct __align__(16) JSlot {
+    unsigned long long key;
+    uint32_t cnt;
+    uint32_t head;
+};
+
 // Device-resident counters of one clustering call (one struct, zeroed first).
 struct Counters {
     uint32_t lmax, lmin;
@@ -233,8 +242,7 @@ struct Buffers {
     uint32_t *bp_units = nullptr;                   // [cap_binpairs+1]
     uint32_t *bp_small = nullptr;                   // [cap_binpairs] schedule positions of small bin pairs
     // segment join: table of (unique, segment) keys and the groups they form
-    unsigned long long *jn_tab = nullptr;           // [jn_mask+1] segment keys
-    uint32_t *jn_count = nullptr, *jn_slot_head = nullptr;   // [jn_mask+1]
+    JSlot *jn_tab = nullptr;                        // [jn_mask+1] segment-join table
     uint64_t jn_mask = 0;
     uint32_t *jn_islot = nullptr;                   // [4*N] slot of (unique, segment)
     uint32_t *jn_head_slot = nullptr;               // [join_smax*N] slot of each key

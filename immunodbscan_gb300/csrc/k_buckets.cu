@@ -550,12 +550,12 @@ __device__ __forceinline__ uint32_t join_mask(uint32_t nu, uint32_t smax, uint64
 }
 
 __global__ void k_join_clear(const Counters *__restrict__ ctr, uint32_t smax, uint64_t cap_mask,
-                             unsigned long long *__restrict__ tab, uint32_t *__restrict__ cnt) {
+                             JSlot *__restrict__ tab) {
     const uint32_t n = join_mask(ctr->n_uniques, smax, cap_mask) + 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        tab[i] = ~0ull;
-        cnt[i] = 0u;
+        tab[i].key = ~0ull;
+        tab[i].cnt = 0u;
     }
 }
 
@@ -564,7 +564,7 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
               const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
               const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
               const uint8_t *__restrict__ codemap, const int16_t *__restrict__ eps_tab,
-              unsigned long long *tab, uint32_t *cnt, uint32_t *__restrict__ slot_head,
+              JSlot *tab,
               uint32_t *__restrict__ head_slot, uint32_t *__restrict__ islot, uint32_t smax,
               uint64_t cap_mask) {
     __shared__ uint8_t cm[256];
@@ -591,9 +591,9 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
                         sl = kNone;
                         break;
                     }
-                    unsigned long long cur = *((volatile unsigned long long *)&tab[sl]);
+                    unsigned long long cur = *((volatile unsigned long long *)&tab[sl].key);
                     if (cur == ~0ull) {
-                        cur = atomicCAS(&tab[sl], ~0ull, key);
+                        cur = atomicCAS(&tab[sl].key, ~0ull, key);
                         if (cur == ~0ull) { won = true; break; }
                     }
                     if (cur == key) break;
@@ -611,11 +611,11 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
             if (won) {
                 const uint32_t hd = base + __popc(wm & ((1u << lane) - 1u));
                 head_slot[hd] = sl;
-                slot_head[sl] = hd;
+                tab[sl].head = hd;
             }
             // one count increment per key among the lanes here together
             const uint32_t grp = __match_any_sync(am, sl);
-            if (lane == (uint32_t)__ffs(grp) - 1 && sl != kNone) atomicAdd(&cnt[sl], (uint32_t)__popc(grp));
+            if (lane == (uint32_t)__ffs(grp) - 1 && sl != kNone) atomicAdd(&tab[sl].cnt, (uint32_t)__popc(grp));
         }
     }
 }
@@ -623,7 +623,7 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
 // Size of every key's group (0 for a key held by one unique) and the group
 // index of the keys that form bin pairs.
 __global__ void k_join_sizes(Counters *ctr, const uint32_t *__restrict__ head_slot,
-                             const uint32_t *__restrict__ cnt, uint32_t *__restrict__ sizes,
+                             const JSlot *__restrict__ tab, uint32_t *__restrict__ sizes,
                              uint32_t *__restrict__ bpidx) {
     const uint32_t nh = ctr->n_heads;
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -631,7 +631,7 @@ __global__ void k_join_sizes(Counters *ctr, const uint32_t *__restrict__ head_sl
     for (uint32_t h0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); h0 < nh; h0 += stride) {
         const uint32_t h = h0 + lane;
         uint32_t c = 0;
-        if (h < nh) c = cnt[head_slot[h]];
+        if (h < nh) c = tab[head_slot[h]].cnt;
         const bool grp = c >= 2;
         if (h < nh) sizes[h] = grp ? c : 0u;
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, grp);
@@ -651,7 +651,7 @@ k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restr
             const int64_t *__restrict__ seq_off, const uint8_t *__restrict__ codemap,
             const int16_t *__restrict__ eps_tab, const uint32_t *__restrict__ islot,
             const uint64_t *__restrict__ vbits, const uint64_t *__restrict__ jbits,
-            const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ slot_head,
+            const JSlot *__restrict__ tab,
             const uint32_t *__restrict__ start, uint32_t *__restrict__ cursor,
             uint32_t *__restrict__ ent_uid, uint4 *__restrict__ ent_rec,
             uint4 *__restrict__ ent_meta, int planes, uint32_t W, uint64_t cap_entries,
@@ -670,8 +670,10 @@ k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restr
         build_small_record<RSC>(seq + seq_off[row], L, cm, planes, W, rec);
         for (uint32_t k = 0; k < S; ++k) {
             const uint32_t sl = islot[(size_t)u * 4 + k];
-            if (sl == kNone || cnt[sl] < 2) continue;
-            const uint32_t h = slot_head[sl];
+            if (sl == kNone) continue;
+            const uint2 ch = *reinterpret_cast<const uint2 *>(&tab[sl].cnt);   // cnt, head
+            if (ch.x < 2) continue;
+            const uint32_t h = ch.y;
             const uint64_t pos = (uint64_t)start[h] + atomicAdd(&cursor[h], 1u);
             if (pos >= cap_entries) { atomicOr(err, kErrEntryOverflow); continue; }
             ent_uid[pos] = u;
@@ -694,19 +696,18 @@ __global__ void k_join_nbp(Counters *ctr) {
 // One bin pair (a group against itself) per key held by two or more uniques.
 __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
                                const uint32_t *__restrict__ head_slot,
-                               const unsigned long long *__restrict__ tab,
-                               const uint32_t *__restrict__ cnt, const uint32_t *__restrict__ start,
+                               const JSlot *__restrict__ tab, const uint32_t *__restrict__ start,
                                const uint32_t *__restrict__ bpidx, const int16_t *__restrict__ eps_tab, uint32_t TX, uint64_t cap_bp,
                                BinPair *__restrict__ out, uint32_t *err) {
     const uint32_t nh = ctr->n_heads;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += stride) {
         const uint32_t sl = head_slot[h];
-        const uint32_t c = cnt[sl];
+        const uint32_t c = tab[sl].cnt;
         if (c < 2) continue;
         const uint32_t k = bpidx[h];
         if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); continue; }
-        const unsigned long long key = tab[sl];
+        const unsigned long long key = tab[sl].key;
         const uint32_t L = (uint32_t)(key >> 32) & 0xFFu;
         const uint32_t li = L - g.Lmin;
         BinPair P;
@@ -731,14 +732,13 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
     if (P.join) {
         const uint64_t heads = (uint64_t)P.join_smax * P.N;
         k_join_clear<<<grid_wave(k_join_clear, B.jn_mask + 1, kThreads), kThreads, 0, s>>>(
-            B.ctr, P.join_smax, B.jn_mask, B.jn_tab, B.jn_count);
+            B.ctr, P.join_smax, B.jn_mask, B.jn_tab);
         cudaMemsetAsync(&B.ctr->n_heads, 0, 2 * sizeof(uint32_t), s);   // n_heads, n_groups
         k_join_insert<<<grid_wave(k_join_insert, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
                                                           B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
-                                                          B.jn_count,
-                                                          B.jn_slot_head, B.jn_head_slot, B.jn_islot,
+                                                          B.jn_head_slot, B.jn_islot,
                                                           P.join_smax, B.jn_mask);
-        k_join_sizes<<<grid_wave(k_join_sizes, heads, kThreads), kThreads, 0, s>>>(B.ctr, B.jn_head_slot, B.jn_count, B.jn_start,
+        k_join_sizes<<<grid_wave(k_join_sizes, heads, kThreads), kThreads, 0, s>>>(B.ctr, B.jn_head_slot, B.jn_tab, B.jn_start,
                                                            B.jn_bpidx);
         scan_u32(B.jn_start, B.jn_start, (uint32_t)heads, &B.ctr->n_heads, &B.ctr->n_entries,
                  B.scan_part, B.scan_part_cap, s);
@@ -768,8 +768,7 @@ void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
         auto go = [&](auto kern) {
             kern<<<grid_wave(kern, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.seq, B.seq_off,
                                                      B.codemap, B.eps_tab, B.jn_islot, B.vbits,
-                                                     B.jbits, B.jn_count,
-                                                     B.jn_slot_head, B.jn_start, B.jn_cur, B.ent_uid,
+                                                     B.jbits, B.jn_tab, B.jn_start, B.jn_cur, B.ent_uid,
                                                      B.ent_rec, B.ent_meta, planes, P.W,
                                                      P.cap_entries, &B.ctr->error);
         };
@@ -827,7 +826,7 @@ void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
         BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
         const uint64_t heads = (uint64_t)P.join_smax * P.N;
         k_join_bp_fill<<<grid_wave(k_join_bp_fill, heads, kThreads), kThreads, 0, s>>>(
-            g, B.ctr, B.jn_head_slot, B.jn_tab, B.jn_count, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX,
+            g, B.ctr, B.jn_head_slot, B.jn_tab, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX,
             P.cap_binpairs, B.bp, &B.ctr->error);
         return;
     }

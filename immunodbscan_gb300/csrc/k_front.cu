@@ -595,7 +595,8 @@ struct DedupArgs {
     const uint64_t *vbits, *jbits; uint32_t VW, JW;
     const uint32_t *rep_off; uint32_t R;
     uint32_t N;
-    uint32_t *table, *tcount, *slot;
+    uint2 *dtab;          // slot: {row of the class, ~(class size)}; all ones when empty
+    uint32_t *slot;
     uint64_t mask;
     Counters *ctr;
 };
@@ -647,9 +648,9 @@ __global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
                 s = kNone;
                 break;
             }
-            uint32_t cur = *((volatile uint32_t *)&a.table[s]);
+            uint32_t cur = *((volatile uint32_t *)&a.dtab[s].x);
             if (cur == kNone) {
-                uint32_t prev = atomicCAS(&a.table[s], kNone, i);
+                uint32_t prev = atomicCAS(&a.dtab[s].x, kNone, i);
                 if (prev == kNone) break;
                 cur = prev;
             }
@@ -661,19 +662,19 @@ __global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
         // rows (lanes hold ascending rows, so the lowest lane has the smallest)
         const uint32_t grp = __match_any_sync(__activemask(), (uint32_t)s);
         if ((threadIdx.x & 31) == (uint32_t)(__ffs(grp) - 1) && s != kNone) {
-            atomicAdd(&a.tcount[s], (uint32_t)__popc(grp));
-            atomicMin(&a.table[s], i);
+            atomicSub(&a.dtab[s].y, (uint32_t)__popc(grp));   // the size is kept complemented
+            atomicMin(&a.dtab[s].x, i);
         }
     }
 }
 
 __global__ void k_dedupe_final(uint32_t N, const uint32_t *__restrict__ slot,
-                               const uint32_t *__restrict__ table, uint32_t *__restrict__ rep_row,
+                               const uint2 *__restrict__ dtab, uint32_t *__restrict__ rep_row,
                                uint32_t *__restrict__ flag) {
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
         const uint32_t s = slot[i];
-        const uint32_t r = s == kNone ? i : table[s];
+        const uint32_t r = s == kNone ? i : dtab[s].x;
         rep_row[i] = r;
         flag[i] = (r == i);
     }
@@ -684,7 +685,7 @@ __global__ void k_dedupe_final(uint32_t N, const uint32_t *__restrict__ slot,
 // columns and the row -> uid map.
 __global__ void k_uniques(uint32_t N, const int64_t *__restrict__ off,
                           const uint32_t *__restrict__ rep_off, uint32_t R,
-                          const uint32_t *__restrict__ slot, const uint32_t *__restrict__ tcount,
+                          const uint32_t *__restrict__ slot, const uint2 *__restrict__ dtab,
                           const uint32_t *__restrict__ rep_row, const uint32_t *__restrict__ uid_of_row,
                           uint32_t *__restrict__ urow, uint32_t *__restrict__ ucopies,
                           uint32_t *__restrict__ ulen, uint32_t *__restrict__ urep,
@@ -695,7 +696,7 @@ __global__ void k_uniques(uint32_t N, const int64_t *__restrict__ off,
         if (r == i) {
             const uint32_t u = uid_of_row[i];
             urow[u] = i;
-            ucopies[u] = slot[i] == kNone ? 1u : tcount[slot[i]];
+            ucopies[u] = slot[i] == kNone ? 1u : ~dtab[slot[i]].y;
             ulen[u] = (uint32_t)(off[i + 1] - off[i]);
             urep[u] = rep_of_row(rep_off, R, i);
         }
@@ -925,18 +926,18 @@ void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s) {
     a.seq = B.seq; a.off = B.seq_off;
     a.vbits = B.vbits; a.jbits = B.jbits; a.VW = P.VW; a.JW = P.JW;
     a.rep_off = B.rep_off; a.R = P.R; a.N = P.N;
-    a.table = B.table; a.tcount = B.tcount; a.slot = B.slot;
+    a.dtab = reinterpret_cast<uint2 *>(B.table); a.slot = B.slot;
     a.mask = B.table_mask; a.ctr = B.ctr;
-    cudaMemsetAsync(B.table, 0xFF, sizeof(uint32_t) * (B.table_mask + 1), s);
-    cudaMemsetAsync(B.tcount, 0, sizeof(uint32_t) * (B.table_mask + 1), s);
+    cudaMemsetAsync(B.table, 0xFF, sizeof(uint2) * (B.table_mask + 1), s);
     k_dedupe_insert<<<grid_wave(k_dedupe_insert, P.N, kThreads), kThreads, 0, s>>>(a);
-    k_dedupe_final<<<grid_wave(k_dedupe_final, P.N, kThreads), kThreads, 0, s>>>(P.N, B.slot, B.table, B.rep_row, B.flag);
+    k_dedupe_final<<<grid_wave(k_dedupe_final, P.N, kThreads), kThreads, 0, s>>>(P.N, B.slot, reinterpret_cast<const uint2 *>(B.table), B.rep_row, B.flag);
 }
 
 void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s) {
     scan_u32(B.flag, B.uid_of_row, P.N, nullptr, &B.ctr->n_uniques, B.scan_part,
              B.scan_part_cap, s);
-    k_uniques<<<grid_wave(k_uniques, P.N, kThreads), kThreads, 0, s>>>(P.N, B.seq_off, B.rep_off, P.R, B.slot, B.tcount,
+    k_uniques<<<grid_wave(k_uniques, P.N, kThreads), kThreads, 0, s>>>(P.N, B.seq_off, B.rep_off, P.R, B.slot,
+                                                   reinterpret_cast<const uint2 *>(B.table),
                                                    B.rep_row, B.uid_of_row, B.urow, B.ucopies,
                                                    B.ulen, B.urep, B.row2uid);
     k_uid_first<<<(P.R + 1 + 255) / 256, 256, 0, s>>>(P.N, P.R, B.rep_off, B.uid_of_row, B.ctr,
