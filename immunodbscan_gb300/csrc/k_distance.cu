@@ -106,6 +106,37 @@ struct EdgeWriter {
         fill += n;
         written += n;
     }
+
+    // Bulk append, warp-uniform: the warp appends T edges at logical positions
+    // 0..T-1 (each lane knows its own); the room left in the held chunk is
+    // used first, then as many new chunks as needed, reserved with one atomic.
+    struct Bulk { uint64_t b0; uint32_t f0; uint64_t nb; };
+    __device__ Bulk reserve(const DistArgs &a, int lane, uint32_t T) {
+        Bulk k;
+        k.f0 = base == kNoChunk ? kEdgeChunk : fill;
+        k.b0 = base;
+        k.nb = kNoChunk;
+        const uint32_t room = kEdgeChunk - k.f0;
+        if (T > room) {
+            const uint32_t nch = (T - room + kEdgeChunk - 1) / kEdgeChunk;
+            uint32_t nb = 0;
+            if (lane == 0) nb = atomicAdd(&a.ctr->edge_reserved, nch * kEdgeChunk);
+            nb = __shfl_sync(0xFFFFFFFFu, nb, 0);
+            if ((uint64_t)nb + (uint64_t)nch * kEdgeChunk > a.cap_edges && lane == 0)
+                atomicOr(&a.ctr->error, kErrEdgeOverflow);
+            k.nb = nb;
+            base = (uint64_t)nb + (uint64_t)(nch - 1) * kEdgeChunk;
+            fill = (T - room) - (nch - 1) * kEdgeChunk;
+        } else {
+            fill = k.f0 + T;
+        }
+        written += T;
+        return k;
+    }
+    __device__ __forceinline__ uint64_t slot_of(const Bulk &k, uint32_t i) const {
+        const uint32_t room = kEdgeChunk - k.f0;
+        return i < room ? k.b0 + k.f0 + i : k.nb + (i - room);
+    }
 };
 
 // lowest common gene of two uniques in one column, -1 if none
@@ -256,36 +287,6 @@ __device__ __noinline__ void emit_hits(const DistArgs &a, EdgeWriter &ew, uint32
                  lowest_common(a.jbits, a.JW, rx, ry) == (int)j;
         }
         ew.append(a, lane, ok, min(ux, uy), max(ux, uy));
-    }
-}
-
-// Same, with the entries' side records in shared memory: the canonical test is
-// (sig_x & sig_y) == 0 over the genes below the bin's V and J gene, and the
-// unique ids come with the records, so a hit reads no global memory.
-__device__ __noinline__ void emit_hits_meta(const DistArgs &a, EdgeWriter &ew, uint32_t hit,
-                                            const uint4 *xm, uint4 ym, uint32_t xbase,
-                                            uint32_t ypos, uint32_t same, uint32_t v, uint32_t j,
-                                            int lane) {
-    uint32_t any = __reduce_or_sync(0xFFFFFFFFu, hit);
-    while (any) {
-        const int r = __ffs(any) - 1;
-        any &= any - 1;
-        const uint32_t xpos = xbase + 32u * r + lane;
-        bool ok = (hit >> r) & 1u;
-        if (ok && same && ypos <= xpos) ok = false;
-        const uint4 m = xm[32 * r + lane];
-        if (ok) {
-            if (a.join) {
-                // segment join: checked when the hit was queued
-            } else if (a.sig_exact) {
-                ok = ((m.x & ym.x) | (m.y & ym.y) | (m.z & ym.z)) == 0;
-            } else {
-                const uint32_t rx = a.urow[m.w], ry = a.urow[ym.w];
-                ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)v &&
-                     lowest_common(a.jbits, a.JW, rx, ry) == (int)j;
-            }
-        }
-        ew.append(a, lane, ok, min(m.w, ym.w), max(m.w, ym.w));
     }
 }
 
@@ -539,15 +540,58 @@ constexpr int kHitQ = 8;   // queued (y, hits) records per lane
 constexpr uint32_t kLevQ = 256;          // queued candidate pairs per warp (Levenshtein)
 constexpr uint32_t kOff = 0x40000000u;   // score of a masked x-entry (never a hit)
 
-__device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, const uint32_t *q,
+// The queue holds (y index in the chunk, hit bits) per lane.  Hits are
+// compacted over the whole warp before they are written: each lane first keeps
+// the bits of its own queue that are edges (pair order and canonical bin),
+// then one warp scan gives every lane its place in one bulk append.
+__device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, uint32_t *q,
                                         uint32_t qn, const uint4 *xm, const uint4 *ym,
                                         uint32_t xbase, uint32_t ypos0, uint32_t same,
                                         uint32_t v, uint32_t j, int lane) {
-    const uint32_t kmax = __reduce_max_sync(0xFFFFFFFFu, qn);
-    for (uint32_t k = 0; k < kmax; ++k) {
-        const uint32_t e = k < qn ? q[k * 32 + lane] : 0u;
-        const uint32_t hit = e & 0xFFu, t = e >> 8;
-        emit_hits_meta(a, ew, hit, xm, ym[t], xbase, ypos0 + t, same, v, j, lane);
+    uint32_t c = 0;
+    for (uint32_t k = 0; k < qn; ++k) {
+        const uint32_t e = q[k * 32 + lane];
+        const uint32_t t = e >> 8, ypos = ypos0 + t;
+        const uint4 my = ym[t];
+        uint32_t keep = 0;
+        for (uint32_t b = e & 0xFFu; b; b &= b - 1) {
+            const uint32_t r = (uint32_t)__ffs(b) - 1u;
+            const uint32_t xpos = xbase + 32u * r + (uint32_t)lane;
+            bool ok = !(same && ypos <= xpos);
+            if (ok && !a.join) {
+                const uint4 m = xm[32 * r + lane];
+                if (a.sig_exact) {
+                    ok = ((m.x & my.x) | (m.y & my.y) | (m.z & my.z)) == 0;
+                } else {
+                    const uint32_t rx = a.urow[m.w], ry = a.urow[my.w];
+                    ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)v &&
+                         lowest_common(a.jbits, a.JW, rx, ry) == (int)j;
+                }
+            }
+            keep |= (uint32_t)ok << r;   // the join was checked when the hit was queued
+        }
+        q[k * 32 + lane] = (t << 8) | keep;
+        c += (uint32_t)__popc(keep);
+    }
+    uint32_t incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t n = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += n;
+    }
+    const uint32_t T = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    if (T == 0) return;
+    const EdgeWriter::Bulk bk = ew.reserve(a, lane, T);
+    uint32_t i = incl - c;
+    for (uint32_t k = 0; k < qn; ++k) {
+        const uint32_t e = q[k * 32 + lane];
+        const uint32_t uy = ym[e >> 8].w;
+        for (uint32_t b = e & 0xFFu; b; b &= b - 1) {
+            const uint32_t r = (uint32_t)__ffs(b) - 1u;
+            const uint32_t ux = xm[32 * r + lane].w;
+            const uint64_t slot = ew.slot_of(bk, i++);
+            if (slot < a.cap_edges) a.edges[slot] = make_uint2(min(ux, uy), max(ux, uy));
+        }
     }
 }
 
