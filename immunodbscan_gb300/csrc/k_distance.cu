@@ -306,6 +306,34 @@ __device__ __forceinline__ void small_pair(uint32_t p, bool same, uint32_t n, ui
     }
 }
 
+// Bulk append of a lane's edges given as bits: bit b stands for pair index
+// p0 + stride*b of a small or tiny bin pair (i, j from the pair index; the
+// unique ids from the side records).  Warp-uniform.
+__device__ __forceinline__ void emit_pair_bits(const DistArgs &a, EdgeWriter &ew, int lane,
+                                               uint32_t bits, uint32_t p0, uint32_t stride,
+                                               bool same, uint32_t n, uint32_t xstart,
+                                               uint32_t ystart) {
+    const uint32_t c = (uint32_t)__popc(bits);
+    uint32_t incl = c;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+        if (lane >= d) incl += t;
+    }
+    const uint32_t T = __shfl_sync(0xFFFFFFFFu, incl, 31);
+    if (T == 0) return;
+    const EdgeWriter::Bulk bk = ew.reserve(a, lane, T);
+    uint32_t k = incl - c;
+    for (uint32_t b = bits; b; b &= b - 1) {
+        const uint32_t p = p0 + stride * ((uint32_t)__ffs(b) - 1u);
+        uint32_t i, j;
+        small_pair(p, same, n, i, j);
+        const uint32_t ux = __ldg(&a.meta[xstart + i].w), uy = __ldg(&a.meta[ystart + j].w);
+        const uint64_t slot = ew.slot_of(bk, k++);
+        if (slot < a.cap_edges) a.edges[slot] = make_uint2(min(ux, uy), max(ux, uy));
+    }
+}
+
 // A small bin pair (at most kSmallSide entries a side), pair-parallel: lane l
 // holds entry l of each side; each round the lanes take 32 pairs and fetch
 // the two records by shuffles.  Canonicity of a hit is decided from the side
@@ -338,6 +366,8 @@ __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew,
     if (lane == 0) pairs += npairs;
     const uint32_t thr = EM == 0 ? (uint32_t)max(P.eps, 0) : 0u;
     const bool neg = EM == 0 && P.eps < 0;
+    static_assert(kSmallSide * kSmallSide <= 32 * 32, "small round mask");
+    uint32_t rmask = 0;           // bit k: the lane's pair of round k is an edge
     for (uint32_t p0 = 0; p0 < npairs && !neg; p0 += 32) {
         const uint32_t p = p0 + lane;
         const bool act = p < npairs;
@@ -366,26 +396,23 @@ __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew,
             }
             sc = dist;
         }
-        const bool hit = act && sc <= thr;
-        if (__any_sync(0xFFFFFFFFu, hit)) {
-            bool ok = hit;
-            uint4 mx = make_uint4(0, 0, 0, 0), my = mx;
-            if (ok) {
-                mx = __ldg(a.meta + P.a_start + i);
-                my = __ldg(a.meta + ystart + j);
-                if (a.join) {
-                    ok = join_meta_ok<W>(mx, my, dw, P.la, P.j, P.v);
-                } else if (a.sig_exact) {
-                    ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
-                } else {
-                    const uint32_t rx = a.urow[mx.w], ry = a.urow[my.w];
-                    ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)P.v &&
-                         lowest_common(a.jbits, a.JW, rx, ry) == (int)P.j;
-                }
+        if (act && sc <= thr) {
+            const uint4 mx = __ldg(a.meta + P.a_start + i), my = __ldg(a.meta + ystart + j);
+            bool ok;
+            if (a.join) {
+                ok = join_meta_ok<W>(mx, my, dw, P.la, P.j, P.v);
+            } else if (a.sig_exact) {
+                ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
+            } else {
+                const uint32_t rx = a.urow[mx.w], ry = a.urow[my.w];
+                ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)P.v &&
+                     lowest_common(a.jbits, a.JW, rx, ry) == (int)P.j;
             }
-            ew.append(a, lane, ok, min(mx.w, my.w), max(mx.w, my.w));
+            rmask |= (uint32_t)ok << (p0 >> 5);
         }
     }
+    // every round's edges of the lane, one bulk append for the warp
+    emit_pair_bits(a, ew, lane, rmask, (uint32_t)lane, 32u, same, n, P.a_start, ystart);
     if (a.bp_cycles && lane == 0)
         atomicAdd(&a.bp_cycles[idx], (unsigned long long)(clock64() - t0));
 }
@@ -475,53 +502,46 @@ __device__ __forceinline__ void hamming_tiny_all(const DistArgs &a, EdgeWriter &
         pairs += n * (n - 1) / 2;
         const uint32_t thr = EM == 0 ? (uint32_t)max((int)P.eps, 0) : 0u;
         const uint4 *rec = a.rec + (size_t)P.a_start * R16;
-        const uint32_t maxp = __reduce_max_sync(0xFFFFFFFFu, np);
-        for (uint32_t p = 0; p < maxp; ++p) {
-            bool hit = false;
-            uint32_t i = 0, j = 0;
-            uint32_t dw[W];
+        // pass 1: each lane scores its bin pair's pairs and keeps the edges
+        // as bits of pair indices (at most 28 pairs)
+        static_assert(kTinySide * (kTinySide - 1) / 2 <= 32, "tiny pair mask");
+        uint32_t emask = 0;
+        for (uint32_t p = 0; p < np; ++p) {
+            uint32_t i, j;
+            small_pair(p, true, n, i, j);
+            uint32_t xw[4 * R16], yw[4 * R16];
 #pragma unroll
-            for (int w = 0; w < W; ++w) dw[w] = 0;
-            if (p < np) {
-                small_pair(p, true, n, i, j);
-                uint32_t xw[4 * R16], yw[4 * R16];
-#pragma unroll
-                for (int q = 0; q < R16; ++q) {
-                    const uint4 u = __ldg(rec + (size_t)i * R16 + q), v = __ldg(rec + (size_t)j * R16 + q);
-                    xw[4 * q] = u.x; xw[4 * q + 1] = u.y; xw[4 * q + 2] = u.z; xw[4 * q + 3] = u.w;
-                    yw[4 * q] = v.x; yw[4 * q + 1] = v.y; yw[4 * q + 2] = v.z; yw[4 * q + 3] = v.w;
-                }
-                uint32_t dist = 0;
-#pragma unroll
-                for (int w = 0; w < W; ++w) {
-                    uint32_t d = xw[w] ^ yw[w];
-#pragma unroll
-                    for (int q = 1; q < BP; ++q) d |= xw[q * W + w] ^ yw[q * W + w];
-                    dw[w] = d;
-                    dist += __popc(d);
-                }
-                const uint32_t sc = EM == 2 ? dw[0] : (EM == 1 ? (dw[0] & (dw[0] - 1u)) : dist);
-                hit = sc <= thr;
+            for (int q = 0; q < R16; ++q) {
+                const uint4 u = __ldg(rec + (size_t)i * R16 + q), v = __ldg(rec + (size_t)j * R16 + q);
+                xw[4 * q] = u.x; xw[4 * q + 1] = u.y; xw[4 * q + 2] = u.z; xw[4 * q + 3] = u.w;
+                yw[4 * q] = v.x; yw[4 * q + 1] = v.y; yw[4 * q + 2] = v.z; yw[4 * q + 3] = v.w;
             }
-            if (__any_sync(0xFFFFFFFFu, hit)) {
-                bool ok = hit;
-                uint4 mx = make_uint4(0, 0, 0, 0), my = mx;
-                if (ok) {
-                    mx = __ldg(a.meta + P.a_start + i);
-                    my = __ldg(a.meta + P.a_start + j);
-                    if (a.join) {
-                        ok = join_meta_ok<W>(mx, my, dw, P.la, P.j, P.v);
-                    } else if (a.sig_exact) {
-                        ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
-                    } else {
-                        const uint32_t rx = a.urow[mx.w], ry = a.urow[my.w];
-                        ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)P.v &&
-                             lowest_common(a.jbits, a.JW, rx, ry) == (int)P.j;
-                    }
-                }
-                ew.append(a, lane, ok, min(mx.w, my.w), max(mx.w, my.w));
+            uint32_t dw[W], dist = 0;
+#pragma unroll
+            for (int w = 0; w < W; ++w) {
+                uint32_t d = xw[w] ^ yw[w];
+#pragma unroll
+                for (int q = 1; q < BP; ++q) d |= xw[q * W + w] ^ yw[q * W + w];
+                dw[w] = d;
+                dist += __popc(d);
             }
+            const uint32_t sc = EM == 2 ? dw[0] : (EM == 1 ? (dw[0] & (dw[0] - 1u)) : dist);
+            if (sc > thr) continue;
+            const uint4 mx = __ldg(a.meta + P.a_start + i), my = __ldg(a.meta + P.a_start + j);
+            bool ok;
+            if (a.join) {
+                ok = join_meta_ok<W>(mx, my, dw, P.la, P.j, P.v);
+            } else if (a.sig_exact) {
+                ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
+            } else {
+                const uint32_t rx = a.urow[mx.w], ry = a.urow[my.w];
+                ok = lowest_common(a.vbits, a.VW, rx, ry) == (int)P.v &&
+                     lowest_common(a.jbits, a.JW, rx, ry) == (int)P.j;
+            }
+            emask |= (uint32_t)ok << p;
         }
+        // pass 2: one bulk append for the warp
+        emit_pair_bits(a, ew, lane, emask, 0u, 1u, true, n, P.a_start, P.a_start);
         if (a.bp_cycles) {
             // the batch's cycles, shared out by pairs (every lane takes part in
             // the reduction; lanes past the list's end hold n = 0)
