@@ -288,6 +288,11 @@ k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
             uint32_t GW, const GeneEntry *__restrict__ tab, GeneMatcher gm,
             uint64_t *__restrict__ bits) {
     extern __shared__ __align__(16) uint8_t sm[];
+    // blocks past the last chunk of rows leave before loading the tables (the
+    // grid is sized for every row having its own call; few rows do)
+    const uint32_t n = n_dev ? *n_dev : n_host;
+    const uint32_t nchunks = (n + kGbRows - 1) / kGbRows;
+    if (blockIdx.x * kGbWarps >= nchunks) return;
     // block-wide tables
     GeneEntry *s_tab = reinterpret_cast<GeneEntry *>(sm);
     int32_t *s_goff = reinterpret_cast<int32_t *>(s_tab + gm.ts);
@@ -310,8 +315,6 @@ k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
         }
     __syncthreads();
     const uint8_t *names = name_bytes ? s_names : genes;
-    const uint32_t n = n_dev ? *n_dev : n_host;
-    const uint32_t nchunks = (n + kGbRows - 1) / kGbRows;
     const uint32_t gwarp = blockIdx.x * kGbWarps + wid, nwarps = gridDim.x * kGbWarps;
     for (uint32_t ch = gwarp; ch < nchunks; ch += nwarps) {
         const uint32_t end = min(ch * kGbRows + kGbRows, n);
@@ -787,24 +790,47 @@ k_scan_parts(uint32_t *__restrict__ part, uint32_t nb, uint32_t *total_out) {
 
 __global__ void __launch_bounds__(kScanThreads)
 k_scan_down(const uint32_t *in, uint32_t *out, uint32_t n_host, const uint32_t *n_dev,
-            const uint32_t *__restrict__ part) {
+            const uint32_t *__restrict__ part, int vec) {
     const uint32_t n = n_dev ? min(*n_dev, n_host) : n_host;
     const uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    // a thread's 16 items are 64 bytes, aligned when both arrays are: then a
+    // thread whose items are all inside moves them as four 16-byte words
+    static_assert(kScanItems % 4 == 0, "vector items");
+    const bool whole = vec && base + kScanItems <= n;
     uint32_t v[kScanItems];
     uint32_t s = 0;
+    if (whole) {
 #pragma unroll
-    for (int k = 0; k < kScanItems; ++k) {
-        uint64_t i = base + k;
-        v[k] = i < n ? in[i] : 0u;
-        s += v[k];
+        for (int q = 0; q < kScanItems / 4; ++q) {
+            const uint4 u = *reinterpret_cast<const uint4 *>(in + base + 4 * q);
+            v[4 * q] = u.x; v[4 * q + 1] = u.y; v[4 * q + 2] = u.z; v[4 * q + 3] = u.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k) {
+            const uint64_t i = base + k;
+            v[k] = i < n ? in[i] : 0u;
+        }
     }
+#pragma unroll
+    for (int k = 0; k < kScanItems; ++k) s += v[k];
     uint32_t total;
     uint32_t pre = block_excl_scan(s, &total) + part[blockIdx.x];
 #pragma unroll
     for (int k = 0; k < kScanItems; ++k) {
-        uint64_t i = base + k;
-        if (i < n) out[i] = pre;
-        pre += v[k];
+        const uint32_t x = v[k];
+        v[k] = pre;
+        pre += x;
+    }
+    if (whole) {
+#pragma unroll
+        for (int q = 0; q < kScanItems / 4; ++q)
+            *reinterpret_cast<uint4 *>(out + base + 4 * q) =
+                make_uint4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < kScanItems; ++k)
+            if (base + k < n) out[base + k] = v[k];
     }
 }
 
@@ -853,9 +879,10 @@ void scan_u32(const uint32_t *in, uint32_t *out, uint32_t n, const uint32_t *n_d
         return;
     }
     (void)part_cap;
+    const int vec = ((reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out)) & 15u) == 0;
     k_scan_reduce<<<nb, kScanThreads, 0, s>>>(in, n, n_dev, part);
     k_scan_parts<<<1, 1024, 0, s>>>(part, nb, total);
-    k_scan_down<<<nb, kScanThreads, 0, s>>>(in, out, n, n_dev, part);
+    k_scan_down<<<nb, kScanThreads, 0, s>>>(in, out, n, n_dev, part, vec);
 }
 
 void launch_stamp(unsigned long long *dst, cudaStream_t s) { k_stamp<<<1, 1, 0, s>>>(dst); }
