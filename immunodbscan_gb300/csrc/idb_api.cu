@@ -71,7 +71,7 @@ enum BufId {
     bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bDeg, bGOff, bGCur, bAdj, bCnt, bUCore,
     bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
     bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bBpSmall,
-    bJnTab, bJnISlot, bJnHeadSlot, bJnStart, bJnCur, bJnBpIdx, bNumBufs
+    bJnTab, bJnISlot, bJnStart, bJnCur, bJnBpIdx, bNumBufs
 };
 
 }  // namespace
@@ -507,14 +507,12 @@ idb_status alloc_fixed(Pipeline &pl) {
         const uint64_t jcap = next_pow2(std::max<uint64_t>(2 * heads, 1024));
         TRY(ensure(c, bJnTab, sizeof(JSlot) * jcap));
         TRY(ensure(c, bJnISlot, 16 * N1));
-        TRY(ensure(c, bJnHeadSlot, 4 * (heads + 1)));
         TRY(ensure(c, bJnStart, 4 * (heads + 1)));
         TRY(ensure(c, bJnCur, 4 * (heads + 1)));
         TRY(ensure(c, bJnBpIdx, 4 * (heads + 1)));
         B.jn_tab = ptr<JSlot>(c, bJnTab);
         B.jn_mask = jcap - 1;
         B.jn_islot = ptr<uint32_t>(c, bJnISlot);
-        B.jn_head_slot = ptr<uint32_t>(c, bJnHeadSlot);
         B.jn_start = ptr<uint32_t>(c, bJnStart);
         B.jn_cur = ptr<uint32_t>(c, bJnCur);
         B.jn_bpidx = ptr<uint32_t>(c, bJnBpIdx);

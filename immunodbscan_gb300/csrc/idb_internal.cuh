@@ -28,6 +28,9 @@ constexpr uint32_t kTinySide = 8;
 // buckets evaluate their pairs faster (64 repertoires, 1M rows: 2.92 against
 // 3.09 ms per call; eps 1: 1.25 against 0.99 ms for the join).
 constexpr int kJoinMaxEps = 2;
+// Segment join: flag in a (unique, segment) entry's slot index for the entry
+// that created the key (slot indices stay below 2^31).
+constexpr uint32_t kHeadBit = 0x80000000u;
 constexpr int kMlpIn = 16;              // learned scheduler: features per bin pair
 constexpr int kMlpHidden = 64;          // two hidden layers of 64
 constexpr int kMlpParams = kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +
@@ -245,7 +248,6 @@ struct Buffers {
     JSlot *jn_tab = nullptr;                        // [jn_mask+1] segment-join table
     uint64_t jn_mask = 0;
     uint32_t *jn_islot = nullptr;                   // [4*N] slot of (unique, segment)
-    uint32_t *jn_head_slot = nullptr;               // [join_smax*N] slot of each key
     uint32_t *jn_start = nullptr;                   // [join_smax*N+1] group sizes -> starts
     uint32_t *jn_cur = nullptr, *jn_bpidx = nullptr;   // [join_smax*N]
     uint32_t *cls_hist = nullptr;                   // [65]

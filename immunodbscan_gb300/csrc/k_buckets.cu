@@ -564,9 +564,7 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
               const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
               const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
               const uint8_t *__restrict__ codemap, const int16_t *__restrict__ eps_tab,
-              JSlot *tab,
-              uint32_t *__restrict__ head_slot, uint32_t *__restrict__ islot, uint32_t smax,
-              uint64_t cap_mask) {
+              JSlot *tab, uint32_t *__restrict__ islot, uint32_t smax, uint64_t cap_mask) {
     __shared__ uint8_t cm[256];
     for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
     __syncthreads();
@@ -600,45 +598,49 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
                     sl = (sl + 1) & (uint32_t)mask;
                 }
             }
-            islot[(size_t)u * 4 + k] = sl;
-            // a new key gets the next head index (one atomic per warp)
-            const uint32_t am = __activemask();
-            const uint32_t wm = __ballot_sync(am, won);
-            const uint32_t ld = (uint32_t)__ffs(am) - 1;
-            uint32_t base = 0;
-            if (lane == ld && wm) base = atomicAdd(&ctr->n_heads, (uint32_t)__popc(wm));
-            base = __shfl_sync(am, base, ld);
-            if (won) {
-                const uint32_t hd = base + __popc(wm & ((1u << lane) - 1u));
-                head_slot[hd] = sl;
-                tab[sl].head = hd;
-            }
+            // the entry that created a key is its head: head index u*smax + k
+            islot[(size_t)u * 4 + k] = sl == kNone ? kNone : (sl | (won ? kHeadBit : 0u));
+            if (won) tab[sl].head = u * smax + k;
             // one count increment per key among the lanes here together
+            const uint32_t am = __activemask();
             const uint32_t grp = __match_any_sync(am, sl);
             if (lane == (uint32_t)__ffs(grp) - 1 && sl != kNone) atomicAdd(&tab[sl].cnt, (uint32_t)__popc(grp));
         }
     }
 }
 
-// Size of every key's group (0 for a key held by one unique) and the group
-// index of the keys that form bin pairs.
-__global__ void k_join_sizes(Counters *ctr, const uint32_t *__restrict__ head_slot,
-                             const JSlot *__restrict__ tab, uint32_t *__restrict__ sizes,
-                             uint32_t *__restrict__ bpidx) {
-    const uint32_t nh = ctr->n_heads;
+// Size of every key's group (0 for a key held by one unique, and for head
+// indices u*smax + k whose entry did not create its key), and the bin-pair
+// index of the keys that form groups (one counter atomic per block and pass).
+__global__ void __launch_bounds__(256)
+k_join_sizes(Counters *ctr, const uint32_t *__restrict__ islot, const JSlot *__restrict__ tab,
+             uint32_t smax, uint32_t *__restrict__ sizes, uint32_t *__restrict__ bpidx) {
+    __shared__ uint32_t s_w[8];
+    __shared__ uint32_t s_base;
+    const uint32_t nh = ctr->n_uniques * smax;
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr->n_heads = nh;
+    const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
-    const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t h0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); h0 < nh; h0 += stride) {
-        const uint32_t h = h0 + lane;
+    for (uint32_t h0 = blockIdx.x * blockDim.x; h0 < nh; h0 += stride) {
+        const uint32_t h = h0 + threadIdx.x;
         uint32_t c = 0;
-        if (h < nh) c = tab[head_slot[h]].cnt;
+        if (h < nh) {
+            const uint32_t e = islot[(size_t)(h / smax) * 4 + h % smax];
+            if (e != kNone && (e & kHeadBit)) c = tab[e & ~kHeadBit].cnt;
+        }
         const bool grp = c >= 2;
         if (h < nh) sizes[h] = grp ? c : 0u;
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, grp);
-        uint32_t base = 0;
-        if (lane == 0 && m) base = atomicAdd(&ctr->n_groups, (uint32_t)__popc(m));
-        base = __shfl_sync(0xFFFFFFFFu, base, 0);
-        if (grp) bpidx[h] = base + __popc(m & ((1u << lane) - 1u));
+        if (lane == 0) s_w[wid] = (uint32_t)__popc(m);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (uint32_t w = 0; w < blockDim.x / 32; ++w) { const uint32_t x = s_w[w]; s_w[w] = t; t += x; }
+            s_base = t ? atomicAdd(&ctr->n_groups, t) : 0u;
+        }
+        __syncthreads();
+        if (grp) bpidx[h] = s_base + s_w[wid] + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        __syncthreads();
     }
 }
 
@@ -669,8 +671,9 @@ k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restr
         uint4 rec[RSC];
         build_small_record<RSC>(seq + seq_off[row], L, cm, planes, W, rec);
         for (uint32_t k = 0; k < S; ++k) {
-            const uint32_t sl = islot[(size_t)u * 4 + k];
-            if (sl == kNone) continue;
+            const uint32_t e = islot[(size_t)u * 4 + k];
+            if (e == kNone) continue;
+            const uint32_t sl = e & ~kHeadBit;
             const uint2 ch = *reinterpret_cast<const uint2 *>(&tab[sl].cnt);   // cnt, head
             if (ch.x < 2) continue;
             const uint32_t h = ch.y;
@@ -695,14 +698,16 @@ __global__ void k_join_nbp(Counters *ctr) {
 
 // One bin pair (a group against itself) per key held by two or more uniques.
 __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
-                               const uint32_t *__restrict__ head_slot,
+                               const uint32_t *__restrict__ islot, uint32_t smax,
                                const JSlot *__restrict__ tab, const uint32_t *__restrict__ start,
                                const uint32_t *__restrict__ bpidx, const int16_t *__restrict__ eps_tab, uint32_t TX, uint64_t cap_bp,
                                BinPair *__restrict__ out, uint32_t *err) {
     const uint32_t nh = ctr->n_heads;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += stride) {
-        const uint32_t sl = head_slot[h];
+        const uint32_t e = islot[(size_t)(h / smax) * 4 + h % smax];
+        if (e == kNone || !(e & kHeadBit)) continue;
+        const uint32_t sl = e & ~kHeadBit;
         const uint32_t c = tab[sl].cnt;
         if (c < 2) continue;
         const uint32_t k = bpidx[h];
@@ -736,10 +741,10 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
         cudaMemsetAsync(&B.ctr->n_heads, 0, 2 * sizeof(uint32_t), s);   // n_heads, n_groups
         k_join_insert<<<grid_wave(k_join_insert, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
                                                           B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
-                                                          B.jn_head_slot, B.jn_islot,
+                                                          B.jn_islot,
                                                           P.join_smax, B.jn_mask);
-        k_join_sizes<<<grid_wave(k_join_sizes, heads, kThreads), kThreads, 0, s>>>(B.ctr, B.jn_head_slot, B.jn_tab, B.jn_start,
-                                                           B.jn_bpidx);
+        k_join_sizes<<<grid_wave(k_join_sizes, heads, kThreads), kThreads, 0, s>>>(
+            B.ctr, B.jn_islot, B.jn_tab, P.join_smax, B.jn_start, B.jn_bpidx);
         scan_u32(B.jn_start, B.jn_start, (uint32_t)heads, &B.ctr->n_heads, &B.ctr->n_entries,
                  B.scan_part, B.scan_part_cap, s);
         return;
@@ -826,7 +831,7 @@ void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
         BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
         const uint64_t heads = (uint64_t)P.join_smax * P.N;
         k_join_bp_fill<<<grid_wave(k_join_bp_fill, heads, kThreads), kThreads, 0, s>>>(
-            g, B.ctr, B.jn_head_slot, B.jn_tab, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX,
+            g, B.ctr, B.jn_islot, P.join_smax, B.jn_tab, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX,
             P.cap_binpairs, B.bp, &B.ctr->error);
         return;
     }
