@@ -288,10 +288,13 @@ k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
             uint32_t GW, const GeneEntry *__restrict__ tab, GeneMatcher gm,
             uint64_t *__restrict__ bits) {
     extern __shared__ __align__(16) uint8_t sm[];
-    // blocks past the last chunk of rows leave before loading the tables (the
-    // grid is sized for every row having its own call; few rows do)
+    // rows per warp window: up to kGbRows, fewer when the rows are few (the
+    // distinct calls of a column), so that every warp of the grid gets some;
+    // blocks past the last window leave before loading the tables
     const uint32_t n = n_dev ? *n_dev : n_host;
-    const uint32_t nchunks = (n + kGbRows - 1) / kGbRows;
+    const uint32_t nwarps = gridDim.x * kGbWarps;
+    const uint32_t rpc = max(1u, min((uint32_t)kGbRows, (n + nwarps - 1) / nwarps));
+    const uint32_t nchunks = (n + rpc - 1) / rpc;
     if (blockIdx.x * kGbWarps >= nchunks) return;
     // block-wide tables
     GeneEntry *s_tab = reinterpret_cast<GeneEntry *>(sm);
@@ -315,10 +318,10 @@ k_gene_bits(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
         }
     __syncthreads();
     const uint8_t *names = name_bytes ? s_names : genes;
-    const uint32_t gwarp = blockIdx.x * kGbWarps + wid, nwarps = gridDim.x * kGbWarps;
+    const uint32_t gwarp = blockIdx.x * kGbWarps + wid;
     for (uint32_t ch = gwarp; ch < nchunks; ch += nwarps) {
-        const uint32_t end = min(ch * kGbRows + kGbRows, n);
-        uint32_t r = ch * kGbRows;
+        const uint32_t end = min(ch * rpc + rpc, n);
+        uint32_t r = ch * rpc;
         while (r < end) {
             uint32_t my_row = 0;
             const uint32_t nr = gm.long_names ? 0u : gb_stage(calls, off, rows, r, end, lane, w, &my_row);
