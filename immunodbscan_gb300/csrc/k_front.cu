@@ -487,7 +487,20 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
              unsigned long long *tab, uint32_t tmask, uint32_t *__restrict__ ref,
              uint32_t *__restrict__ todo, uint32_t *n_todo) {
     extern __shared__ __align__(16) uint8_t sm[];
+    // rows that compute their own bitset, gathered per warp and appended to
+    // todo a batch at a time (one atomic per batch, not per window)
+    __shared__ uint32_t s_todo[kGbWarps][2 * kGbRows];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    uint32_t tcnt = 0;
+    auto flush_todo = [&]() {
+        __syncwarp();
+        uint32_t b0 = 0;
+        if (lane == 0 && tcnt) b0 = atomicAdd(n_todo, tcnt);
+        b0 = __shfl_sync(0xFFFFFFFFu, b0, 0);
+        for (uint32_t k = (uint32_t)lane; k < tcnt; k += 32) todo[b0 + k] = s_todo[wid][k];
+        __syncwarp();
+        tcnt = 0;
+    };
     const GbSlice w = cs_slice(sm, wid);
     const uint8_t *wb = w.bytes();
     const uint32_t nchunks = (N + kGbRows - 1) / kGbRows;
@@ -553,10 +566,11 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
             }
             if (own) myref = kNone;
             const uint32_t m = __ballot_sync(0xFFFFFFFFu, own);
-            uint32_t b0 = 0;
-            if (lane == 0 && m) b0 = atomicAdd(n_todo, (uint32_t)__popc(m));
-            b0 = __shfl_sync(0xFFFFFFFFu, b0, 0);
-            if (own) todo[b0 + __popc(m & ((1u << lane) - 1u))] = nr == 0 ? r : my_row;
+            if (m) {
+                if (tcnt + 32u > 2u * kGbRows) flush_todo();
+                if (own) s_todo[wid][tcnt + __popc(m & ((1u << lane) - 1u))] = nr == 0 ? r : my_row;
+                tcnt += (uint32_t)__popc(m);
+            }
             if (nr == 0) {
                 if (lane == 0) ref[r] = kNone;
                 ++r;
@@ -567,6 +581,7 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
             __syncwarp();
         }
     }
+    flush_todo();
 }
 
 // Rows that share a representative's string take its bitset.
