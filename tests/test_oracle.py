@@ -131,3 +131,33 @@ def test_library_eps_matches_reference_functor():
         ham = g["hamming"][k]
         for q in range(g["diag_len"] + 1):
             assert L.idb_diag_eps(q, q, C.c_float(t), -1) == ham[q], (t, q)
+
+
+def _segments(L, S):
+    return [(k * L // S, (k + 1) * L // S) for k in range(S)]
+
+
+@pytest.mark.parametrize("eps", [0, 1, 2])
+def test_segment_join_rule_emits_each_neighbour_pair_once(eps):
+    """The segment join's rule (k_buckets.cu join kernels, k_distance.cu
+    emission), restated on the host: with S = eps+1 segments
+    [kL/S, (k+1)L/S), two equal-length sequences within Hamming eps share at
+    least one identical segment, and exactly one group k passes the emission
+    test (segment k identical, no lower segment identical).  Includes lengths
+    below S (empty segments) and identical sequences."""
+    rng = np.random.default_rng(eps)
+    S = eps + 1
+    checked = 0
+    for _ in range(4000):
+        L = int(rng.integers(1, 40))
+        x = rng.integers(0, 4, size=L)
+        y = x.copy()
+        for p in rng.choice(L, size=min(L, int(rng.integers(0, eps + 1))), replace=False):
+            y[p] = (y[p] + 1 + rng.integers(0, 3)) % 4
+        assert int(np.sum(x != y)) <= eps
+        same = [bool(np.array_equal(x[lo:hi], y[lo:hi])) for lo, hi in _segments(L, S)]
+        assert any(same)                                    # pigeonhole
+        emit = [same[k] and not any(same[:k]) for k in range(S)]
+        assert sum(emit) == 1                               # emitted exactly once
+        checked += 1
+    assert checked == 4000
