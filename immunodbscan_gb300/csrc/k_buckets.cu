@@ -554,8 +554,7 @@ __global__ void k_join_clear(const Counters *__restrict__ ctr, uint32_t smax, ui
     const uint32_t n = join_mask(ctr->n_uniques, smax, cap_mask) + 1u;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        tab[i].key = ~0ull;
-        tab[i].cnt = 0u;
+        *reinterpret_cast<uint4 *>(&tab[i]) = make_uint4(~0u, ~0u, 0u, 0u);   // one 16-byte store
     }
 }
 

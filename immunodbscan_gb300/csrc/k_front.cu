@@ -41,10 +41,22 @@ __global__ void k_survey(const uint8_t *__restrict__ seq, const int64_t *__restr
     __syncthreads();
     uint32_t lmax = 0, lmin = 0xFFFFFFFFu;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
-        uint32_t L = (uint32_t)(off[i + 1] - off[i]);
-        lmax = max(lmax, L);
-        lmin = min(lmin, L);
+    // four rows (and below four 16-byte words) per step: their loads in flight together
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 < N; i0 += 4 * stride) {
+        int64_t a[4], b[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint64_t i = (uint64_t)i0 + (uint64_t)u * stride;
+            a[u] = i < N ? off[i] : 0;
+            b[u] = i < N ? off[i + 1] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if ((uint64_t)i0 + (uint64_t)u * stride < N) {
+                const uint32_t L = (uint32_t)(b[u] - a[u]);
+                lmax = max(lmax, L);
+                lmin = min(lmin, L);
+            }
     }
     // byte values present: 16 bytes per thread and step (aligned 16-byte loads,
     // the ragged ends byte by byte); values 64..127 (the letters) go to a
@@ -66,13 +78,22 @@ __global__ void k_survey(const uint8_t *__restrict__ seq, const int64_t *__restr
     for (int64_t p = b0 + gtid; p < head_end; p += stride) note(seq[p]);
     const int64_t nvec = b1 > head_end ? (b1 - head_end) >> 4 : 0;
     const uint4 *vec = reinterpret_cast<const uint4 *>(seq + head_end);
-    for (int64_t k = gtid; k < nvec; k += stride) {
-        const uint4 v = __ldg(vec + k);
-        const uint32_t w4[4] = {v.x, v.y, v.z, v.w};
+    for (int64_t k0 = gtid; k0 < nvec; k0 += 4 * (int64_t)stride) {
+        uint4 v[4];
 #pragma unroll
-        for (int e = 0; e < 4; ++e)
+        for (int u = 0; u < 4; ++u) {
+            const int64_t k = k0 + (int64_t)u * stride;
+            v[u] = k < nvec ? __ldg(vec + k) : make_uint4(0x41414141u, 0x41414141u, 0x41414141u, 0x41414141u);
+        }
 #pragma unroll
-            for (int q = 0; q < 4; ++q) note((w4[e] >> (8 * q)) & 0xFFu);
+        for (int u = 0; u < 4; ++u) {
+            if (k0 + (int64_t)u * stride >= nvec) break;
+            const uint32_t w4[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) note((w4[e] >> (8 * q)) & 0xFFu);
+        }
     }
     for (int64_t p = head_end + 16 * nvec + gtid; p < b1; p += stride) note(seq[p]);
     {
