@@ -177,6 +177,7 @@ def test_segment_join(gpu_ctx, eps, lo, hi):
     o = oracle.cluster(w)
     assert_same(g, o, w, f"segment join eps={eps} L={lo}-{hi}")
     assert g.stats.neighbour_pairs == o.neighbour_pairs
+    assert g.stats.candidates == (1 if eps <= 2 else 0)
 
 
 def test_nucleotide_two_planes(gpu_ctx):
