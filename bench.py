@@ -1,8 +1,11 @@
 """Throughput of the DBSCAN clone-collapsing path on GB300.
 
 Default workload: 64 synthetic amino-acid repertoires of log-uniform size
-5k-500k (~6M sequences), Hamming eps=1, minPts=2 -- the batched workload the
-throughput target is quoted on.  A step clusters all 64 repertoires.
+5k-500k (5.0M sequences), Hamming eps=1, minPts=2 -- the batched workload the
+throughput target is quoted on.  A step clusters all 64 repertoires; with
+Hamming eps <= 2 the library takes its candidate pairs from the segment join
+(`candidates` in the JSON line), which scores fewer pairs than the admissible
+count in the numerator.
 
 Metric: Gpair-distances/s = admissible unique pairs (V and J overlap, admissible
 length gap, counted once; a property of the workload, not of the schedule) per
