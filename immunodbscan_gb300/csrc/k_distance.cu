@@ -25,6 +25,12 @@
 //    never decreases, so the early exit is exact).
 //  * A neighbour pair is kept only in the bin of its lowest common V gene and
 //    lowest common J gene, so a pair that shares several bins counts once.
+//  * Segment join (Hamming, eps <= 2): the "bins" are groups of uniques that
+//    share one whole segment; a pair is kept only in the group of its lowest
+//    identical segment, and only if its V and J sets intersect.
+//  * Bin pairs of at most 32 entries a side are scored pair-parallel (records
+//    by shuffles), and a bin with itself of at most 8 entries by one lane.
+//  * Hits are queued per lane and written as one warp-compacted bulk append.
 #include "idb_internal.cuh"
 
 namespace idb {
