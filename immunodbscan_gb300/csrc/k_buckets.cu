@@ -21,6 +21,10 @@
 // pairs is canonical here and the pair of sub-buckets is not scheduled: a
 // family's internal pairs are evaluated once, in its lowest (V, J) bin, and not
 // again in each of the |V|*|J| bins it occupies.
+//
+// Hamming with eps <= 2 at every length takes its candidates from a segment
+// join instead (the k_join_* kernels below): groups of uniques that share one
+// whole segment of eps+1, which every neighbour pair does (pigeonhole).
 #include "idb_internal.cuh"
 
 namespace idb {
