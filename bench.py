@@ -63,6 +63,9 @@ def parse():
                          "workload (workload 3, 500k rows)")
     ap.add_argument("--static-only", action="store_true",
                     help="time the static schedule only (no network is trained)")
+    ap.add_argument("--candidates", default="auto", choices=["auto", "buckets"],
+                    help="candidate pairs: automatic (the segment join for Hamming eps <= 2) or "
+                         "every admissible pair of the buckets")
     ap.add_argument("--cpu-seconds", type=float, default=None,
                     help="CPU time budget of the oracle sample (per step for --impl reference; "
                          "default 10 s, or 150 s / steps for the reference arm)")
@@ -303,6 +306,7 @@ def main():
     from immunodbscan_gb300 import synth
     t0 = time.time()
     w = synth.workload(args.workload, scale=args.scale)
+    w.candidates = 1 if args.candidates == "buckets" else 0
     gen_s = time.time() - t0
     if args.impl == "reference":
         reference_arm(args, world, rank, w)
@@ -319,7 +323,8 @@ def main():
 
     # numerator: admissible unique pairs (setup, untimed)
     inp, keep = build_host_input(w, pinned=False)
-    prm0 = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming)
+    prm0 = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming,
+                       candidates=w.candidates)
     adm = C.c_uint64()
     _lib.check(L.idb_count_admissible(ctx_setup.handle, C.byref(inp), C.byref(prm0), C.byref(adm)))
     admissible = int(adm.value)
@@ -340,6 +345,7 @@ def main():
     loss = float("nan")
     if learn:
         wt = synth.workload(args.workload, scale=min(args.scale, 0.1), seed=4242 + args.workload)
+        wt.candidates = w.candidates
         X, T = learned.profile(wt, ctx_setup, tune=shape)
         params, loss = learned.train(X, T, ctx_setup, epochs=args.mlp_epochs)
         learned.install(ctx_learned, params)
@@ -458,7 +464,8 @@ def main():
     # e2e through idb_cluster (the InterlinkClass replacement) with pinned host buffers
     if not args.no_e2e:
         hin, hkeep = build_host_input(w, pinned=True)
-        prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, int(learn), shape)
+        prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, int(learn), shape,
+                          w.candidates)
         clone = torch.empty(n, dtype=torch.int32).pin_memory()
         core = torch.empty(n, dtype=torch.int32).pin_memory()
         copies = torch.empty(n, dtype=torch.int32).pin_memory()

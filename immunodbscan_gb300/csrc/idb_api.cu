@@ -179,6 +179,8 @@ idb_status validate(const idb_input *in, const idb_params *prm, const idb_output
         return fail(IDB_ERR_UNSUPPORTED, "at most %d J reference genes", 64 * kMaxGeneWords);
     if (std::isnan(prm->threshold) && prm->abs_eps < 0)
         return fail(IDB_ERR_INVALID_ARG, "neither threshold nor abs_eps is set");
+    if (prm->candidates != 0 && prm->candidates != 1)
+        return fail(IDB_ERR_INVALID_ARG, "candidates must be 0 (automatic) or 1 (buckets)");
     if (in->n_repertoires > 0 && in->rep_offsets) {
         if (in->rep_offsets[0] != 0 || in->rep_offsets[in->n_repertoires] != in->n_rows)
             return fail(IDB_ERR_INVALID_ARG, "rep_offsets must start at 0 and end at n_rows");
@@ -436,7 +438,7 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
     // Hamming with a small eps at every length: candidate pairs by segment join
     // (the side records then carry the V bits and the J bits with the segment;
     // a key holds the repertoire in 24 bits and the table at most 2^31 slots)
-    P.join = pl.allow_join && P.hamming && P.fast && emax_same <= kJoinMaxEps &&
+    P.join = pl.allow_join && prm->candidates == 0 && P.hamming && P.fast && emax_same <= kJoinMaxEps &&
              P.Gv <= 64 && P.Gj <= 30 && P.R < (1u << 24) - 1 &&
              2ull * (uint64_t)(emax_same + 1) * P.N <= (1ull << 30);
     P.join_smax = P.join ? (uint32_t)std::max(1, emax_same + 1) : 1u;

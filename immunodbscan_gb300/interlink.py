@@ -73,7 +73,7 @@ class Context:
 
 
 def make_params(threshold=float("nan"), abs_eps=-1, min_pts=2, use_hamming=False,
-                eval_trees=False, schedule=0, tune=None) -> Params:
+                eval_trees=False, schedule=0, tune=None, candidates=0) -> Params:
     p = Params()
     p.threshold = float(threshold) if threshold is not None else math.nan
     p.abs_eps = int(abs_eps)
@@ -84,6 +84,7 @@ def make_params(threshold=float("nan"), abs_eps=-1, min_pts=2, use_hamming=False
     if tune:
         p.tile_rx = int(tune[0])
         p.tile_ty = int(tune[1])
+    p.candidates = int(candidates)
     return p
 
 
@@ -114,7 +115,8 @@ class Interlink:
     def __init__(self, v_calls, j_calls, seqs, n_entries: int, v_genes_reference,
                  j_genes_reference, threshold: float, min_pts: int, use_only_hamming: bool,
                  eval_trees: bool = False, *, abs_eps: int = -1, rep_sizes=None,
-                 context: Optional[Context] = None, schedule: int = 0, tune=None):
+                 context: Optional[Context] = None, schedule: int = 0, tune=None,
+                 candidates: int = 0):
         n = int(n_entries)
         keep = []
         inp = Input()
@@ -148,7 +150,8 @@ class Interlink:
             keep.append(roff)
             inp.n_repertoires = len(rep_sizes)
             inp.rep_offsets = _p(roff)
-        prm = make_params(threshold, abs_eps, min_pts, use_only_hamming, eval_trees, schedule, tune)
+        prm = make_params(threshold, abs_eps, min_pts, use_only_hamming, eval_trees, schedule, tune,
+                          candidates)
         self._result = _run(inp, prm, n, context, eval_trees)
 
     # getters of cuda/Interlink.hpp:59-63
@@ -194,7 +197,8 @@ def cluster_workload(w, context: Optional[Context] = None, *, schedule: int = 0,
                    None if no_seq else (w.seq_blob, w.seq_off), w.n, w.v_genes, w.j_genes,
                    w.threshold, w.min_pts, w.use_hamming, eval_trees, abs_eps=w.abs_eps,
                    rep_sizes=np.diff(w.rep_off).tolist() if w.n_rep > 1 else None,
-                   context=context, schedule=schedule, tune=tune)
+                   context=context, schedule=schedule, tune=tune,
+                   candidates=w.candidates)
     return it.result
 
 
@@ -235,7 +239,8 @@ class DeviceBatch:
         inp.n_repertoires = w.n_rep
         inp.rep_offsets = _p(roff)
         self.inp = inp
-        self.prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, schedule, tune)
+        self.prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, schedule, tune,
+                               w.candidates)
         self.out = Output(_p(self.clone), _p(self.core), _p(self.copies), None, None, None, None)
 
     def cluster_once(self) -> Stats:

@@ -59,7 +59,8 @@ def forward(p: np.ndarray, X: np.ndarray) -> np.ndarray:
 
 def profile(w, ctx: Optional[Context] = None, tune=None) -> Tuple[np.ndarray, np.ndarray]:
     inp, keep = _input(w)
-    prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, tune=tune)
+    prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, tune=tune,
+                      candidates=w.candidates)
     cap = 1 << 22
     X = np.zeros((cap, F), np.float32)
     T = np.zeros(cap, np.float32)

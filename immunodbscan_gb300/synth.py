@@ -52,6 +52,7 @@ class Workload:
     rep_off: np.ndarray           # uint32 [R+1]
     alphabet: bytes = AA
     seed: int = 0
+    candidates: int = 0           # 0 = automatic candidate pairs, 1 = buckets only
 
     @property
     def n(self) -> int:

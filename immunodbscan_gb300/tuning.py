@@ -32,6 +32,7 @@ def workload_key(w) -> str:
         "words": max(1, (L + 31) // 32),
         "codes": "<=4" if codes <= 4 else ("<=32" if codes <= 32 else ">32"),
         "rows_log10": int(math.log10(max(w.n, 1))),
+        "candidates": int(w.candidates),
     }, sort_keys=True)
 
 
@@ -61,7 +62,8 @@ def _input(w):
 def measure(w, ctx: Optional[Context] = None) -> dict:
     """Run idb_autotune on the workload; returns the best shape and all timings."""
     inp, keep = _input(w)
-    prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming)
+    prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming,
+                      candidates=w.candidates)
     t = _lib.Tuning()
     _lib.check(_lib.lib().idb_autotune(ctx.handle if ctx else None, C.byref(inp), C.byref(prm),
                                        C.byref(t)))

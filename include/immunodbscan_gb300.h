@@ -60,7 +60,9 @@ typedef struct idb_params {
     int32_t  schedule;         /* 0 = static (pair-count) order, 1 = learned       */
     int32_t  tile_rx;          /* x-entries per lane of a work unit (0 = default)  */
     int32_t  tile_ty;          /* y-entries of a work unit (0 = default)           */
-    int32_t  reserved[4];
+    int32_t  candidates;       /* 0 = automatic (Hamming eps <= 2: segment join),
+                                  1 = every admissible pair of the buckets        */
+    int32_t  reserved[3];
 } idb_params;
 
 /* Input rows (cuda/Interlink.hpp:54-57: zip(V calls, J calls, sequences)). */

@@ -165,3 +165,16 @@ def test_mlp_cpu_gradient_is_exact():
         fd = (np.mean((learned.forward(pp, X) - T) ** 2) -
               np.mean((learned.forward(pm, X) - T) ** 2)) / (2 * h)
         assert abs(fd - g[k]) <= 1e-5 * max(1.0, abs(fd))
+
+
+def test_params_and_stats_mirror_the_header():
+    """The ctypes mirrors of idb_params and idb_stats follow the header's
+    layout (the candidate-path fields included)."""
+    import ctypes as C
+    from immunodbscan_gb300 import _lib
+    hdr = open(os.path.join(ROOT, "include", "immunodbscan_gb300.h")).read()
+    assert "int32_t  candidates;" in hdr and "uint32_t candidates;" in hdr
+    assert _lib.Params.candidates.offset == 8 * 4
+    assert C.sizeof(_lib.Params) == 12 * 4
+    assert _lib.Stats.candidates.offset == _lib.Stats.lev_columns.offset + 8
+    assert C.sizeof(_lib.Stats) % 8 == 0

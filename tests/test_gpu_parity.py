@@ -336,3 +336,18 @@ def test_gene_bits_synthetic(gpu_ctx):
     calls = [w.vcall(i) for i in range(w.n)]
     got = _as_words32(_gpu_bits(gpu_ctx, calls, w.v_genes), len(w.v_genes))
     assert np.array_equal(got, oracle.gene_bitsets(calls, w.v_genes))
+
+
+def test_candidates_buckets_same_partition(gpu_ctx):
+    """idb_params.candidates = 1 scores every admissible pair of the buckets
+    instead of the segment join; the answer is the same."""
+    w = synth.workload(2, scale=0.004)
+    g0 = cluster_workload(w, gpu_ctx)
+    w.candidates = 1
+    g1 = cluster_workload(w, gpu_ctx)
+    assert g0.stats.candidates == 1 and g1.stats.candidates == 0
+    assert g1.stats.pairs_evaluated > g0.stats.pairs_evaluated
+    assert g0.stats.neighbour_pairs == g1.stats.neighbour_pairs
+    assert np.array_equal(g0.clone_id, g1.clone_id)
+    assert np.array_equal(g0.core, g1.core)
+    assert np.array_equal(g0.copies, g1.copies)
