@@ -62,6 +62,7 @@ class Benchmark {
 // Configuration keys (cpp/ConfigHolder.hpp:65-259).  Added optional keys:
 //   maximum_absolute_edit_distance  int, caps eps (or replaces the relative key)
 //   work_schedule                   "static" (default) or "learned"
+//   candidate_pairs                 "auto" (default) or "buckets"
 // ---------------------------------------------------------------------------
 class Config {
     InfoNode tree_;
@@ -112,6 +113,13 @@ class Config {
         if (s == "static") return 0;
         if (s == "learned") return 1;
         throw std::runtime_error("work_schedule must be static or learned");
+    }
+    int candidates() const {
+        if (!tree_.has("candidate_pairs")) return 0;
+        const std::string &s = tree_.get("candidate_pairs");
+        if (s == "auto") return 0;
+        if (s == "buckets") return 1;
+        throw std::runtime_error("candidate_pairs must be auto or buckets");
     }
     // gene_columns.first_gene.name etc.; "" when not configured
     std::string opt(const std::string &p) const { return tree_.has(p) ? tree_.get(p) : std::string(); }
@@ -243,6 +251,7 @@ class Table {
         prm.use_hamming = cfg_.flag("use_hamming", false);
         prm.eval_trees = cfg_.flag("get_tree_depth_statistics", false);
         prm.schedule = cfg_.schedule();
+        prm.candidates = cfg_.candidates();
         bm.message("DBSCAN settings: epsilon = " + std::to_string(prm.threshold));
         bm.message("DBSCAN settings: minPts = " + std::to_string(prm.min_pts));
         if (prm.use_hamming)

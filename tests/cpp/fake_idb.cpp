@@ -1,8 +1,10 @@
 // A stand-in for libimmunodbscan_gb300 with the three entry points psdbscan
 // calls, so the host's table flow (read, delete empty rows, append results,
 // noise removal, write) runs on a machine without a GPU.  Row r gets
-// clone_id = r % 3, core = r % 2 and copies = 1 + r % 4; its V call's length is
-// folded into the stats so the tests can see the columns arrived.
+// clone_id = r % 3, core = r % 2 and copies = 1 + r % 4 (copies = 7 when the
+// parameters ask for the buckets-only candidate path, so the tests can see the
+// key arrive); its V call's length is folded into the stats so the tests can
+// see the columns arrived.
 #include <cstdio>
 #include <cstring>
 
@@ -15,7 +17,7 @@ idb_status idb_cluster(idb_context *, const idb_input *in, const idb_params *prm
     for (uint32_t r = 0; r < in->n_rows; ++r) {
         out->clone_id[r] = r % 3;
         out->core[r] = (int32_t)(r % 2);
-        out->copies[r] = 1 + r % 4;
+        out->copies[r] = prm->candidates == 1 ? 7u : 1 + r % 4;
     }
     if (out->n_uniques) *out->n_uniques = in->n_rows;
     if (out->stats) {

@@ -178,3 +178,38 @@ def test_params_and_stats_mirror_the_header():
     assert C.sizeof(_lib.Params) == 12 * 4
     assert _lib.Stats.candidates.offset == _lib.Stats.lev_columns.offset + 8
     assert C.sizeof(_lib.Stats) % 8 == 0
+
+
+def test_psdbscan_candidate_pairs_key(tmp_path):
+    """The optional INFO key candidate_pairs reaches idb_params.candidates
+    ("buckets" -> 1; the stand-in library then reports copies 7 on every row),
+    and an unknown value stops the host with a message."""
+    import sys
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from test_gpu_cli import _write_inputs
+    from immunodbscan_gb300 import synth
+    d = tmp_path / "bin"
+    d.mkdir()
+    inc = ["-I", os.path.join(ROOT, "include")]
+    subprocess.run(["g++", "-std=c++17", "-O1", "-shared", "-fPIC", *inc,
+                    os.path.join(ROOT, "tests", "cpp", "fake_idb.cpp"), "-o",
+                    str(d / "libimmunodbscan_gb300.so")], check=True)
+    subprocess.run(["g++", "-std=c++17", "-O1", *inc, "-I", os.path.join(ROOT, "immunodbscan_gb300", "host"),
+                    os.path.join(ROOT, "immunodbscan_gb300", "host", "psdbscan.cpp"), "-o",
+                    str(d / "psdbscan"), "-L" + str(d), "-limmunodbscan_gb300", "-Wl,-rpath,$ORIGIN"],
+                   check=True)
+    w = synth.workload(0, scale=0.02)
+    cf, inp, keep = _write_inputs(tmp_path, w, True, False)
+    base = cf.read_text()
+    cf.write_text(base + "\ncandidate_pairs buckets\n")
+    r = subprocess.run([str(d / "psdbscan"), "--config_file", str(cf), "--input", str(inp)],
+                       capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = (tmp_path / "output_repertoire.csv").read_text().split("\n")
+    copies = lines[0].split("\t").index("Copies")
+    assert len(lines) > 3 and all(l.split("\t")[copies] == "7" for l in lines[1:-1])
+    cf.write_text(base + "\ncandidate_pairs sideways\n")
+    r = subprocess.run([str(d / "psdbscan"), "--config_file", str(cf), "--input", str(inp)],
+                       capture_output=True, text=True, cwd=str(tmp_path))
+    assert r.returncode != 0
+    assert "candidate_pairs must be auto or buckets" in (r.stdout + r.stderr)
