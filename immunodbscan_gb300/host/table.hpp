@@ -78,7 +78,7 @@ class Config {
         return as_char(tree_.child(names[f]).get(what), std::string(names[f]) + "." + what);
     }
     std::string filename(const std::string &main, FileSel f) const {
-        // path + prefix + stem + suffix + filetype (cpp/ConfigHolder.hpp:355-379)
+        // path + prefix + stem + suffix + filetype (cpp/ConfigHolder.hpp:42-48, 89-113)
         const std::string path = main.substr(0, main.find_last_of('/') + 1);
         std::string stem = main.substr(0, main.find_last_of('.'));
         stem = stem.substr(stem.find_last_of('/') + 1);
@@ -180,7 +180,7 @@ class Table {
         Benchmark::instance().message("Deleting empty rows for column " + name);
         delete_rows(del);
     }
-    // append_column with make_output_string = std::to_string (cpp/TableHolder.hpp:150-160, 221-227)
+    // append_column with make_output_string = std::to_string (cpp/TableHolder.hpp:56-66, 126-131)
     template <typename T>
     void append(const std::string &name, const std::vector<T> &v) {
         std::vector<std::string> col(rows());
@@ -192,7 +192,7 @@ class Table {
         cols_.push_back(std::move(col));
     }
 
-    // cpp/TableHolder.hpp:370-443
+    // cpp/TableHolder.hpp:275-348
     void cluster() {
         Benchmark &bm = Benchmark::instance();
         bm.start("Deleting Empty Rows");
@@ -290,7 +290,7 @@ class Table {
         append("cores", cores);
     }
 
-    // cpp/TableHolder.hpp:312-366
+    // cpp/TableHolder.hpp:217-271
     void write() {
         const char sep = cfg_.special(Config::Output, "separator");
         const char eol = cfg_.special(Config::Output, "endline");

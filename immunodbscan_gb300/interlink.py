@@ -105,8 +105,8 @@ class Interlink:
     use_only_hamming, eval_trees).
 
     ``v_calls`` / ``j_calls`` may be None (gene column not configured: every row
-    matches the single gene "V", cpp/TableHolder.hpp:388-391); ``seqs`` may be
-    None (every row is "Gene", cpp/TableHolder.hpp:421-423).  ``abs_eps`` is the
+    matches the single gene "V", cpp/TableHolder.hpp:293-296); ``seqs`` may be
+    None (every row is "Gene", cpp/TableHolder.hpp:326-328).  ``abs_eps`` is the
     added absolute threshold (-1 = unused); ``threshold`` may be NaN when only
     ``abs_eps`` is used.  ``rep_sizes`` splits the rows into independent
     repertoires (clone ids numbered per repertoire).

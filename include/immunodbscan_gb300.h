@@ -69,12 +69,12 @@ typedef struct idb_params {
 typedef struct idb_input {
     uint32_t n_rows;
     /* V and J gene calls; NULL data = column not configured: every row matches
-       the single gene "V" (cpp/TableHolder.hpp:388-391, 406-409). */
+       the single gene "V" (cpp/TableHolder.hpp:293-296, 311-314). */
     const char    *v_calls;
     const int64_t *v_offsets;
     const char    *j_calls;
     const int64_t *j_offsets;
-    /* sequences; NULL = every row is "Gene" (cpp/TableHolder.hpp:421-423) */
+    /* sequences; NULL = every row is "Gene" (cpp/TableHolder.hpp:326-328) */
     const char    *seqs;
     const int64_t *seq_offsets;
     /* reference gene names (cpp/GeneReader.hpp:65-76), host memory always */

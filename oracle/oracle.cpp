@@ -210,8 +210,8 @@ extern "C" int ora_cluster(uint32_t n_rows,
 #ifdef _OPENMP
     if (prm->n_threads > 0) omp_set_num_threads(prm->n_threads);
 #endif
-    // Missing gene columns: every row "V" against ["V"] (cpp/TableHolder.hpp:388-391,
-    // :406-409); missing sequence column: every row "Gene" (:421-423).
+    // Missing gene columns: every row "V" against ["V"] (cpp/TableHolder.hpp:293-296,
+    // :311-314); missing sequence column: every row "Gene" (:326-328).
     Rows R;
     R.n = n_rows;
     R.seq = StrCol{s_data, s_off, "Gene"};

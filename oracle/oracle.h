@@ -14,9 +14,9 @@
  *
  * All strings are passed as a byte blob plus int64 offsets (n+1 entries).
  * A NULL gene-call blob means "gene column not configured": every row gets
- * the call "V" and the reference list ["V"] (cpp/TableHolder.hpp:388-391).
+ * the call "V" and the reference list ["V"] (cpp/TableHolder.hpp:293-296).
  * A NULL sequence blob means every row carries the sequence "Gene"
- * (cpp/TableHolder.hpp:421-423).
+ * (cpp/TableHolder.hpp:326-328).
  */
 #pragma once
 #include <stdint.h>

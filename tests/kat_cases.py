@@ -115,7 +115,7 @@ def cases():
 
 
 def no_seq_case():
-    """No sequence column: every row is "Gene" (cpp/TableHolder.hpp:421-423)."""
+    """No sequence column: every row is "Gene" (cpp/TableHolder.hpp:326-328)."""
     w = from_strings([b"Gene"] * 3, [b"IGHV1-2*01", b"IGHV1-2*01", b"IGHV3-23*01"], None, V3, [],
                      abs_eps=1, min_pts=2, use_hamming=True)
     return w, dict(clone=[1, 1, 0], core=[1, 0, 0], copies=[2, 0, 1])

@@ -1,6 +1,6 @@
 """psdbscan end to end: TSV in -> clustering on the GPU -> TSV out, checked
 against the oracle on the rows that survive the empty-value deletion
-(cpp/TableHolder.hpp:378-380) -- including the empty row the reader appends for
+(cpp/TableHolder.hpp:283-285) -- including the empty row the reader appends for
 the file's final newline (cpp/csvreader.hpp:152-180)."""
 import os
 import subprocess

@@ -351,3 +351,17 @@ def test_candidates_buckets_same_partition(gpu_ctx):
     assert np.array_equal(g0.clone_id, g1.clone_id)
     assert np.array_equal(g0.core, g1.core)
     assert np.array_equal(g0.copies, g1.copies)
+
+
+import ref_fixtures  # noqa: E402
+
+
+@pytest.mark.parametrize("name", ref_fixtures.names())
+def test_reference_fixtures(gpu_ctx, name):
+    """The library against the reference's own answers (its InterlinkClass on
+    the same rows): clone ids, cores, copies, uniques, and the parts of the
+    tree-depth histogram that do not depend on the union order."""
+    _, w, want = next(c for c in ref_fixtures.load() if c[0] == name)
+    r = cluster_workload(w, gpu_ctx, eval_trees=True)
+    ref_fixtures.assert_matches(name, want, r.clone_id, r.core, r.copies,
+                                uniques=r.uniques[: r.n_uniques], hist=r.tree_depth_hist)

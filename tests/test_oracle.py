@@ -4,6 +4,7 @@ These pin the oracle (the reference ships no tests or fixtures; its CUDA path
 cannot run here), which then serves as the checker for the GPU path.
 """
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -161,3 +162,40 @@ def test_segment_join_rule_emits_each_neighbour_pair_once(eps):
         assert sum(emit) == 1                               # emitted exactly once
         checked += 1
     assert checked == 4000
+
+
+# --- the oracle against the reference's own code -------------------------------
+
+import ref_fixtures  # noqa: E402
+
+
+@pytest.mark.parametrize("name", ref_fixtures.names())
+def test_oracle_matches_reference_fixtures(name):
+    """Golden answers of the reference's InterlinkClass (relative threshold,
+    Hamming and Levenshtein modes, minPts 0-5, ambiguous and unmatched gene
+    calls, missing gene columns, several repertoires)."""
+    _, w, want = next(c for c in ref_fixtures.load() if c[0] == name)
+    r = oracle.cluster(w)
+    ref_fixtures.assert_matches(name, want, r.clone_id, r.core, r.copies,
+                                uniques=np.nonzero(r.copies)[0])
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_oracle_matches_live_reference(seed):
+    """Fresh random cases through the reference's own code, when its tree is
+    available (IDB_REFERENCE_TREE); the fixtures above cover every other run."""
+    import ref_run
+    if not ref_run.available():
+        pytest.skip("IDB_REFERENCE_TREE does not name a reference tree")
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    from make_ref_golden import _random_case
+    rng = np.random.default_rng(seed)
+    hamming = bool(seed % 2)
+    alphabet = list(b"ACGT") if seed != 12 else list(b"ACDEFGHIKLMNPQRSTVWY")
+    w = _random_case(seed, 300, 4, 10, alphabet, hamming, float(rng.choice([0.1, 0.2, 0.3])),
+                     int(rng.integers(1, 5)), 30)
+    want = ref_run.run(w)
+    r = oracle.cluster(w)
+    assert np.array_equal(r.copies, want.copies)
+    assert np.array_equal(r.core, want.core)
+    assert np.array_equal(r.clone_id, want.clone_id)
