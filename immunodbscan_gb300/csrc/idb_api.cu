@@ -96,6 +96,32 @@ struct idb_context {
     // learned schedule: MLP parameters (BF16 for inference)
     void *mlp_bf16 = nullptr;
     bool has_model = false;
+    // bumped whenever a workspace buffer moves: a graph captured at another
+    // generation would read freed memory and is not replayed
+    uint64_t generation = 0;
+    uint64_t batch_generation = 0;
+    // bumped by every call that stages inputs: the staged gene tables,
+    // repertoire offsets and columns a graph reads are those of that call
+    uint64_t stage_epoch = 0;
+    uint64_t batch_epoch = 0;
+    // idb_cluster's plan cache (host inputs): the launch sequence of the last
+    // input shape, captured after an eager call and replayed by later calls
+    // with the same shape (see host_plan_*)
+    struct HostPlan {
+        bool valid = false;
+        uint64_t generation = 0, epoch = 0;
+        uint32_t N = 0, R = 0;
+        std::vector<uint32_t> roff;
+        idb_params prm{};
+        bool no_v = false, no_j = false, no_seq = false, uniques = false, model = false;
+        std::vector<char> vgenes, jgenes;
+        std::vector<int64_t> vgoff, jgoff;
+        Plan P;
+        Buffers B;
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        uint32_t kernels = 0;
+    } hp;
 };
 
 namespace {
@@ -107,6 +133,7 @@ idb_status ensure(idb_context *c, BufId id, size_t bytes, bool exact = false) {
     if (b.p) CU(cudaFree(b.p));
     b.p = nullptr;
     b.cap = 0;
+    ++c->generation;
     size_t want = exact ? bytes : bytes + bytes / 8 + 256;
     want = (want + 255) & ~(size_t)255;
     cudaError_t e = cudaMalloc(&b.p, want);
@@ -197,6 +224,7 @@ idb_status validate(const idb_input *in, const idb_params *prm, const idb_output
 idb_status upload_genes(idb_context *c, const char *names, const int64_t *off, uint32_t G,
                         BufId blob_id, BufId off_id, BufId tab_id, uint32_t *bytes_out,
                         GeneMatcher *gm) {
+    ++c->stage_epoch;   // the gene tables a captured graph reads are replaced
     std::vector<int32_t> o(G + 1);
     const int64_t base = G ? off[0] : 0;
     for (uint32_t g = 0; g <= G; ++g) o[g] = (int32_t)(off[g] - base);
@@ -270,6 +298,7 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
     Plan &P = pl.P;
     Buffers &B = pl.B;
     cudaStream_t s = c->stream;
+    ++c->stage_epoch;
     P.N = in->n_rows;
     P.R = (in->n_repertoires > 0 && in->rep_offsets) ? in->n_repertoires : 1;
     P.no_v = in->v_calls == nullptr;
@@ -693,6 +722,215 @@ idb_status fill_stats(Pipeline &pl, idb_stats *st) {
     return IDB_OK;
 }
 
+// ---------------------------------------------------------------------------
+// idb_cluster's plan cache.  An eager call reads sizes back from the device
+// between phases (survey, bucket entries, bin pairs, edge overflow) and so
+// waits on the device several times.  When a second call arrives with the same
+// shape -- row count, repertoire offsets, gene lists, parameters, which columns
+// are present -- its eager run is followed by a capture of the whole launch
+// sequence with capacities of the graph path (idb_batch_plan); later calls of
+// that shape copy their columns into the same staging buffers and replay the
+// graph, with one wait at the end.  The graph starts with the plan check
+// (k_check_plan): data whose lengths or byte alphabet fall outside the plan,
+// or that outgrows a capacity, reports IDB_ERR_REPLAN / IDB_ERR_CAPACITY and
+// the call runs eagerly instead, so a replay never changes an answer.
+
+bool same_params(const idb_params &a, const idb_params &b) {
+    uint32_t ta, tb;
+    std::memcpy(&ta, &a.threshold, 4);
+    std::memcpy(&tb, &b.threshold, 4);
+    return ta == tb && a.abs_eps == b.abs_eps && a.min_pts == b.min_pts &&
+           a.use_hamming == b.use_hamming && a.schedule == b.schedule && a.tile_rx == b.tile_rx &&
+           a.tile_ty == b.tile_ty && a.candidates == b.candidates;
+}
+
+void gene_key(const char *names, const int64_t *off, uint32_t G, std::vector<char> &b,
+              std::vector<int64_t> &o) {
+    o.assign((size_t)G + 1, 0);
+    const int64_t base = G ? off[0] : 0;
+    for (uint32_t g = 0; g <= G; ++g) o[g] = off[g] - base;
+    b.assign(G ? names + base : nullptr, G ? names + base + o[G] : nullptr);
+}
+
+bool same_genes(const char *names, const int64_t *off, uint32_t G, const std::vector<char> &b,
+                const std::vector<int64_t> &o) {
+    if (o.size() != (size_t)G + 1) return false;
+    const int64_t base = G ? off[0] : 0;
+    for (uint32_t g = 0; g <= G; ++g)
+        if (off[g] - base != o[g]) return false;
+    return !G || std::memcmp(names + base, b.data(), (size_t)o[G]) == 0;
+}
+
+// Does this call have the shape of the cached key?
+bool host_plan_key_matches(const idb_context *c, const idb_input *in, const idb_params *prm,
+                           const idb_output *out) {
+    const auto &h = c->hp;
+    const uint32_t R = (in->n_repertoires > 0 && in->rep_offsets) ? in->n_repertoires : 1;
+    if (h.N != in->n_rows || h.R != R || h.roff.size() != (size_t)R + 1) return false;
+    if (h.no_v != (in->v_calls == nullptr) || h.no_j != (in->j_calls == nullptr) ||
+        h.no_seq != (in->seqs == nullptr) || h.uniques != (out->uniques != nullptr))
+        return false;
+    if (!same_params(h.prm, *prm)) return false;
+    if (in->n_repertoires > 0 && in->rep_offsets) {
+        if (std::memcmp(h.roff.data(), in->rep_offsets, 4 * ((size_t)R + 1)) != 0) return false;
+    } else if (h.roff[0] != 0 || h.roff[1] != in->n_rows) {
+        return false;
+    }
+    if (!h.no_v && !same_genes(in->v_genes, in->v_gene_offsets, in->n_v_genes, h.vgenes, h.vgoff))
+        return false;
+    if (!h.no_j && !same_genes(in->j_genes, in->j_gene_offsets, in->n_j_genes, h.jgenes, h.jgoff))
+        return false;
+    return true;
+}
+
+void host_plan_set_key(idb_context *c, const idb_input *in, const idb_params *prm,
+                       const idb_output *out) {
+    auto &h = c->hp;
+    h.N = in->n_rows;
+    h.R = (in->n_repertoires > 0 && in->rep_offsets) ? in->n_repertoires : 1;
+    if (in->n_repertoires > 0 && in->rep_offsets) h.roff.assign(in->rep_offsets, in->rep_offsets + h.R + 1);
+    else h.roff = {0u, in->n_rows};
+    h.no_v = in->v_calls == nullptr;
+    h.no_j = in->j_calls == nullptr;
+    h.no_seq = in->seqs == nullptr;
+    h.uniques = out->uniques != nullptr;
+    h.prm = *prm;
+    if (!h.no_v) gene_key(in->v_genes, in->v_gene_offsets, in->n_v_genes, h.vgenes, h.vgoff);
+    if (!h.no_j) gene_key(in->j_genes, in->j_gene_offsets, in->n_j_genes, h.jgenes, h.jgoff);
+    h.valid = true;
+}
+
+void host_plan_drop_graph(idb_context *c) {
+    auto &h = c->hp;
+    if (h.exec) cudaGraphExecDestroy(h.exec);
+    if (h.graph) cudaGraphDestroy(h.graph);
+    h.exec = nullptr;
+    h.graph = nullptr;
+}
+
+uint32_t graph_kernel_count(cudaGraph_t g) {
+    size_t nn = 0;
+    if (cudaGraphGetNodes(g, nullptr, &nn) != cudaSuccess) return 0;
+    std::vector<cudaGraphNode_t> nodes(nn);
+    if (cudaGraphGetNodes(g, nodes.data(), &nn) != cudaSuccess) return 0;
+    uint32_t k = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess) k += t == cudaGraphNodeTypeKernel;
+    }
+    return k;
+}
+
+// After a successful eager call of the cached shape: capacities with headroom,
+// then the capture of the launch sequence over the staging buffers.
+idb_status host_plan_capture(Pipeline &pl) {
+    idb_context *c = pl.c;
+    auto &h = c->hp;
+    host_plan_drop_graph(c);
+    const Counters hc = *c->h_ctr;
+    TRY(alloc_entries(pl, (uint64_t)hc.n_entries + hc.n_entries / 16 + 1024));
+    TRY(alloc_binpairs(pl, (uint64_t)hc.n_binpairs + hc.n_binpairs / 16 + 1024));
+    TRY(alloc_edges(pl, (uint64_t)hc.edge_reserved + hc.edge_reserved / 8 + 64ull * kEdgeChunk * 1024));
+    cudaStream_t s = c->stream;
+    CU(cudaStreamSynchronize(s));
+    pl.timing = true;
+    pl.trees = false;
+    pl.wait_v = pl.wait_j = nullptr;
+    CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    cudaMemsetAsync(pl.B.ctr, 0, sizeof(Counters), s);
+    cudaMemsetAsync(&pl.B.ctr->lmin, 0xFF, sizeof(uint32_t), s);
+    record(pl, 0);
+    launch_survey(pl.P, pl.B, s);
+    idb_status st = run_phases(pl, false);
+    cudaGraph_t g = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (st != IDB_OK) {
+        if (g) cudaGraphDestroy(g);
+        return st;
+    }
+    if (ce != cudaSuccess) return fail(IDB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    h.graph = g;
+    CU(cudaGraphInstantiate(&h.exec, g, 0));
+    h.kernels = graph_kernel_count(g);
+    h.P = pl.P;
+    h.B = pl.B;
+    h.model = c->has_model;
+    h.generation = c->generation;
+    h.epoch = c->stage_epoch;
+    return IDB_OK;
+}
+
+// Replay for host inputs of the cached shape.  IDB_ERR_REPLAN / IDB_ERR_CAPACITY
+// send the call to the eager path.
+idb_status host_plan_run(idb_context *c, const idb_input *in, idb_output *out) {
+    auto &h = c->hp;
+    const size_t N = h.N;
+    // the staging buffers must hold this call's columns without moving
+    auto fits = [&](BufId bid, BufId oid, const int64_t *off) {
+        return c->buf[bid].cap >= (size_t)off[N] + 16 && c->buf[oid].cap >= 8 * (N + 1);
+    };
+    if ((!h.no_seq && !fits(bSeq, bSeqOff, in->seq_offsets)) ||
+        (!h.no_v && !fits(bV, bVOff, in->v_offsets)) || (!h.no_j && !fits(bJ, bJOff, in->j_offsets)))
+        return fail(IDB_ERR_CAPACITY, "columns larger than the cached plan's staging buffers");
+    cudaStream_t s = c->stream, cs = c->copy_stream;
+    struct CopyGuard {   // no copy from the caller's buffers stays in flight
+        cudaStream_t cs;
+        ~CopyGuard() { cudaStreamSynchronize(cs); }
+    } guard{cs};
+    if (!h.no_seq) {
+        if (in->seq_offsets[N])
+            CU(cudaMemcpyAsync(c->buf[bSeq].p, in->seqs, (size_t)in->seq_offsets[N],
+                               cudaMemcpyHostToDevice, s));
+        CU(cudaMemcpyAsync(c->buf[bSeqOff].p, in->seq_offsets, 8 * (N + 1), cudaMemcpyHostToDevice, s));
+    }
+    if (!h.no_v) {
+        if (in->v_offsets[N])
+            CU(cudaMemcpyAsync(c->buf[bV].p, in->v_calls, (size_t)in->v_offsets[N],
+                               cudaMemcpyHostToDevice, cs));
+        CU(cudaMemcpyAsync(c->buf[bVOff].p, in->v_offsets, 8 * (N + 1), cudaMemcpyHostToDevice, cs));
+    }
+    if (!h.no_j) {
+        if (in->j_offsets[N])
+            CU(cudaMemcpyAsync(c->buf[bJ].p, in->j_calls, (size_t)in->j_offsets[N],
+                               cudaMemcpyHostToDevice, cs));
+        CU(cudaMemcpyAsync(c->buf[bJOff].p, in->j_offsets, 8 * (N + 1), cudaMemcpyHostToDevice, cs));
+    }
+    CU(cudaEventRecord(c->ev_v, cs));
+    CU(cudaStreamWaitEvent(s, c->ev_v, 0));
+    CU(cudaEventRecord(c->ev[0], s));
+    CU(cudaGraphLaunch(h.exec, s));
+    CU(cudaEventRecord(c->ev[1], s));
+    const Buffers &B = h.B;
+    CU(cudaMemcpyAsync(c->h_ctr, B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(out->clone_id, B.clone_id, 4 * N, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(out->core, B.core, 4 * N, cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(out->copies, B.copies, 4 * N, cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    TRY(device_errors(*c->h_ctr));
+    const Counters &hc = *c->h_ctr;
+    if (out->uniques) CU(cudaMemcpy(out->uniques, B.uniques, 4 * (size_t)hc.n_uniques, cudaMemcpyDeviceToHost));
+    if (out->n_uniques) *out->n_uniques = hc.n_uniques;
+    if (out->stats) {
+        idb_stats *st = out->stats;
+        std::memset(st, 0, sizeof *st);
+        st->n_uniques = hc.n_uniques;
+        st->n_cores = hc.n_cores;
+        st->n_clusters = hc.n_clusters;
+        st->n_noise_rows = hc.n_noise_rows;
+        st->pairs_evaluated = hc.pairs_evaluated;
+        st->neighbour_pairs = hc.n_edges;
+        st->n_entries = hc.n_entries;
+        st->n_units = hc.n_units;
+        st->lev_columns = hc.lev_columns;
+        st->core_edges = hc.n_core_edges;
+        st->candidates = h.P.join ? 1u : 0u;
+        phase_times(hc, st);
+        st->ms_total = hc.stamp[5] > hc.stamp[0] ? 1e-6 * (double)(hc.stamp[5] - hc.stamp[0]) : 0.0;
+        st->kernel_launches = h.kernels;
+    }
+    return IDB_OK;
+}
+
 idb_status cluster_impl(idb_context *c, const idb_input *in, const idb_params *prm,
                         idb_output *out, bool host_io) {
     TRY(validate(in, prm, out));
@@ -706,6 +944,18 @@ idb_status cluster_impl(idb_context *c, const idb_input *in, const idb_params *p
         if (out->n_uniques) *out->n_uniques = 0;
         if (out->stats) std::memset(out->stats, 0, sizeof *out->stats);
         return IDB_OK;
+    }
+    // the plan cache serves host inputs without the tree-depth statistics
+    const bool cacheable = host_io && !pl.trees && (prm->schedule != 1 || c->has_model);
+    bool seen = false;
+    if (cacheable && c->hp.valid && host_plan_key_matches(c, in, prm, out)) {
+        seen = true;
+        if (c->hp.exec && c->hp.generation == c->generation && c->hp.epoch == c->stage_epoch &&
+            c->hp.model == c->has_model) {
+            const idb_status st = host_plan_run(c, in, out);
+            if (st != IDB_ERR_REPLAN && st != IDB_ERR_CAPACITY) return st;
+            host_plan_drop_graph(c);   // the data outgrew the plan: eager, then capture anew
+        }
     }
     TRY(stage_inputs_and_survey(pl, in, host_io));
     TRY(derive_plan(pl, prm));
@@ -753,6 +1003,16 @@ idb_status cluster_impl(idb_context *c, const idb_input *in, const idb_params *p
     }
     if (pl.trees) std::memcpy(out->tree_depth_hist, hist.data(), 4 * (kDepthMax + 1));
     TRY(fill_stats(pl, out->stats));
+    if (cacheable) {
+        // the second eager call of a shape captures it; a failed capture only
+        // means the next call runs eagerly too
+        if (seen && host_plan_capture(pl) != IDB_OK) {
+            cudaGetLastError();
+            host_plan_drop_graph(c);
+        }
+        host_plan_set_key(c, in, prm, out);
+        g_err.clear();
+    }
     return IDB_OK;
 }
 
@@ -860,6 +1120,7 @@ idb_status idb_context_destroy(idb_context *c) {
     cudaSetDevice(c->device);
     if (c->exec) cudaGraphExecDestroy(c->exec);
     if (c->graph) cudaGraphDestroy(c->graph);
+    host_plan_drop_graph(c);
     for (auto &b : c->buf)
         if (b.p) cudaFree(b.p);
     for (auto &e : c->ev)
@@ -955,11 +1216,16 @@ idb_status idb_batch_plan(idb_context *c, const idb_input *in, const idb_params 
     c->bufs = pl.B;
     c->out_dev = o;
     c->planned = true;
+    c->batch_generation = c->generation;
+    c->batch_epoch = c->stage_epoch;
     return IDB_OK;
 }
 
 idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
     if (!c || !c->planned) return fail(IDB_ERR_INVALID_ARG, "no batch plan");
+    if (c->batch_generation != c->generation || c->batch_epoch != c->stage_epoch)
+        return fail(IDB_ERR_REPLAN, "another call on this context replaced the staged inputs or "
+                                    "moved the workspace since idb_batch_plan: plan again");
     CU(cudaSetDevice(c->device));
     cudaStream_t s = c->stream;
     CU(cudaEventRecord(c->ev[0], s));

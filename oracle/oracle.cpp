@@ -105,6 +105,37 @@ extern "C" int32_t ora_levenshtein(const char *a, uint32_t la, const char *b, ui
     return prev[lb];
 }
 
+extern "C" int32_t ora_levenshtein_within(const char *a, uint32_t la, const char *b, uint32_t lb,
+                                          int32_t e) {
+    // Ukkonen's cutoff: a cell (i, j) with |i - j| > e holds more than e, so
+    // only the band |i - j| <= e is computed (cells outside read as e + 1), and
+    // once every cell of a row exceeds e the distance does.
+    if (e < 0) return 0;
+    if ((int64_t)la - (int64_t)lb > e || (int64_t)lb - (int64_t)la > e) return 0;
+    const int32_t big = e + 1;
+    thread_local std::vector<int32_t> prev, cur;
+    prev.assign(lb + 2, big);
+    cur.assign(lb + 2, big);
+    for (uint32_t j = 0; j <= lb && (int32_t)j <= e; ++j) prev[j] = (int32_t)j;
+    for (uint32_t i = 1; i <= la; ++i) {
+        const int64_t lo = std::max<int64_t>(1, (int64_t)i - e);
+        const int64_t hi = std::min<int64_t>(lb, (int64_t)i + e);
+        cur[lo - 1] = (lo == 1 && (int32_t)i <= e) ? (int32_t)i : big;
+        int32_t rowmin = cur[lo - 1];
+        for (int64_t j = lo; j <= hi; ++j) {
+            int32_t v = prev[j - 1] + (a[i - 1] != b[j - 1]);
+            v = std::min(v, prev[j] + 1);
+            v = std::min(v, cur[j - 1] + 1);
+            cur[j] = std::min(v, big);
+            rowmin = std::min(rowmin, cur[j]);
+        }
+        if (hi + 1 <= (int64_t)lb) cur[hi + 1] = big;
+        if (rowmin > e) return 0;
+        std::swap(prev, cur);
+    }
+    return prev[lb] <= e;
+}
+
 extern "C" int32_t ora_hamming(const char *a, const char *b, uint32_t len) {
     // Count of differing positions (cuda/PSDBSCAN.hcu:410-428).
     int32_t d = 0;
@@ -151,7 +182,17 @@ struct Rows {
             if (jb[(size_t)x * jw + k] != jb[(size_t)y * jw + k]) return false;
         return true;
     }
-    int32_t eps(uint32_t a, uint32_t b) const { return ora_eps(a, b, threshold, abs_eps); }
+    // eps per length pair, tabulated up to the longest sequence
+    uint32_t max_len = 0;
+    std::vector<int32_t> eps_tab;
+    void tabulate_eps() {
+        for (uint32_t i = 0; i < n; ++i) max_len = std::max(max_len, len(i));
+        eps_tab.resize((size_t)(max_len + 1) * (max_len + 1));
+        for (uint32_t a = 0; a <= max_len; ++a)
+            for (uint32_t b = 0; b <= max_len; ++b)
+                eps_tab[(size_t)a * (max_len + 1) + b] = ora_eps(a, b, threshold, abs_eps);
+    }
+    int32_t eps(uint32_t a, uint32_t b) const { return eps_tab[(size_t)a * (max_len + 1) + b]; }
 };
 
 // S4 -- neighbour predicate on two uniques (x != y).
@@ -160,7 +201,8 @@ struct Rows {
 //  Levenshtein DP <= eps.
 //  Hamming mode (cuda/PSDBSCAN.hcu:608-651): equal lengths, V and J overlap, and
 //  a Hamming count that stops once it exceeds eps.
-bool neighbours(const Rows &R, uint32_t x, uint32_t y, bool hamming_mode, bool &admissible) {
+bool neighbours(const Rows &R, uint32_t x, uint32_t y, bool hamming_mode, bool indexed,
+                bool &admissible) {
     uint32_t lx = R.len(x), ly = R.len(y);
     int32_t e = R.eps(lx, ly);
     admissible = false;
@@ -179,6 +221,7 @@ bool neighbours(const Rows &R, uint32_t x, uint32_t y, bool hamming_mode, bool &
     if (!R.overlap(x, y) || gap > e) return false;
     admissible = true;
     if (lx == ly && ora_hamming(R.s(x), R.s(y), lx) <= e) return true;
+    if (indexed) return ora_levenshtein_within(R.s(x), lx, R.s(y), ly, e) != 0;
     return ora_levenshtein(R.s(x), lx, R.s(y), ly) <= e;
 }
 
@@ -223,6 +266,10 @@ extern "C" int ora_cluster(uint32_t n_rows,
         StrCol jc{j_data, j_off, "V"}, jg{j_data ? jg_data : nullptr, jg_off, "V"};
         build_bitsets(n_rows, jc, jg, j_data ? n_jg : 1u, R.jb, R.jw);
     }
+    R.tabulate_eps();
+    const bool indexed = prm->indexed != 0;
+    int32_t max_gap = 0;   // the largest eps of any length pair bounds an admissible gap
+    for (int32_t v : R.eps_tab) max_gap = std::max(max_gap, v);
     std::vector<uint32_t> roff;
     if (rep_off && n_rep > 0) roff.assign(rep_off, rep_off + n_rep + 1);
     else roff = {0u, n_rows};
@@ -276,17 +323,27 @@ extern "C" int ora_cluster(uint32_t n_rows,
 #endif
         std::vector<std::vector<std::pair<uint32_t, uint32_t>>> local(nthr);
         uint64_t adm = 0;
+        // indexed mode: uniques in (length, row) order, and each one is paired
+        // with the later ones up to the largest admissible length gap (equal
+        // lengths only in Hamming mode); the full mode pairs every two uniques
+        std::vector<uint32_t> V(U);
+        if (indexed)
+            std::stable_sort(V.begin(), V.end(),
+                             [&](uint32_t p, uint32_t q) { return R.len(p) < R.len(q); });
+        const uint32_t gap = ham ? 0u : (uint32_t)max_gap;
 #pragma omp parallel for schedule(dynamic, 16) reduction(+ : adm)
         for (int64_t a = 0; a < nu; ++a) {
             int t = 0;
 #ifdef _OPENMP
             t = omp_get_thread_num();
 #endif
-            uint32_t x = U[a];
+            uint32_t x = V[a];
+            const uint32_t lx = R.len(x);
             for (int64_t b = a + 1; b < nu; ++b) {
-                uint32_t y = U[b];
+                uint32_t y = V[b];
+                if (indexed && R.len(y) > lx + gap) break;
                 bool is_adm;
-                if (neighbours(R, x, y, ham, is_adm)) {
+                if (neighbours(R, x, y, ham, indexed, is_adm)) {
                     local[t].emplace_back(x, y);
                     count[x].fetch_add(copies[y], std::memory_order_relaxed);
                     count[y].fetch_add(copies[x], std::memory_order_relaxed);

@@ -32,6 +32,11 @@ typedef struct ora_params {
     int32_t  use_hamming;    /* use_hamming                                       */
     int32_t  n_threads;      /* OpenMP threads (<=0: library default)             */
     int32_t  max_candidates; /* K: border candidate labels reported per row       */
+    int32_t  indexed;        /* 0: every pair of uniques, full DP (the reference's
+                                structure and cost, used as the CPU baseline);
+                                1: only pairs within the largest admissible length
+                                gap, edit distance with a cutoff at eps -- the same
+                                answer, for checking large inputs               */
 } ora_params;
 
 typedef struct ora_result {
@@ -78,6 +83,9 @@ int32_t ora_eps(uint32_t lx, uint32_t ly, float threshold, int32_t abs_eps);
    (cuda/PSDBSCAN.hcu:410-428) on raw bytes. */
 int32_t ora_levenshtein(const char *a, uint32_t la, const char *b, uint32_t lb);
 int32_t ora_hamming(const char *a, const char *b, uint32_t len);
+/* 1 iff the edit distance of a and b is at most e (banded DP, stops once a row
+   of the band exceeds e); the indexed mode's test. */
+int32_t ora_levenshtein_within(const char *a, uint32_t la, const char *b, uint32_t lb, int32_t e);
 
 #ifdef __cplusplus
 }

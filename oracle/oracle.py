@@ -24,7 +24,7 @@ _lib = None
 class _Params(C.Structure):
     _fields_ = [("threshold", C.c_float), ("abs_eps", C.c_int32), ("min_pts", C.c_uint32),
                 ("use_hamming", C.c_int32), ("n_threads", C.c_int32),
-                ("max_candidates", C.c_int32)]
+                ("max_candidates", C.c_int32), ("indexed", C.c_int32)]
 
 
 class _Result(C.Structure):
@@ -47,6 +47,9 @@ def lib():
         L.ora_levenshtein.argtypes = [C.c_char_p, C.c_uint32, C.c_char_p, C.c_uint32]
         L.ora_hamming.restype = C.c_int32
         L.ora_hamming.argtypes = [C.c_char_p, C.c_char_p, C.c_uint32]
+        L.ora_levenshtein_within.restype = C.c_int32
+        L.ora_levenshtein_within.argtypes = [C.c_char_p, C.c_uint32, C.c_char_p, C.c_uint32,
+                                             C.c_int32]
         L.ora_gene_bitsets.restype = C.c_int
         _lib = L
     return _lib
@@ -79,14 +82,17 @@ class OracleResult:
 
 
 def cluster(w, *, n_threads: int = 0, max_candidates: int = 8, no_v=False, no_j=False,
-            no_seq=False) -> OracleResult:
-    """Run the oracle on a synth.Workload (all repertoires)."""
+            no_seq=False, indexed: bool = False) -> OracleResult:
+    """Run the oracle on a synth.Workload (all repertoires).  ``indexed``
+    pairs only uniques within the largest admissible length gap and stops the
+    edit distance at eps: the same answer, for large inputs; the default keeps
+    the reference's all-pairs, full-DP structure."""
     L = lib()
     n = w.n
     vgb, vgo = _genes(w.v_genes)
     jgb, jgo = _genes(w.j_genes)
     prm = _Params(float(w.threshold), int(w.abs_eps), int(w.min_pts), int(bool(w.use_hamming)),
-                  int(n_threads), int(max_candidates))
+                  int(n_threads), int(max_candidates), int(bool(indexed)))
     K = max(int(max_candidates), 0)
     clone = np.zeros(n, np.uint32)
     core = np.zeros(n, np.int32)
@@ -118,6 +124,10 @@ def eps(lx: int, ly: int, threshold: float = float("nan"), abs_eps: int = -1) ->
 
 def levenshtein(a: bytes, b: bytes) -> int:
     return int(lib().ora_levenshtein(a, len(a), b, len(b)))
+
+
+def levenshtein_within(a: bytes, b: bytes, e: int) -> bool:
+    return bool(lib().ora_levenshtein_within(a, len(a), b, len(b), e))
 
 
 def hamming(a: bytes, b: bytes) -> int:

@@ -199,3 +199,39 @@ def test_oracle_matches_live_reference(seed):
     assert np.array_equal(r.copies, want.copies)
     assert np.array_equal(r.core, want.core)
     assert np.array_equal(r.clone_id, want.clone_id)
+
+
+def test_levenshtein_cutoff_matches_full_dp():
+    rng = np.random.default_rng(3)
+    for _ in range(4000):
+        a = bytes(rng.choice(list(b"ACGT"), size=int(rng.integers(0, 14))).astype(np.uint8))
+        b = bytearray(a)
+        for _ in range(int(rng.integers(0, 5))):
+            op = rng.integers(0, 3)
+            if op == 0 and b:
+                b[int(rng.integers(0, len(b)))] = int(rng.choice(list(b"ACGT")))
+            elif op == 1 and b:
+                del b[int(rng.integers(0, len(b)))]
+            else:
+                b.insert(int(rng.integers(0, len(b) + 1)), int(rng.choice(list(b"ACGT"))))
+        b = bytes(b)
+        d = oracle.levenshtein(a, b)
+        for e in range(-1, 6):
+            assert oracle.levenshtein_within(a, b, e) == (d <= e), (a, b, e, d)
+
+
+@pytest.mark.parametrize("k,scale,threshold", [(1, 0.01, None), (3, 0.005, None),
+                                               (4, 0.001, None), (0, 0.3, 0.15), (2, 0.01, 0.1)])
+def test_indexed_mode_matches_all_pairs(k, scale, threshold):
+    """The oracle's indexed mode (length-windowed pairs, cutoff DP) gives the
+    all-pairs answer, so it can check inputs too large for the full mode."""
+    from immunodbscan_gb300 import synth
+    w = synth.workload(k, scale=scale)
+    if threshold is not None:
+        w.abs_eps, w.threshold = -1, threshold
+    a = oracle.cluster(w)
+    b = oracle.cluster(w, indexed=True)
+    assert np.array_equal(a.clone_id, b.clone_id)
+    assert np.array_equal(a.core, b.core)
+    assert np.array_equal(a.copies, b.copies)
+    assert (a.admissible_pairs, a.neighbour_pairs) == (b.admissible_pairs, b.neighbour_pairs)
