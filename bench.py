@@ -18,9 +18,14 @@ second of device time; sequences/s alongside.
           H2D of the columns, the whole path, D2H of clone_id/core/copies.
   plain   the same workload as 64 per-repertoire idb_cluster_device calls.
 
+  parity  every row of the batched result against the oracle (indexed mode:
+          the all-pairs answer); a mismatch ends the run with exit status 3.
+
 `--impl reference` times the CPU restatement of the reference path (the
-all-pairs oracle, OpenMP on all host cores) on a bounded sample of the same
-workload; the reference's CUDA code has no CPU backend.
+all-pairs oracle, OpenMP on all host cores) on a fixed sample of the same
+workload (the smallest repertoires up to a row-pair budget), the rows the GPU
+arm's cpu_baseline also clusters on the GPU; the reference's CUDA code has no
+CPU backend.
 """
 from __future__ import annotations
 
@@ -66,9 +71,11 @@ def parse():
     ap.add_argument("--candidates", default="auto", choices=["auto", "buckets"],
                     help="candidate pairs: automatic (the segment join for Hamming eps <= 2) or "
                          "every admissible pair of the buckets")
-    ap.add_argument("--cpu-seconds", type=float, default=None,
-                    help="CPU time budget of the oracle sample (per step for --impl reference; "
-                         "default 10 s, or 150 s / steps for the reference arm)")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="skip the table of the other workloads (0, 1, 3 at 2M rows, 4 at 10M "
+                         "rows: batched and plain device time, identical partitions)")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the check of every row against the oracle's indexed mode")
     return ap.parse_args()
 
 
@@ -151,41 +158,76 @@ def allreduce_max(world, x: float) -> float:
     return float(t.item())
 
 
-def _pick(sizes, order, rate, seconds):
-    pick, budget = [], 0.0
-    for r in order:
-        cost = sizes[r] ** 2 / rate
-        if pick and budget + cost > seconds:
-            break
-        pick.append(int(r))
-        budget += cost
-    return sorted(pick)
+# The CPU sample: the oracle in its all-pairs, full-DP mode (the reference's
+# structure) visits n(n-1)/2 row pairs per repertoire, so the sample is the
+# smallest repertoires up to a budget of row pairs -- the same rows in both
+# arms.  A single repertoire above the budget is cut to its first rows.
+CPU_SAMPLE_ROW_PAIRS = {True: 5e10, False: 5e8}   # Hamming / Levenshtein
 
 
-def run_cpu(w, seconds: float, threads: int):
-    """Oracle on the smallest repertoires that fill about `seconds` of CPU time.
-
-    The oracle visits every pair of uniques of a repertoire, so its cost grows
-    with the sum of squared repertoire sizes; the rate is calibrated on the
-    smallest repertoire and refined once on the first full sample."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle
+def cpu_sample(w):
+    """(repertoire ids, rows kept of the last one or None) of the CPU sample."""
+    budget = CPU_SAMPLE_ROW_PAIRS[bool(w.use_hamming)]
     sizes = np.diff(w.rep_off).astype(np.float64)
     order = np.argsort(sizes, kind="stable")
-    t0 = time.perf_counter()
-    oracle.cluster(w.subset_repertoires([int(order[0])]), n_threads=threads, max_candidates=0)
-    rate = sizes[order[0]] ** 2 / max(time.perf_counter() - t0, 1e-3)
-    for attempt in range(3):
-        pick = _pick(sizes, order, rate, seconds)
-        sub = w.subset_repertoires(pick)
-        t0 = time.perf_counter()
-        r = oracle.cluster(sub, n_threads=threads, max_candidates=0)
-        dt = time.perf_counter() - t0
-        if dt >= 0.5 * seconds or len(pick) == len(order):
+    pick, acc = [], 0.0
+    for r in order:
+        c = sizes[r] * (sizes[r] - 1) / 2
+        if pick and acc + c > budget:
             break
-        rate = float(np.sum(sizes[pick] ** 2)) / max(dt, 1e-3)
+        pick.append(int(r))
+        acc += c
+    cut = None
+    if len(pick) == 1 and acc > budget:
+        cut = int(math.sqrt(2 * budget))
+    return sorted(pick), cut
+
+
+def sample_workload(w, pick, cut):
+    from immunodbscan_gb300 import synth
+    if cut is None:
+        return w.subset_repertoires(pick)
+    lo = int(w.rep_off[pick[0]])
+    return synth.take_rows(w, np.arange(lo, lo + cut))
+
+
+def run_cpu(w, threads: int):
+    """The oracle (all-pairs, full DP) on the CPU sample; returns its rate and
+    its answer."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    pick, cut = cpu_sample(w)
+    sub = sample_workload(w, pick, cut)
+    t0 = time.perf_counter()
+    r = oracle.cluster(sub, n_threads=threads, max_candidates=0)
+    dt = time.perf_counter() - t0
     return dict(value=r.admissible_pairs / dt / 1e9, seq_per_s=sub.n / dt, seconds=dt,
-                rows=sub.n, reps=len(pick), pairs=r.admissible_pairs)
+                rows=sub.n, reps=len(pick), pairs=r.admissible_pairs, pick=pick, cut=cut,
+                result=r, sub=sub)
+
+
+def sample_text(res):
+    what = (f"first {res['cut']} rows of the workload" if res["cut"] is not None else
+            f"{res['reps']} smallest repertoires of the workload")
+    return f"{what} ({res['rows']} rows, {res['pairs']} admissible pairs)"
+
+
+def full_parity(w, clone, core, copies, threads: int):
+    """Every row of the timed workload against the oracle's indexed mode (pairs
+    within the largest admissible length gap, edit distance cut off at eps:
+    the all-pairs answer, tested in tests/test_oracle.py)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    t0 = time.perf_counter()
+    o = oracle.cluster(w, n_threads=threads, max_candidates=0, indexed=True)
+    dt = time.perf_counter() - t0
+    bad = ((clone != o.clone_id) | (core != o.core) | (copies != o.copies))
+    return {"rows": int(w.n), "repertoires": int(w.n_rep),
+            "identical": bool(not bad.any()), "differing_rows": int(bad.sum()),
+            "oracle": "oracle/oracle.cpp indexed mode (the all-pairs answer), "
+                      f"{threads} host threads, {dt:.1f} s",
+            "compared": "clone_id, core, copies of every row (batched path)",
+            "n_clusters": int(o.n_clusters), "neighbour_pairs": int(o.neighbour_pairs)}
 
 
 def profiled_traffic(kernel: str, workload: str):
@@ -229,17 +271,14 @@ def reference_arm(args, world, rank, w):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    if args.warmup > 0:
-        run_cpu(w, 0.5, threads)
     vals, secs = [], []
-    per_step = args.cpu_seconds or min(10.0, 150.0 / max(args.steps, 1))
-    for _ in range(args.steps):
-        res = run_cpu(w, per_step, threads)
-        vals.append(res["value"])
-        secs.append(res["seconds"])
+    for k in range(args.warmup + args.steps):
+        res = run_cpu(w, threads)
+        if k >= args.warmup:
+            vals.append(res["value"])
+            secs.append(res["seconds"])
     value = float(np.median(vals))
-    sample = (f"{res['reps']} smallest repertoires of the workload ({res['rows']} rows, "
-              f"{res['pairs']} admissible pairs) per step")
+    sample = sample_text(res) + " per step, the same rows as the GPU arm's cpu_baseline"
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)),
@@ -469,24 +508,35 @@ def main():
         clone = torch.empty(n, dtype=torch.int32).pin_memory()
         core = torch.empty(n, dtype=torch.int32).pin_memory()
         copies = torch.empty(n, dtype=torch.int32).pin_memory()
+        est = _lib.Stats()
         o = _lib.Output(clone.data_ptr(), core.data_ptr(), copies.data_ptr(), None, None, None,
-                        None)
-        for _ in range(max(1, args.warmup)):
+                        C.cast(C.pointer(est), C.c_void_p))
+        # the first call runs eagerly, the second also captures the shape, the
+        # rest replay it (idb_cluster's plan cache)
+        for _ in range(max(3, args.warmup)):
             _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
         barrier(world)
-        times = []
+        times, dev_ms = [], []
         for _ in range(args.steps):
             t0 = time.perf_counter()
             _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
             times.append(time.perf_counter() - t0)
+            dev_ms.append(est.ms_total)
         barrier(world)
         e2e_s = allreduce_max(world, float(np.mean(times)))
         h2d = sum(int(a.numel() * a.element_size()) for a in hkeep if isinstance(a, torch.Tensor))
+        # breakdown: the same host->device copies alone, the device time of the
+        # path (the call's own time stamps), the result copies alone
+        up_ms, down_ms = copy_times(hkeep, (clone, core, copies))
         out["e2e"] = {"value": world * admissible / e2e_s / 1e9, "unit": UNIT,
                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * n,
                       "ms_per_step": e2e_s * 1e3, "seq_per_s": world * n / e2e_s,
                       "api": "idb_cluster (host buffers, %s schedule)" % ("learned" if learn else
-                                                                           "static")}
+                                                                           "static"),
+                      "replayed": bool(est.kernel_launches > 0),
+                      "breakdown_ms": {"upload": up_ms, "device": float(np.mean(dev_ms)),
+                                       "download": down_ms,
+                                       "other": e2e_s * 1e3 - up_ms - float(np.mean(dev_ms)) - down_ms}}
         same = (np.array_equal(clone.numpy().view(np.uint32), clone_b) and
                 np.array_equal(core.numpy(), core_b))
         out["e2e"]["identical_partitions_vs_batched"] = bool(same)
@@ -525,17 +575,101 @@ def main():
                                                               args.warmup, world, local,
                                                               args.mlp_epochs)
 
+    if rank == 0 and not args.no_workloads and args.workload == 2 and args.scale == 1.0:
+        out["workloads"] = workload_table(local)
+
+    parity_ok = True
     if rank == 0 and not args.no_cpu:
-        res = run_cpu(w, args.cpu_seconds or 10.0, os.cpu_count() or 1)
-        out["cpu_baseline"] = {"value": res["value"], "unit": UNIT, "cores": os.cpu_count(),
-                               "kind": "port",
-                               "sample": f"{res['reps']} smallest repertoires ({res['rows']} rows, "
-                                         f"{res['pairs']} admissible pairs), "
-                                         f"{res['seconds']:.1f} s"}
+        threads = os.cpu_count() or 1
+        res = run_cpu(w, threads)
+        # the GPU on the same rows, for a like-for-like rate
+        sub = res["sub"]
+        gb = DeviceBatch(sub, ctx_setup, schedule=0, tune=shape)
+        gb.plan()
+        rs = time_batch(gb, 5, 2, 1)
+        cs_, ks_, ps_ = gb.results()
+        o = res["result"]
+        same = (np.array_equal(cs_, o.clone_id) and np.array_equal(ks_, o.core) and
+                np.array_equal(ps_, o.copies))
+        out["cpu_baseline"] = {"value": res["value"], "unit": UNIT, "cores": threads,
+                               "kind": "port", "sample": sample_text(res) + f", {res['seconds']:.1f} s",
+                               "gpu_same_sample": {"value": res["pairs"] / (rs["step_ms"] * 1e-3) / 1e9,
+                                                   "ms_per_step": rs["step_ms"],
+                                                   "identical_to_oracle": bool(same)}}
+        parity_ok &= same
+    if rank == 0 and not args.no_parity:
+        out["parity"] = full_parity(w, clone_b, core_b, copies_b, os.cpu_count() or 1)
+        parity_ok &= out["parity"]["identical"]
     if rank == 0:
         print(json.dumps(out), flush=True)
+        if not parity_ok:
+            sys.stderr.write("PARITY FAILURE: the GPU result differs from the oracle\n")
+            sys.exit(3)
     for c in (ctx_setup, ctx_static, ctx_learned):
         c.close()
+
+
+def workload_table(local, steps: int = 3, warmup: int = 2):
+    """The other workloads at their full sizes: batched device time (a captured
+    plan, static schedule, default tile) against one eager call of the plain
+    path, with the partitions compared."""
+    import torch
+    from immunodbscan_gb300 import Context, DeviceBatch, _lib
+    from immunodbscan_gb300.interlink import make_params
+    L = _lib.lib()
+    rows = []
+    for k in (0, 1, 3, 4):
+        t0 = time.time()
+        w = synth_workload(k)
+        gen = time.time() - t0
+        ctx_b, ctx_p = Context(local), Context(local)
+        try:
+            inp, keep = build_host_input(w, pinned=False)
+            prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming)
+            adm = C.c_uint64()
+            _lib.check(L.idb_count_admissible(ctx_p.handle, C.byref(inp), C.byref(prm), C.byref(adm)))
+            b = DeviceBatch(w, ctx_b)
+            b.plan()
+            r = time_batch(b, steps, warmup, 1)
+            clone_b, core_b, copies_b = b.results()
+            st = r["last"]
+            del b
+            p = DeviceBatch(w, ctx_p)
+            p.cluster_once()                       # warm
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            p.cluster_once()
+            torch.cuda.synchronize()
+            plain_ms = 1e3 * (time.perf_counter() - t1)
+            clone_p, core_p, copies_p = p.results()
+            del p
+            same = (np.array_equal(clone_b, clone_p) and np.array_equal(core_b, core_p) and
+                    np.array_equal(copies_b, copies_p))
+            ms = r["step_ms"]
+            rows.append({"workload": workload_name(w), "rows": int(w.n),
+                         "admissible_pairs": int(adm.value), "ms_per_step": ms,
+                         "seq_per_s": w.n / (ms * 1e-3),
+                         "gpair_per_s": int(adm.value) / (ms * 1e-3) / 1e9,
+                         "distance_ms": r["ms_dist"],
+                         "phase_ms": {n: float(np.mean([ph[i] for ph in r["phases"]])) for i, n in
+                                      enumerate(["front_dedupe", "buckets_schedule", "distance",
+                                                 "graph", "outputs"])},
+                         "plain_ms": plain_ms,
+                         "plain_api": "idb_cluster_device (eager)",
+                         "identical_partitions_plain_vs_batched": bool(same),
+                         "candidates": "segment join" if st.candidates == 1 else "buckets",
+                         "streamed": bool(st.streamed),
+                         "neighbour_pairs": int(st.neighbour_pairs),
+                         "n_clusters": int(st.n_clusters), "generate_s": gen})
+        finally:
+            ctx_b.close()
+            ctx_p.close()
+    return rows
+
+
+def synth_workload(k):
+    from immunodbscan_gb300 import synth
+    return synth.workload(k)
 
 
 def learned_vs_static(k, scale, steps, warmup, world, local, epochs):
@@ -569,6 +703,32 @@ def learned_vs_static(k, scale, steps, warmup, world, local, epochs):
     finally:
         ctx_s.close()
         ctx_l.close()
+
+
+def copy_times(host_inputs, host_outputs, reps: int = 5):
+    """Time (ms) of the host->device copies of the input columns and of the
+    device->host copies of the outputs alone (pinned memory, CUDA events)."""
+    import torch
+    ins = [t for t in host_inputs if isinstance(t, torch.Tensor)]
+    dev_in = [torch.empty_like(t, device="cuda") for t in ins]
+    dev_out = [torch.empty_like(t, device="cuda") for t in host_outputs]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(pairs):
+        best = float("inf")
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0.record()
+            for dst, src in pairs:
+                dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+    up = timed(list(zip(dev_in, ins)))
+    down = timed(list(zip(host_outputs, dev_out)))
+    del dev_in, dev_out
+    return up, down
 
 
 def ops_per_pair(w, batch) -> int:

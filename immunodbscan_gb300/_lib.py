@@ -31,7 +31,7 @@ class Params(C.Structure):
     _fields_ = [("threshold", C.c_float), ("abs_eps", C.c_int32), ("min_pts", C.c_uint32),
                 ("use_hamming", C.c_int32), ("eval_trees", C.c_int32), ("schedule", C.c_int32),
                 ("tile_rx", C.c_int32), ("tile_ty", C.c_int32), ("candidates", C.c_int32),
-                ("reserved", C.c_int32 * 3)]
+                ("edge_memory_mb", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class Tuning(C.Structure):
@@ -56,7 +56,7 @@ class Stats(C.Structure):
                 ("neighbour_pairs", C.c_uint64), ("n_entries", C.c_uint64), ("n_units", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_distance", C.c_double), ("ms_phase", C.c_double * 8),
                 ("kernel_launches", C.c_uint32), ("core_edges", C.c_uint32),
-                ("lev_columns", C.c_uint64), ("candidates", C.c_uint32), ("reserved", C.c_uint32)]
+                ("lev_columns", C.c_uint64), ("candidates", C.c_uint32), ("streamed", C.c_uint32)]
 
 
 class Output(C.Structure):
@@ -89,6 +89,8 @@ SIGNATURES = {
     "idb_mlp_load": (C.c_int, [C.c_void_p, C.c_void_p]),
     "idb_diag_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
                                     C.c_void_p, C.POINTER(C.c_float)]),
+    "idb_diag_mlp_predict": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32,
+                                       C.c_void_p]),
     "idb_diag_int_peak": (C.c_int, [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "idb_diag_gene_bits": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                      C.c_void_p, C.c_uint32, C.c_void_p]),

@@ -402,6 +402,8 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
     P.hamming = prm->use_hamming != 0;
     P.min_pts = prm->min_pts;
     P.schedule = prm->schedule;
+    P.streamed = prm->edge_memory_mb < 0;
+    P.edge_budget = prm->edge_memory_mb > 0 ? (uint64_t)prm->edge_memory_mb << 20 : 0;
     P.Lmin = P.N ? h.lmin : 0;
     P.Lmax = P.N ? h.lmax : 0;
     if (P.Lmin > P.Lmax) P.Lmin = P.Lmax;
@@ -673,26 +675,49 @@ idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false
     TRY(check_launch());
     record(pl, 2);
     if (stop_after_schedule) return IDB_OK;
-    if (eager && P.cap_edges == 0) TRY(alloc_edges(pl, std::max<uint64_t>(4ull * P.N, 1ull << 16)));
-    for (int attempt = 0; attempt < 3; ++attempt) {
+    // The neighbour pairs go to an edge list for the graph phase, unless they
+    // would take more than the edge memory allowed (or than the device has):
+    // then the streamed mode keeps no list and runs the distance work twice.
+    const uint64_t kEdgeBytes = sizeof(uint2) + 2 * sizeof(uint32_t);   // list + CSR per edge
+    if (eager && !P.streamed && P.cap_edges == 0) {
+        uint64_t first = std::max<uint64_t>(4ull * P.N, 1ull << 16);
+        if (P.edge_budget) first = std::max<uint64_t>(std::min(first, P.edge_budget / kEdgeBytes), 4096);
+        TRY(alloc_edges(pl, first));
+    }
+    for (int attempt = 0; !P.streamed && attempt < 3; ++attempt) {
         launch_distance(P, B, 0, s);
         TRY(check_launch());
         if (!eager) break;
         TRY(read_counters(pl));
         const Counters &h = *c->h_ctr;
         if (!(h.error & kErrEdgeOverflow)) break;
-        // grow to the exact requirement and sweep again
-        TRY(alloc_edges(pl, (uint64_t)h.edge_reserved + 64ull * kEdgeChunk * 1024));
+        // grow to the exact requirement and sweep again, or stream
+        const uint64_t need = (uint64_t)h.edge_reserved + 64ull * kEdgeChunk * 1024;
+        if ((P.edge_budget && need * kEdgeBytes > P.edge_budget) || need > 0xFFFFFFF0ull) {
+            P.streamed = true;
+        } else {
+            const idb_status st = alloc_edges(pl, need);
+            if (st == IDB_ERR_OUT_OF_MEMORY) P.streamed = true;
+            else if (st != IDB_OK) return st;
+        }
         const uint32_t clear_err = h.error & ~kErrEdgeOverflow;
         CU(cudaMemsetAsync(&B.ctr->unit_cursor, 0, 4, s));
         CU(cudaMemsetAsync(&B.ctr->edge_reserved, 0, 4, s));
         CU(cudaMemsetAsync(&B.ctr->n_edges, 0, 4, s));
         CU(cudaMemsetAsync(&B.ctr->pairs_evaluated, 0, 8, s));
+        CU(cudaMemsetAsync(&B.ctr->lev_columns, 0, 8, s));
         CU(cudaMemcpyAsync(&B.ctr->error, &clear_err, 4, cudaMemcpyHostToDevice, s));
         CU(cudaStreamSynchronize(s));
     }
-    record(pl, 3);
-    launch_graph(P, B, pl.trees, s);
+    if (P.streamed) {
+        launch_streamed_sweeps(P, B, s);
+        TRY(check_launch());
+        record(pl, 3);
+        launch_streamed_labels(P, B, pl.trees, s);
+    } else {
+        record(pl, 3);
+        launch_graph(P, B, pl.trees, s);
+    }
     record(pl, 4);
     launch_outputs(P, B, s);
     TRY(check_launch());
@@ -715,6 +740,7 @@ idb_status fill_stats(Pipeline &pl, idb_stats *st) {
     st->lev_columns = h.lev_columns;
     st->core_edges = h.n_core_edges;
     st->candidates = pl.P.join ? 1u : 0u;
+    st->streamed = pl.P.streamed ? 1u : 0u;
     if (pl.timing) {
         phase_times(h, st);
         st->ms_total = h.stamp[5] > h.stamp[0] ? 1e-6 * (double)(h.stamp[5] - h.stamp[0]) : 0.0;
@@ -741,7 +767,8 @@ bool same_params(const idb_params &a, const idb_params &b) {
     std::memcpy(&tb, &b.threshold, 4);
     return ta == tb && a.abs_eps == b.abs_eps && a.min_pts == b.min_pts &&
            a.use_hamming == b.use_hamming && a.schedule == b.schedule && a.tile_rx == b.tile_rx &&
-           a.tile_ty == b.tile_ty && a.candidates == b.candidates;
+           a.tile_ty == b.tile_ty && a.candidates == b.candidates &&
+           a.edge_memory_mb == b.edge_memory_mb;
 }
 
 void gene_key(const char *names, const int64_t *off, uint32_t G, std::vector<char> &b,
@@ -830,7 +857,8 @@ idb_status host_plan_capture(Pipeline &pl) {
     const Counters hc = *c->h_ctr;
     TRY(alloc_entries(pl, (uint64_t)hc.n_entries + hc.n_entries / 16 + 1024));
     TRY(alloc_binpairs(pl, (uint64_t)hc.n_binpairs + hc.n_binpairs / 16 + 1024));
-    TRY(alloc_edges(pl, (uint64_t)hc.edge_reserved + hc.edge_reserved / 8 + 64ull * kEdgeChunk * 1024));
+    if (!pl.P.streamed)
+        TRY(alloc_edges(pl, (uint64_t)hc.edge_reserved + hc.edge_reserved / 8 + 64ull * kEdgeChunk * 1024));
     cudaStream_t s = c->stream;
     CU(cudaStreamSynchronize(s));
     pl.timing = true;
@@ -924,6 +952,7 @@ idb_status host_plan_run(idb_context *c, const idb_input *in, idb_output *out) {
         st->lev_columns = hc.lev_columns;
         st->core_edges = hc.n_core_edges;
         st->candidates = h.P.join ? 1u : 0u;
+        st->streamed = h.P.streamed ? 1u : 0u;
         phase_times(hc, st);
         st->ms_total = hc.stamp[5] > hc.stamp[0] ? 1e-6 * (double)(hc.stamp[5] - hc.stamp[0]) : 0.0;
         st->kernel_launches = h.kernels;
@@ -1179,7 +1208,8 @@ idb_status idb_batch_plan(idb_context *c, const idb_input *in, const idb_params 
     const Counters h = *c->h_ctr;
     TRY(alloc_entries(pl, (uint64_t)h.n_entries + h.n_entries / 16 + 1024));
     TRY(alloc_binpairs(pl, (uint64_t)h.n_binpairs + h.n_binpairs / 16 + 1024));
-    TRY(alloc_edges(pl, (uint64_t)h.edge_reserved + h.edge_reserved / 8 + 64ull * kEdgeChunk * 1024));
+    if (!pl.P.streamed)
+        TRY(alloc_edges(pl, (uint64_t)h.edge_reserved + h.edge_reserved / 8 + 64ull * kEdgeChunk * 1024));
     // 3. capture the complete launch sequence
     cudaStream_t s = c->stream;
     CU(cudaStreamSynchronize(s));
@@ -1248,6 +1278,7 @@ idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
         stats->lev_columns = h.lev_columns;
         stats->core_edges = h.n_core_edges;
         stats->candidates = c->plan.join ? 1u : 0u;
+        stats->streamed = c->plan.streamed ? 1u : 0u;
         float ms = 0;
         CU(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
         stats->ms_total = ms;
@@ -1472,6 +1503,32 @@ idb_status idb_diag_mlp_grad(idb_context *c, const float *params, const float *f
     cudaFree(X); cudaFree(T); cudaFree(p); cudaFree(g); cudaFree(loss);
     if (e != cudaSuccess) return fail(IDB_ERR_CUDA, "idb_diag_mlp_grad: %s", cudaGetErrorString(e));
     if (loss_out) *loss_out = hl / (float)n;
+    return IDB_OK;
+}
+
+idb_status idb_diag_mlp_predict(idb_context *c, const float *params, const float *features,
+                                uint32_t n, float *log2_cycles_out) {
+    TRY(get_ctx(&c));
+    if (!params || !features || !log2_cycles_out || n == 0)
+        return fail(IDB_ERR_INVALID_ARG, "idb_diag_mlp_predict: bad arguments");
+    CU(cudaSetDevice(c->device));
+    cudaStream_t s = c->stream;
+    float *X = nullptr, *p = nullptr, *y = nullptr;
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&X, sizeof(float) * kMlpIn * n);
+    if (e == cudaSuccess) e = cudaMalloc(&p, sizeof(float) * kMlpParams);
+    if (e == cudaSuccess) e = cudaMalloc(&y, sizeof(float) * n);
+    if (e == cudaSuccess) e = cudaMalloc(&q, 2 * kMlpParams);
+    if (e == cudaSuccess) {
+        cudaMemcpyAsync(X, features, sizeof(float) * kMlpIn * n, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, s);
+        launch_to_bf16(p, q, s);              // the conversion idb_mlp_load applies
+        launch_mlp_forward_rows(X, n, q, y, s);
+        cudaMemcpyAsync(log2_cycles_out, y, sizeof(float) * n, cudaMemcpyDeviceToHost, s);
+        e = cudaStreamSynchronize(s);
+    }
+    cudaFree(X); cudaFree(p); cudaFree(y); cudaFree(q);
+    if (e != cudaSuccess) return fail(IDB_ERR_CUDA, "idb_diag_mlp_predict: %s", cudaGetErrorString(e));
     return IDB_OK;
 }
 

@@ -36,6 +36,13 @@ constexpr int kMlpHidden = 64;          // two hidden layers of 64
 constexpr int kMlpParams = kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +
                            kMlpHidden + 1;
 
+// where the distance kernel sends neighbour pairs
+enum : uint32_t {
+    kSinkEdges = 0u,   // the edge list (the graph phase reads it)
+    kSinkCount = 1u,   // streamed mode, first sweep: copies-weighted counts
+    kSinkGrow = 2u,    // streamed mode, second sweep: unions and border minima
+};
+
 // error bits raised by kernels (Counters::error)
 enum : uint32_t {
     kErrHashStall = 1u,       // duplicate-table probe exceeded its bound
@@ -197,6 +204,9 @@ struct Plan {
     bool sig_exact = true;                        // V genes <= 64 and J genes <= 32
     bool join = false;                            // Hamming by segment join (eps <= kJoinMaxEps)
     uint32_t join_smax = 1;                       // most segments of any length
+    bool streamed = false;                        // neighbour pairs not stored: the
+                                                  // distance work runs twice
+    uint64_t edge_budget = 0;                     // bytes for the edge list (0: no limit)
     uint8_t codemap[256];
     int first_byte = -1;                          // byte value with code 0
     // capacities
@@ -289,9 +299,14 @@ void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_schedule(const Plan &P, const Buffers &B, cudaStream_t s);
-void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s);
+void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s,
+                     uint32_t sink = kSinkEdges);
 void launch_count_admissible(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s);
+// streamed mode: both distance sweeps (counts, core flags, unions and border
+// minima), then depths, compression and labels
+void launch_streamed_sweeps(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_streamed_labels(const Plan &P, const Buffers &B, bool trees, cudaStream_t s);
 void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s);
 
 // exclusive scan of n (host) or *n_dev (device, capacity n) uint32 values;
@@ -306,6 +321,8 @@ void launch_mlp_grad(const float *X, const float *T, uint32_t n, const float *p,
                      float *grad, float *loss, cudaStream_t s);
 void launch_adam(float *p, const float *grad, float *m, float *v, float lr, int step, cudaStream_t s);
 void launch_to_bf16(const float *p, void *q, cudaStream_t s);
+void launch_mlp_forward_rows(const float *X, uint32_t n, const void *wq_bf16, float *y,
+                             cudaStream_t s);
 
 int sm_count();
 const char *distance_variant_name(const Plan &P);

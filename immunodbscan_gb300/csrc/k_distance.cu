@@ -64,7 +64,67 @@ struct DistArgs {
     // segment join: a hit is a neighbour pair if the V and J sets intersect and
     // no lower segment is identical (that segment's group emits it)
     int join;
+    // where neighbour pairs go: kSinkEdges = the edge list; kSinkCount /
+    // kSinkGrow = the two sweeps of the streamed mode (no edge list kept)
+    uint32_t sink;
+    uint32_t *cnt;                   // copies-weighted neighbour counts (count sweep)
+    const uint32_t *ucopies;
+    const uint32_t *ucore;           // core flags (grow sweep)
+    uint32_t *parent;                // union-find forest (grow sweep)
+    uint32_t *bmin;                  // minimum core neighbour of a non-core unique
 };
+
+// Streamed mode, for neighbour graphs larger than the edge memory allowed: the
+// distance work runs twice and no pair is stored.  The count sweep adds each
+// side's copies to the other's count (rule S5); after the core flags, the grow
+// sweep merges core-core pairs into the union-find forest (link to the smaller
+// root, as the reference's union_a_and_b does, cuda/PSDBSCAN.hcu:76-107) and
+// keeps for every non-core unique its minimum core neighbour (atomicMin: the
+// same border rule as the edge-list path).  Both are order-independent.
+__device__ __forceinline__ uint32_t sweep_find(uint32_t *p, uint32_t x) {
+    volatile uint32_t *vp = p;
+    while (true) {   // parent[y] <= y: x strictly decreases
+        const uint32_t px = vp[x];
+        if (px == x) return x;
+        const uint32_t ppx = vp[px];
+        if (ppx == px) return px;
+        vp[x] = ppx;   // path halving
+        x = ppx;
+    }
+}
+
+__device__ __noinline__ void sink_streamed(const DistArgs &a, uint32_t lo, uint32_t hi) {
+    if (a.sink == kSinkCount) {
+        atomicAdd(&a.cnt[lo], __ldg(&a.ucopies[hi]));
+        atomicAdd(&a.cnt[hi], __ldg(&a.ucopies[lo]));
+        return;
+    }
+    const uint32_t clo = a.ucore[lo], chi = a.ucore[hi];
+    if (clo != chi) {
+        atomicMin(&a.bmin[clo ? hi : lo], clo ? lo : hi);
+        return;
+    }
+    if (!clo) return;
+    uint32_t x = lo, y = hi, it = 0;
+    for (; it < kSpinCap; ++it) {
+        uint32_t rx = sweep_find(a.parent, x), ry = sweep_find(a.parent, y);
+        if (rx == ry) break;
+        if (rx < ry) { const uint32_t t = rx; rx = ry; ry = t; }
+        if (atomicCAS(&a.parent[rx], rx, ry) == rx) break;   // hook the larger root
+        x = rx;
+        y = ry;
+    }
+    if (it == kSpinCap) atomicOr(&a.ctr->error, kErrUnionStall);
+}
+
+// One neighbour pair (lo < hi, unique ids) at edge slot `slot`.
+__device__ __forceinline__ void put_edge(const DistArgs &a, uint64_t slot, uint32_t lo, uint32_t hi) {
+    if (a.sink == kSinkEdges) {
+        if (slot < a.cap_edges) a.edges[slot] = make_uint2(lo, hi);
+    } else {
+        sink_streamed(a, lo, hi);
+    }
+}
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -83,7 +143,7 @@ struct EdgeWriter {
     __device__ void init() { base = kNoChunk; fill = 0; written = 0; }
 
     __device__ void pad(const DistArgs &a, int lane) {
-        if (base == kNoChunk) return;
+        if (base == kNoChunk || a.sink != kSinkEdges) return;
         for (uint32_t t = fill + lane; t < kEdgeChunk; t += 32) {
             const uint64_t slot = base + t;
             if (slot < a.cap_edges) a.edges[slot] = make_uint2(kNone, kNone);
@@ -105,10 +165,7 @@ struct EdgeWriter {
             if ((uint64_t)b + kEdgeChunk > a.cap_edges && lane == 0)
                 atomicOr(&a.ctr->error, kErrEdgeOverflow);
         }
-        if (ok) {
-            const uint64_t slot = base + fill + __popc(m & lanemask_lt());
-            if (slot < a.cap_edges) a.edges[slot] = make_uint2(lo, hi);
-        }
+        if (ok) put_edge(a, base + fill + __popc(m & lanemask_lt()), lo, hi);
         fill += n;
         written += n;
     }
@@ -335,8 +392,7 @@ __device__ __forceinline__ void emit_pair_bits(const DistArgs &a, EdgeWriter &ew
         uint32_t i, j;
         small_pair(p, same, n, i, j);
         const uint32_t ux = __ldg(&a.meta[xstart + i].w), uy = __ldg(&a.meta[ystart + j].w);
-        const uint64_t slot = ew.slot_of(bk, k++);
-        if (slot < a.cap_edges) a.edges[slot] = make_uint2(min(ux, uy), max(ux, uy));
+        put_edge(a, ew.slot_of(bk, k++), min(ux, uy), max(ux, uy));
     }
 }
 
@@ -344,7 +400,7 @@ __device__ __forceinline__ void emit_pair_bits(const DistArgs &a, EdgeWriter &ew
 // holds entry l of each side; each round the lanes take 32 pairs and fetch
 // the two records by shuffles.  Canonicity of a hit is decided from the side
 // records (global loads: hits are rare).
-template <int BP, int W, int EM>
+template <int BP, int W, int EM, bool JN>
 __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew, const BinPair &P,
                                               uint32_t idx, int lane, uint64_t &pairs) {
     constexpr int NW = BP * W;
@@ -405,7 +461,7 @@ __device__ __forceinline__ void hamming_small(const DistArgs &a, EdgeWriter &ew,
         if (act && sc <= thr) {
             const uint4 mx = __ldg(a.meta + P.a_start + i), my = __ldg(a.meta + ystart + j);
             bool ok;
-            if (a.join) {
+            if (JN) {
                 ok = join_meta_ok<W>(mx, my, dw, P.la, P.j, P.v);
             } else if (a.sig_exact) {
                 ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
@@ -445,7 +501,7 @@ __device__ __forceinline__ void prefetch_l1(const void *p) {
     asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
 }
 
-template <int BP, int W, int EM>
+template <int BP, int W, int EM, bool JN>
 __device__ __forceinline__ void hamming_small_all(const DistArgs &a, EdgeWriter &ew, int lane,
                                                   uint64_t &pairs) {
     constexpr int R16 = (BP * W + 3) / 4;
@@ -474,7 +530,7 @@ __device__ __forceinline__ void hamming_small_all(const DistArgs &a, EdgeWriter 
                 if (!ns && (uint32_t)lane < nm) prefetch_l1(a.rec + (size_t)(nb + lane) * R16);
             }
             const BinPair P = shfl_binpair(myP, (int)g);
-            hamming_small<BP, W, EM>(a, ew, P, __shfl_sync(0xFFFFFFFFu, myidx, g), lane, pairs);
+            hamming_small<BP, W, EM, JN>(a, ew, P, __shfl_sync(0xFFFFFFFFu, myidx, g), lane, pairs);
         }
     }
 }
@@ -483,7 +539,7 @@ __device__ __forceinline__ void hamming_small_all(const DistArgs &a, EdgeWriter 
 // every pair of the l-th bin pair of a batch of 32, so the latency of loading
 // a bin pair and its records is paid once per 32 bin pairs.  Records are read
 // per pair from L1 (a tiny bin's records share one or two cache lines).
-template <int BP, int W, int EM>
+template <int BP, int W, int EM, bool JN>
 __device__ __forceinline__ void hamming_tiny_all(const DistArgs &a, EdgeWriter &ew, int lane,
                                                  uint64_t &pairs) {
     constexpr int NW = BP * W;
@@ -535,7 +591,7 @@ __device__ __forceinline__ void hamming_tiny_all(const DistArgs &a, EdgeWriter &
             if (sc > thr) continue;
             const uint4 mx = __ldg(a.meta + P.a_start + i), my = __ldg(a.meta + P.a_start + j);
             bool ok;
-            if (a.join) {
+            if (JN) {
                 ok = join_meta_ok<W>(mx, my, dw, P.la, P.j, P.v);
             } else if (a.sig_exact) {
                 ok = ((mx.x & my.x) | (mx.y & my.y) | (mx.z & my.z)) == 0;
@@ -570,6 +626,7 @@ constexpr uint32_t kOff = 0x40000000u;   // score of a masked x-entry (never a h
 // compacted over the whole warp before they are written: each lane first keeps
 // the bits of its own queue that are edges (pair order and canonical bin),
 // then one warp scan gives every lane its place in one bulk append.
+template <bool JN>
 __device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, uint32_t *q,
                                         uint32_t qn, const uint4 *xm, const uint4 *ym,
                                         uint32_t xbase, uint32_t ypos0, uint32_t same,
@@ -584,7 +641,7 @@ __device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, ui
             const uint32_t r = (uint32_t)__ffs(b) - 1u;
             const uint32_t xpos = xbase + 32u * r + (uint32_t)lane;
             bool ok = !(same && ypos <= xpos);
-            if (ok && !a.join) {
+            if (ok && !JN) {
                 const uint4 m = xm[32 * r + lane];
                 if (a.sig_exact) {
                     ok = ((m.x & my.x) | (m.y & my.y) | (m.z & my.z)) == 0;
@@ -615,8 +672,7 @@ __device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, ui
         for (uint32_t b = e & 0xFFu; b; b &= b - 1) {
             const uint32_t r = (uint32_t)__ffs(b) - 1u;
             const uint32_t ux = xm[32 * r + lane].w;
-            const uint64_t slot = ew.slot_of(bk, i++);
-            if (slot < a.cap_edges) a.edges[slot] = make_uint2(min(ux, uy), max(ux, uy));
+            put_edge(a, ew.slot_of(bk, i++), min(ux, uy), max(ux, uy));
         }
     }
 }
@@ -624,7 +680,7 @@ __device__ __forceinline__ void drain_hits(const DistArgs &a, EdgeWriter &ew, ui
 // The y loop of one Hamming unit.  FULL: every r-block of the lane's x-entries
 // is inside the unit, so all RX chains run without branches; otherwise the
 // chains of r-blocks past the unit's end are skipped.
-template <int BP, int W, int RX, int EM, bool FULL>
+template <int BP, int W, int RX, int EM, bool FULL, bool JN>
 __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew, const Unit &U,
                                                const uint32_t (&x)[RX][BP * W],
                                                const uint32_t (&vmask)[RX], uint32_t valid,
@@ -697,7 +753,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
             for (int r = 0; r < RX; ++r)
                 if (sc[r] <= thr) {
                     bool ok = true;
-                    if (a.join) {
+                    if (JN) {
                         // segment join: V and J sets intersect, the group's
                         // segment is identical and no lower one is (masks of
                         // segment kk, word w at sseg[4 kk + w])
@@ -731,7 +787,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
         auto drain_if_full = [&](uint32_t room) {
             if (__any_sync(0xFFFFFFFFu, qn + room > (uint32_t)kHitQ)) {
                 __syncwarp();
-                drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same, U.P.v, U.P.j, lane);
+                drain_hits<JN>(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same, U.P.v, U.P.j, lane);
                 qn = 0;
                 __syncwarp();
             }
@@ -771,7 +827,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
         }
         if (__any_sync(0xFFFFFFFFu, qn)) {
             __syncwarp();
-            drain_hits(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same, U.P.v, U.P.j, lane);
+            drain_hits<JN>(a, ew, shq, qn, sxm, sym, U.xbase, U.ybase + yb, same, U.P.v, U.P.j, lane);
         }
         __syncwarp();
     }
@@ -781,7 +837,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
 // Hamming, fast path.  BP planes x W words per record; RX x-entries per lane.
 // EM: 0 = popcount test, 1 = eps == 1 (d & (d-1)) == 0, 2 = eps == 0.
 // ---------------------------------------------------------------------------
-template <int BP, int W, int RX, int EM>
+template <int BP, int W, int RX, int EM, bool JN>
 __global__ void __launch_bounds__(kWarps * 32, (W == 1 && RX <= 4 ? 5 : 4))
 k_hamming(DistArgs a) {
     constexpr int NW = BP * W;                 // words per record used
@@ -820,7 +876,7 @@ k_hamming(DistArgs a) {
             if (ok) pairs += unit_pairs(U, U.xbase + xi);
             sxm[wid][xi] = __ldg(a.meta + U.P.a_start + U.xbase + (ok ? xi : 0));
         }
-        if (a.join && lane < 16) {
+        if (JN && lane < 16) {
             // segment kk = lane / 4 of length la split into j segments, word w = lane % 4
             const uint32_t kk = (uint32_t)lane >> 2, w = (uint32_t)lane & 3u;
             const uint32_t L = U.P.la, S = U.P.j;
@@ -835,16 +891,16 @@ k_hamming(DistArgs a) {
         }
         __syncwarp();
         if (U.nx == (uint32_t)(32 * RX))
-            hamming_unit_y<BP, W, RX, EM, true>(a, ew, U, x, vmask, valid, sy[wid], sym[wid], sxm[wid],
+            hamming_unit_y<BP, W, RX, EM, true, JN>(a, ew, U, x, vmask, valid, sy[wid], sym[wid], sxm[wid],
                                                 shq[wid], sseg[wid], lane);
         else
-            hamming_unit_y<BP, W, RX, EM, false>(a, ew, U, x, vmask, valid, sy[wid], sym[wid],
+            hamming_unit_y<BP, W, RX, EM, false, JN>(a, ew, U, x, vmask, valid, sy[wid], sym[wid],
                                                  sxm[wid], shq[wid], sseg[wid], lane);
         log_unit(a, U, lane);
     }
     // then the small bin pairs (they also fill the tail of the tiled work)
-    hamming_small_all<BP, W, EM>(a, ew, lane, pairs);
-    hamming_tiny_all<BP, W, EM>(a, ew, lane, pairs);
+    hamming_small_all<BP, W, EM, JN>(a, ew, lane, pairs);
+    hamming_tiny_all<BP, W, EM, JN>(a, ew, lane, pairs);
     finish(a, ew, pairs, lane);
 }
 
@@ -1175,11 +1231,20 @@ void run(K kernel, const DistArgs &a, size_t smem, int grid, cudaStream_t s) {
     kernel<<<grid, kWarps * 32, smem, s>>>(a);
 }
 
+// The segment join and the buckets are separate instantiations, so the
+// bucket path's hot loop carries none of the join's per-hit tests (and the
+// instruction cache holds one of them, not both).
+template <int BP, int W, int RX, bool JN>
+void run_hamming_jn(const Plan &P, const DistArgs &a, int grid, cudaStream_t s) {
+    if (P.hamming_eps_mode == 2) run(k_hamming<BP, W, RX, 2, JN>, a, 0, grid, s);
+    else if (P.hamming_eps_mode == 1 && W == 1) run(k_hamming<BP, W, RX, 1, JN>, a, 0, grid, s);
+    else run(k_hamming<BP, W, RX, 0, JN>, a, 0, grid, s);
+}
+
 template <int BP, int W, int RX>
 void run_hamming(const Plan &P, const DistArgs &a, int grid, cudaStream_t s) {
-    if (P.hamming_eps_mode == 2) run(k_hamming<BP, W, RX, 2>, a, 0, grid, s);
-    else if (P.hamming_eps_mode == 1 && W == 1) run(k_hamming<BP, W, RX, 1>, a, 0, grid, s);
-    else run(k_hamming<BP, W, RX, 0>, a, 0, grid, s);
+    if (P.join) run_hamming_jn<BP, W, RX, true>(P, a, grid, s);
+    else run_hamming_jn<BP, W, RX, false>(P, a, grid, s);
 }
 
 }  // namespace
@@ -1206,6 +1271,12 @@ static DistArgs make_args(const Plan &P, const Buffers &B) {
     a.small_list = B.bp_small;
     a.small_cap = (uint32_t)P.cap_binpairs + 1u;
     a.join = P.join ? 1 : 0;
+    a.sink = kSinkEdges;
+    a.cnt = B.cnt;
+    a.ucopies = B.ucopies;
+    a.ucore = B.ucore;
+    a.parent = B.parent;
+    a.bmin = B.bmin;
     return a;
 }
 
@@ -1222,8 +1293,13 @@ const char *distance_variant_name(const Plan &P) {
     return P.hamming ? "k_hamming" : "k_levenshtein";
 }
 
-void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s) {
+void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s, uint32_t sink) {
     DistArgs a = make_args(P, B);
+    a.sink = sink;
+    if (sink != kSinkEdges) {   // no list: nothing to overflow
+        a.edges = nullptr;
+        a.cap_edges = ~0ull;
+    }
     cudaMemsetAsync(&B.ctr->unit_cursor, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(&B.ctr->small_cursor, 0, sizeof(uint32_t), s);
     cudaMemsetAsync(&B.ctr->tiny_cursor, 0, sizeof(uint32_t), s);

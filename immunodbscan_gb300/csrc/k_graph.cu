@@ -286,6 +286,35 @@ void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s) {
                                       B.uid_first, B.cnt);
 }
 
+// Streamed mode: counts from a first distance sweep, core flags, then a second
+// sweep that merges core-core pairs and keeps every non-core unique's minimum
+// core neighbour; depths, compression and labels as above.  The sweep-local
+// statistics are cleared between the sweeps so that they count one sweep.
+void launch_streamed_sweeps(const Plan &P, const Buffers &B, cudaStream_t s) {
+    k_graph_init<<<grid_wave(k_graph_init, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ucopies, B.cnt, B.parent, B.bmin);
+    launch_distance(P, B, 0, s, kSinkCount);
+    k_core<<<grid_wave(k_core, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ctr, B.cnt, P.min_pts, B.ucore);
+    cudaMemsetAsync(&B.ctr->pairs_evaluated, 0, sizeof(B.ctr->pairs_evaluated), s);
+    cudaMemsetAsync(&B.ctr->n_edges, 0, sizeof(B.ctr->n_edges), s);
+    cudaMemsetAsync(&B.ctr->edge_reserved, 0, sizeof(B.ctr->edge_reserved), s);
+    cudaMemsetAsync(&B.ctr->lev_columns, 0, sizeof(B.ctr->lev_columns), s);
+    launch_distance(P, B, 0, s, kSinkGrow);
+}
+
+void launch_streamed_labels(const Plan &P, const Buffers &B, bool trees, cudaStream_t s) {
+    if (trees) {
+        cudaMemsetAsync(B.depth_hist, 0, sizeof(uint32_t) * (kDepthMax + 1), s);
+        k_depth<<<grid_for(P.N), kThreads, 0, s>>>(P.N, B.row2uid, B.urow, B.ucore, B.bmin, B.parent,
+                                                   B.depth_hist);
+    }
+    cudaMemsetAsync(B.rootflag, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
+    k_compress<<<grid_wave(k_compress, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ucore, B.parent, B.rootflag);
+    scan_u32(B.rootflag, B.rootflag, P.N + 1, nullptr, &B.ctr->n_clusters, B.scan_part,
+             B.scan_part_cap, s);
+    k_labels<<<grid_wave(k_labels, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ucore, B.parent, B.bmin, B.rootflag, B.urep,
+                                      B.uid_first, B.cnt);
+}
+
 void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s) {
     const int gu = grid_for(P.N);
     k_rows_out<<<grid_wave(k_rows_out, P.N, kThreads), kThreads, 0, s>>>(P.N, P.min_pts, B.row2uid, B.urow, B.ucopies, B.ucore,

@@ -91,6 +91,35 @@ __global__ void k_mlp_select(Counters *ctr, const BinPair *__restrict__ bp,
     }
 }
 
+// BF16 forward pass of one sample (weights in shared memory): inputs and
+// hidden activations rounded to BF16, products accumulated in FP32.  Returns
+// the predicted log2 cycles.
+__device__ __forceinline__ float mlp_forward_bf16(const __nv_bfloat16 *w, const float (&f)[kIn]) {
+    __nv_bfloat16 x[kIn];
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) x[k] = __float2bfloat16(f[k]);
+    // fully unrolled so the activations stay in registers
+    float h1[kH];
+#pragma unroll
+    for (int j = 0; j < kH; ++j) {
+        float acc = __bfloat162float(w[kOffB1 + j]);
+#pragma unroll
+        for (int k = 0; k < kIn; ++k)
+            acc = fmaf(__bfloat162float(x[k]), __bfloat162float(w[kOffW1 + k * kH + j]), acc);
+        h1[j] = __bfloat162float(__float2bfloat16(fmaxf(acc, 0.0f)));
+    }
+    float y = __bfloat162float(w[kOffB3]);
+    for (int j = 0; j < kH; ++j) {
+        float acc = __bfloat162float(w[kOffB2 + j]);
+#pragma unroll
+        for (int k = 0; k < kH; ++k)
+            acc = fmaf(h1[k], __bfloat162float(w[kOffW2 + k * kH + j]), acc);
+        const float h2 = __bfloat162float(__float2bfloat16(fmaxf(acc, 0.0f)));
+        y = fmaf(h2, __bfloat162float(w[kOffW3 + j]), y);
+    }
+    return y;
+}
+
 // BF16 inference over the listed bin pairs: pred[i] = 2^mlp(features)
 __global__ void __launch_bounds__(kThreads)
 k_mlp_predict_bf16(const Counters *__restrict__ ctr, const BinPair *__restrict__ bp,
@@ -103,32 +132,26 @@ k_mlp_predict_bf16(const Counters *__restrict__ ctr, const BinPair *__restrict__
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += stride) {
         const uint32_t i = heavy[k0];
-        const BinPair P = bp[i];
         float f[kIn];
-        binpair_features(P, f);
-        __nv_bfloat16 x[kIn];
+        binpair_features(bp[i], f);
+        pred[i] = exp2f(fminf(mlp_forward_bf16(w, f), 60.0f));
+    }
+}
+
+// The same forward pass on given feature rows (log2 cycles out), for checking
+// the inference against a CPU forward pass.
+__global__ void __launch_bounds__(kThreads)
+k_mlp_forward_rows(const float *__restrict__ X, uint32_t n, const __nv_bfloat16 *__restrict__ wq,
+                   float *__restrict__ y) {
+    __shared__ __nv_bfloat16 w[kMlpParams];
+    for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) w[k] = wq[k];
+    __syncthreads();
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        float f[kIn];
 #pragma unroll
-        for (int k = 0; k < kIn; ++k) x[k] = __float2bfloat16(f[k]);
-        // fully unrolled so the activations stay in registers
-        float h1[kH];
-#pragma unroll
-        for (int j = 0; j < kH; ++j) {
-            float acc = __bfloat162float(w[kOffB1 + j]);
-#pragma unroll
-            for (int k = 0; k < kIn; ++k)
-                acc = fmaf(__bfloat162float(x[k]), __bfloat162float(w[kOffW1 + k * kH + j]), acc);
-            h1[j] = __bfloat162float(__float2bfloat16(fmaxf(acc, 0.0f)));
-        }
-        float y = __bfloat162float(w[kOffB3]);
-        for (int j = 0; j < kH; ++j) {
-            float acc = __bfloat162float(w[kOffB2 + j]);
-#pragma unroll
-            for (int k = 0; k < kH; ++k)
-                acc = fmaf(h1[k], __bfloat162float(w[kOffW2 + k * kH + j]), acc);
-            const float h2 = __bfloat162float(__float2bfloat16(fmaxf(acc, 0.0f)));
-            y = fmaf(h2, __bfloat162float(w[kOffW3 + j]), y);
-        }
-        pred[i] = exp2f(fminf(y, 60.0f));
+        for (int k = 0; k < kIn; ++k) f[k] = X[(size_t)i * kIn + k];
+        y[i] = mlp_forward_bf16(w, f);
     }
 }
 
@@ -298,6 +321,13 @@ void launch_adam(float *p, const float *grad, float *m, float *v, float lr, int 
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
     k_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(p, grad, m, v, lr, b1, b2, 1e-8f, c1, c2);
+}
+
+void launch_mlp_forward_rows(const float *X, uint32_t n, const void *wq_bf16, float *y,
+                             cudaStream_t s) {
+    const int grid = (int)std::min<uint64_t>((n + kThreads - 1) / kThreads, (uint64_t)sm_count() * 2);
+    k_mlp_forward_rows<<<grid > 0 ? grid : 1, kThreads, 0, s>>>(
+        X, n, static_cast<const __nv_bfloat16 *>(wq_bf16), y);
 }
 
 void launch_to_bf16(const float *p, void *q, cudaStream_t s) {

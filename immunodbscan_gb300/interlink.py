@@ -73,7 +73,8 @@ class Context:
 
 
 def make_params(threshold=float("nan"), abs_eps=-1, min_pts=2, use_hamming=False,
-                eval_trees=False, schedule=0, tune=None, candidates=0) -> Params:
+                eval_trees=False, schedule=0, tune=None, candidates=0,
+                edge_memory_mb=0) -> Params:
     p = Params()
     p.threshold = float(threshold) if threshold is not None else math.nan
     p.abs_eps = int(abs_eps)
@@ -85,6 +86,7 @@ def make_params(threshold=float("nan"), abs_eps=-1, min_pts=2, use_hamming=False
         p.tile_rx = int(tune[0])
         p.tile_ty = int(tune[1])
     p.candidates = int(candidates)
+    p.edge_memory_mb = int(edge_memory_mb)
     return p
 
 
@@ -116,7 +118,7 @@ class Interlink:
                  j_genes_reference, threshold: float, min_pts: int, use_only_hamming: bool,
                  eval_trees: bool = False, *, abs_eps: int = -1, rep_sizes=None,
                  context: Optional[Context] = None, schedule: int = 0, tune=None,
-                 candidates: int = 0):
+                 candidates: int = 0, edge_memory_mb: int = 0):
         n = int(n_entries)
         keep = []
         inp = Input()
@@ -151,7 +153,7 @@ class Interlink:
             inp.n_repertoires = len(rep_sizes)
             inp.rep_offsets = _p(roff)
         prm = make_params(threshold, abs_eps, min_pts, use_only_hamming, eval_trees, schedule, tune,
-                          candidates)
+                          candidates, edge_memory_mb)
         self._result = _run(inp, prm, n, context, eval_trees)
 
     # getters of cuda/Interlink.hpp:59-63
@@ -198,7 +200,7 @@ def cluster_workload(w, context: Optional[Context] = None, *, schedule: int = 0,
                    w.threshold, w.min_pts, w.use_hamming, eval_trees, abs_eps=w.abs_eps,
                    rep_sizes=np.diff(w.rep_off).tolist() if w.n_rep > 1 else None,
                    context=context, schedule=schedule, tune=tune,
-                   candidates=w.candidates)
+                   candidates=w.candidates, edge_memory_mb=w.edge_memory_mb)
     return it.result
 
 
@@ -240,7 +242,7 @@ class DeviceBatch:
         inp.rep_offsets = _p(roff)
         self.inp = inp
         self.prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, schedule, tune,
-                               w.candidates)
+                               w.candidates, w.edge_memory_mb)
         self.out = Output(_p(self.clone), _p(self.core), _p(self.copies), None, None, None, None)
 
     def cluster_once(self) -> Stats:

@@ -117,6 +117,34 @@ def device_grad(params: np.ndarray, X: np.ndarray, T: np.ndarray, ctx: Optional[
     return g, float(loss.value)
 
 
+def device_forward(params: np.ndarray, X: np.ndarray, ctx: Optional[Context] = None) -> np.ndarray:
+    """The scheduler's BF16 inference (log2 cycles) on feature rows X."""
+    X = np.ascontiguousarray(X, np.float32)
+    p = np.ascontiguousarray(params, np.float32)
+    y = np.zeros(len(X), np.float32)
+    _lib.check(_lib.lib().idb_diag_mlp_predict(ctx.handle if ctx else None, p.ctypes.data,
+                                               X.ctypes.data, len(X), y.ctypes.data))
+    return y
+
+
+def _bf16(a: np.ndarray) -> np.ndarray:
+    """Round float32 values to BF16 (nearest, ties to even), kept as float32."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+def forward_bf16(p: np.ndarray, X: np.ndarray) -> np.ndarray:
+    """CPU model of the BF16 inference: parameters, inputs and hidden
+    activations rounded to BF16 as the device rounds them, float64 sums."""
+    w1, b1, w2, b2, w3, b3 = [np.asarray(_bf16(np.asarray(t, np.float32)), np.float64)
+                              for t in unpack(p)]
+    x = np.asarray(_bf16(np.asarray(X, np.float32)), np.float64)
+    h1 = np.asarray(_bf16(np.maximum(x @ w1 + b1, 0).astype(np.float32)), np.float64)
+    h2 = np.asarray(_bf16(np.maximum(h1 @ w2 + b2, 0).astype(np.float32)), np.float64)
+    return h2 @ w3 + b3
+
+
 def cpu_grad(params: np.ndarray, X: np.ndarray, T: np.ndarray):
     """Reference gradient of the mean squared error (float64, NumPy)."""
     w1, b1, w2, b2, w3, b3 = unpack(params)

@@ -53,6 +53,7 @@ class Workload:
     alphabet: bytes = AA
     seed: int = 0
     candidates: int = 0           # 0 = automatic candidate pairs, 1 = buckets only
+    edge_memory_mb: int = 0       # neighbour-pair list memory (0 no limit, < 0 streamed)
 
     @property
     def n(self) -> int:

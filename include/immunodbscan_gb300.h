@@ -62,7 +62,14 @@ typedef struct idb_params {
     int32_t  tile_ty;          /* y-entries of a work unit (0 = default)           */
     int32_t  candidates;       /* 0 = automatic (Hamming eps <= 2: segment join),
                                   1 = every admissible pair of the buckets        */
-    int32_t  reserved[3];
+    int32_t  edge_memory_mb;   /* device memory for the neighbour-pair list:
+                                  0 = as much as the pairs need; > 0 = at most this
+                                  many MiB; < 0 = none.  Neighbour graphs that do
+                                  not fit are clustered in streamed mode: the
+                                  distance work runs twice (counts, then unions
+                                  and border minima) and no pair is stored.  Same
+                                  answer either way.                              */
+    int32_t  reserved[2];
 } idb_params;
 
 /* Input rows (cuda/Interlink.hpp:54-57: zip(V calls, J calls, sequences)). */
@@ -111,7 +118,8 @@ typedef struct idb_stats {
     uint32_t candidates;       /* 0: every admissible pair of the buckets scored;
                                   1: Hamming segment join (eps <= 2 at every
                                   length): only pairs sharing a whole segment    */
-    uint32_t reserved;
+    uint32_t streamed;         /* 1: neighbour pairs were not stored (two sweeps;
+                                  core_edges is not counted)                      */
 } idb_stats;
 
 /* Outputs (cuda/Interlink.hpp:59-67).  clone_id/core/copies are required. */

@@ -47,6 +47,14 @@ idb_status idb_diag_gene_bits(idb_context *ctx, const char *calls, const int64_t
 idb_status idb_diag_mlp_grad(idb_context *ctx, const float *params, const float *features,
                              const float *targets, uint32_t n, float *grad_out, float *loss_out);
 
+/* The learned scheduler's inference on given feature rows: the parameters are
+   converted to BF16 as idb_mlp_load converts them, and the forward pass the
+   scheduler runs on bin pairs (BF16 inputs, weights and activations, FP32
+   accumulation) writes log2_cycles_out[i] for features[i * IDB_MLP_FEATURES ..];
+   for checking against a CPU forward pass. */
+idb_status idb_diag_mlp_predict(idb_context *ctx, const float *params, const float *features,
+                                uint32_t n, float *log2_cycles_out);
+
 #ifdef __cplusplus
 }
 #endif

@@ -73,3 +73,21 @@ def test_autotune_shapes_agree(gpu_ctx, tmp_path, k, scale):
         assert np.array_equal(got.clone_id, ref.clone_id)
     rx, ty, _ = tuning.shape_for(w, gpu_ctx, cache_path=str(tmp_path / "tune.json"))
     assert (rx, ty) == (rec["rx"], rec["ty"]) or rx > 0
+
+
+def test_bf16_inference_matches_cpu_forward(gpu_ctx):
+    """The scheduler's BF16 inference against two CPU forward passes on trained
+    weights and profiled bin-pair features: a model of the same BF16 rounding
+    (inputs, weights, hidden activations; only the summation order differs,
+    FP32 on the device) within 1e-3 of the output range, and the exact float64
+    network within the BF16 error budget (2% of the output range)."""
+    w = synth.workload(2, scale=0.01)
+    X, T = learned.profile(w, gpu_ctx)
+    p, _ = learned.train(X, T, gpu_ctx, epochs=100)
+    y_dev = learned.device_forward(p, X, gpu_ctx)
+    y_bf16 = learned.forward_bf16(p, X)
+    y_f64 = learned.forward(p, X)
+    span = float(np.ptp(y_f64)) or 1.0
+    assert np.max(np.abs(y_dev - y_bf16)) <= 1e-3 * span + 1e-3
+    assert np.max(np.abs(y_dev - y_f64)) <= 2e-2 * span
+    assert np.corrcoef(y_dev, y_f64)[0, 1] > 0.999
