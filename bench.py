@@ -537,9 +537,10 @@ def main():
                       "breakdown_ms": {"upload": up_ms, "device": float(np.mean(dev_ms)),
                                        "download": down_ms,
                                        "other": e2e_s * 1e3 - up_ms - float(np.mean(dev_ms)) - down_ms}}
-        same = (np.array_equal(clone.numpy().view(np.uint32), clone_b) and
-                np.array_equal(core.numpy(), core_b))
-        out["e2e"]["identical_partitions_vs_batched"] = bool(same)
+        diff = ((clone.numpy().view(np.uint32) != clone_b) | (core.numpy() != core_b) |
+                (copies.numpy().view(np.uint32) != copies_b))
+        out["e2e"]["identical_partitions_vs_batched"] = bool(not diff.any())
+        out["e2e"]["differing_rows"] = int(diff.sum())
 
     # plain per-repertoire path: one eager call per repertoire, default shape, static order
     if not args.no_plain:
@@ -712,6 +713,7 @@ def copy_times(host_inputs, host_outputs, reps: int = 5):
     ins = [t for t in host_inputs if isinstance(t, torch.Tensor)]
     dev_in = [torch.empty_like(t, device="cuda") for t in ins]
     dev_out = [torch.empty_like(t, device="cuda") for t in host_outputs]
+    host_out = [torch.empty_like(t).pin_memory() for t in host_outputs]   # leave the results
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
     def timed(pairs):
@@ -726,8 +728,8 @@ def copy_times(host_inputs, host_outputs, reps: int = 5):
             best = min(best, e0.elapsed_time(e1))
         return best
     up = timed(list(zip(dev_in, ins)))
-    down = timed(list(zip(host_outputs, dev_out)))
-    del dev_in, dev_out
+    down = timed(list(zip(host_out, dev_out)))
+    del dev_in, dev_out, host_out
     return up, down
 
 

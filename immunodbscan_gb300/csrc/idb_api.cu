@@ -68,7 +68,7 @@ enum BufId {
     bSeq, bSeqOff, bV, bVOff, bJ, bJOff, bVGenes, bVGOff, bJGenes, bJGOff, bRepOff, bEps, bCode,
     bVBits, bJBits, bSlot, bRepRow, bFlag, bUidOfRow, bRow2Uid, bTable, bTCount,
     bURow, bUCopies, bULen, bURep, bBinHist, bBinCursor, bEntUid, bEntRec, bBpCount, bBp,
-    bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bDeg, bGOff, bGCur, bAdj, bCnt, bUCore,
+    bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bCnt, bUCore,
     bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
     bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bBpSmall,
     bJnTab, bJnISlot, bJnStart, bJnCur, bJnBpIdx, bNumBufs
@@ -523,9 +523,6 @@ idb_status alloc_fixed(Pipeline &pl) {
     TRY(ensure(c, bUClass, 4 * N1));
     TRY(ensure(c, bBpCount, 4 * (P.nbins + 1)));
     TRY(ensure(c, bClsHist, 4 * 130));
-    TRY(ensure(c, bDeg, 4 * N1));
-    TRY(ensure(c, bGOff, 4 * N1));
-    TRY(ensure(c, bGCur, 4 * N1));
     TRY(ensure(c, bCnt, 4 * N1));
     TRY(ensure(c, bUCore, 4 * N1));
     TRY(ensure(c, bParent, 4 * N1));
@@ -566,7 +563,6 @@ idb_status alloc_fixed(Pipeline &pl) {
     B.bin_hist = ptr<uint32_t>(c, bBinHist); B.bin_cursor = ptr<uint32_t>(c, bBinCursor);
     B.sig_and = ptr<unsigned long long>(c, bSigAnd); B.uclass = ptr<uint32_t>(c, bUClass);
     B.bp_count = ptr<uint32_t>(c, bBpCount); B.cls_hist = ptr<uint32_t>(c, bClsHist);
-    B.deg = ptr<uint32_t>(c, bDeg); B.goff = ptr<uint32_t>(c, bGOff); B.gcur = ptr<uint32_t>(c, bGCur);
     B.cnt = ptr<uint32_t>(c, bCnt); B.ucore = ptr<uint32_t>(c, bUCore);
     B.parent = ptr<uint32_t>(c, bParent); B.bmin = ptr<uint32_t>(c, bBMin);
     B.rootflag = ptr<uint32_t>(c, bRootFlag); B.uid_first = ptr<uint32_t>(c, bUidFirst);
@@ -615,9 +611,7 @@ idb_status alloc_edges(Pipeline &pl, uint64_t cap) {
     if (cap > 0xFFFFFFF0ull) return fail(IDB_ERR_UNSUPPORTED, "more than 2^32 neighbour pairs");
     pl.P.cap_edges = cap;
     TRY(ensure(c, bEdges, sizeof(uint2) * cap, true));
-    TRY(ensure(c, bAdj, 2 * sizeof(uint32_t) * cap, true));
     pl.B.edges = ptr<uint2>(c, bEdges);
-    pl.B.adj = ptr<uint32_t>(c, bAdj);
     return IDB_OK;
 }
 
@@ -678,7 +672,7 @@ idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false
     // The neighbour pairs go to an edge list for the graph phase, unless they
     // would take more than the edge memory allowed (or than the device has):
     // then the streamed mode keeps no list and runs the distance work twice.
-    const uint64_t kEdgeBytes = sizeof(uint2) + 2 * sizeof(uint32_t);   // list + CSR per edge
+    const uint64_t kEdgeBytes = sizeof(uint2);   // one list entry per neighbour pair
     if (eager && !P.streamed && P.cap_edges == 0) {
         uint64_t first = std::max<uint64_t>(4ull * P.N, 1ull << 16);
         if (P.edge_budget) first = std::max<uint64_t>(std::min(first, P.edge_budget / kEdgeBytes), 4096);
@@ -1109,6 +1103,24 @@ const char *idb_status_string(idb_status s) {
         case IDB_ERR_REPLAN: return "inputs no longer match the plan";
     }
     return "unknown status";
+}
+
+idb_status idb_host_alloc(size_t bytes, void **out) {
+    if (!out) return fail(IDB_ERR_INVALID_ARG, "NULL output pointer");
+    *out = nullptr;
+    const cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return fail(IDB_ERR_OUT_OF_MEMORY, "page-locked allocation of %zu bytes failed: %s", bytes,
+                    cudaGetErrorString(e));
+    }
+    return IDB_OK;
+}
+
+idb_status idb_host_free(void *p) {
+    if (p) CU(cudaFreeHost(p));
+    return IDB_OK;
 }
 
 size_t idb_last_error(char *buf, size_t size) {

@@ -264,10 +264,6 @@ struct Buffers {
     float *pred = nullptr;                          // learned cost per bin pair
     // graph
     uint2 *edges = nullptr;                         // [cap_edges]
-    uint32_t *deg = nullptr;                        // [N+1] degrees
-    uint32_t *goff = nullptr;                       // [N+1] CSR offsets
-    uint32_t *gcur = nullptr;                       // [N+1] fill cursors
-    uint32_t *adj = nullptr;                        // [2*cap_edges]
     uint32_t *cnt = nullptr;                        // [N] neighbour copies count
     uint32_t *ucore = nullptr;                      // [N]
     uint32_t *parent = nullptr;                     // [N]

@@ -16,12 +16,11 @@
 // Counts are accumulated per edge; core-core edges are merged by unions that
 // hook the larger root under the smaller one with atomicCAS while find()
 // halves paths, so every component's root is its minimum core index, as in the
-// reference.  The core-to-non-core edges form a CSR graph (count in the union
-// pass / scan / fill) whose row of a non-core unique lists its core
-// neighbours; the unique joins the cluster of the minimum one (deterministic;
-// one of the outcomes the reference's race allows).  Labels are 1 + the rank
-// of the root among the repertoire's core roots, found with one exclusive
-// scan over root flags.
+// reference.  In the same pass every core-to-non-core edge offers its core end
+// to the non-core end with atomicMin, so a non-core unique joins the cluster
+// of its minimum-index core neighbour (deterministic; one of the outcomes the
+// reference's race allows).  Labels are 1 + the rank of the root among the
+// repertoire's core roots, found with one exclusive scan over root flags.
 #include "idb_internal.cuh"
 
 namespace idb {
@@ -68,22 +67,6 @@ __global__ void k_count(const Counters *__restrict__ ctr, uint64_t cap, const ui
     }
 }
 
-// fill pass of the border CSR: each non-core unique lists its core neighbours
-__global__ void k_fill_adj(const Counters *__restrict__ ctr, uint64_t cap, const uint2 *__restrict__ edges,
-                           const uint32_t *__restrict__ ucore, const uint32_t *__restrict__ off,
-                           uint32_t *__restrict__ cursor, uint32_t *__restrict__ adj) {
-    const uint32_t ne = edge_slots(ctr, cap);
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < ne; e += stride) {
-        const uint2 ed = edges[e];
-        if (ed.x == kNone) continue;
-        const uint32_t cx = ucore[ed.x], cy = ucore[ed.y];
-        if (cx == cy) continue;
-        const uint32_t nc = cx ? ed.y : ed.x, c = cx ? ed.x : ed.y;
-        adj[off[nc] + atomicAdd(&cursor[nc], 1u)] = c;
-    }
-}
-
 __global__ void k_core(const Counters *__restrict__ ctr0, Counters *ctr, const uint32_t *__restrict__ cnt,
                        uint32_t min_pts, uint32_t *__restrict__ ucore) {
     const uint32_t nu = ctr0->n_uniques;
@@ -111,11 +94,11 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t *p, uint32_t x) {
     }
 }
 
-// Core-core edges are merged (S6); an edge with one core end counts towards
-// the border CSR degree of its non-core end.
+// Core-core edges are merged (S6); an edge with one core end offers the core
+// to its non-core end, which keeps the minimum (the border rule).
 __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ edges,
                         const uint32_t *__restrict__ ucore, uint32_t *parent,
-                        uint32_t *__restrict__ deg) {
+                        uint32_t *__restrict__ bmin) {
     const uint32_t ne = edge_slots(ctr, cap);
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t n_cc = 0;
@@ -123,7 +106,7 @@ __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ e
         const uint2 ed = edges[e];
         if (ed.x == kNone) continue;
         const uint32_t cx = ucore[ed.x], cy = ucore[ed.y];
-        if (cx != cy) { atomicAdd(&deg[cx ? ed.y : ed.x], 1u); continue; }
+        if (cx != cy) { atomicMin(&bmin[cx ? ed.y : ed.x], cx ? ed.x : ed.y); continue; }
         if (!cx) continue;
         ++n_cc;
         uint32_t a = ed.x, b = ed.y;
@@ -142,21 +125,6 @@ __global__ void k_union(Counters *ctr, uint64_t cap, const uint2 *__restrict__ e
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) n_cc += __shfl_xor_sync(0xFFFFFFFFu, n_cc, d);
     if ((threadIdx.x & 31) == 0 && n_cc) atomicAdd(&ctr->n_core_edges, n_cc);
-}
-
-// border rule: a non-core unique joins its minimum-index core neighbour (its
-// CSR row holds exactly its core neighbours)
-__global__ void k_border(const Counters *__restrict__ ctr, const uint32_t *__restrict__ off,
-                         const uint32_t *__restrict__ adj, const uint32_t *__restrict__ ucore,
-                         uint32_t *__restrict__ bmin) {
-    const uint32_t nu = ctr->n_uniques;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
-        if (ucore[u]) continue;
-        uint32_t best = kNone;
-        for (uint32_t k = off[u]; k < off[u + 1]; ++k) best = min(best, adj[k]);
-        bmin[u] = best;
-    }
 }
 
 // depth of every row in the union-find forest before compression (diagnostic)
@@ -263,16 +231,11 @@ __global__ void k_uniques_out(const Counters *__restrict__ ctr, const uint32_t *
 void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s) {
     const uint64_t ecap = P.cap_edges;
     const int gu = grid_for(P.N);
-    cudaMemsetAsync(B.deg, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
-    cudaMemsetAsync(B.gcur, 0, sizeof(uint32_t) * ((size_t)P.N + 1), s);
     k_graph_init<<<grid_wave(k_graph_init, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ucopies, B.cnt, B.parent, B.bmin);
     k_count<<<grid_wave(k_count, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucopies, B.cnt);
     k_core<<<grid_wave(k_core, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ctr, B.cnt, P.min_pts, B.ucore);
-    // unions, and the degrees of the border CSR (count / scan / fill)
-    k_union<<<grid_wave(k_union, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.parent, B.deg);
-    scan_u32(B.deg, B.goff, P.N + 1, nullptr, nullptr, B.scan_part, B.scan_part_cap, s);
-    k_fill_adj<<<grid_wave(k_fill_adj, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.goff, B.gcur, B.adj);
-    k_border<<<grid_wave(k_border, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.goff, B.adj, B.ucore, B.bmin);
+    // unions of core-core edges; each non-core unique keeps its minimum core neighbour
+    k_union<<<grid_wave(k_union, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.parent, B.bmin);
     if (trees) {
         cudaMemsetAsync(B.depth_hist, 0, sizeof(uint32_t) * (kDepthMax + 1), s);
         k_depth<<<gu, kThreads, 0, s>>>(P.N, B.row2uid, B.urow, B.ucore, B.bmin, B.parent,

@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 #include <fstream>
 #include <iostream>
 #include <map>
@@ -126,6 +127,64 @@ class Config {
 };
 
 // ---------------------------------------------------------------------------
+// One row column as idb_cluster takes it (blob + int64 offsets), in page-locked
+// memory when the library can provide it, packed by all host threads.
+// ---------------------------------------------------------------------------
+class HostColumn {
+    void *mem_ = nullptr;   // page-locked: offsets then bytes
+    std::vector<char> heap_;
+    int64_t *off_ = nullptr;
+    char *blob_ = nullptr;
+
+  public:
+    HostColumn() = default;
+    HostColumn(const HostColumn &) = delete;
+    HostColumn &operator=(const HostColumn &) = delete;
+    ~HostColumn() {
+        if (mem_) idb_host_free(mem_);
+    }
+    void pack(const std::vector<std::string> &v) {
+        const size_t n = v.size();
+        std::vector<int64_t> off(n + 1, 0);
+        // offsets: per-range sums, then a scan over the ranges
+        const size_t nt = std::max<size_t>(1, std::min<size_t>(host_threads(), n / 65536));
+        std::vector<int64_t> part(nt + 1, 0);
+        parallel_ranges(nt, [&](size_t lo, size_t hi) {
+            for (size_t t = lo; t < hi; ++t) {
+                int64_t acc = 0;
+                for (size_t r = n * t / nt; r < n * (t + 1) / nt; ++r) {
+                    acc += (int64_t)v[r].size();
+                    off[r + 1] = acc;
+                }
+                part[t + 1] = acc;
+            }
+        }, 1);
+        for (size_t t = 0; t < nt; ++t) part[t + 1] += part[t];
+        const size_t bytes = (size_t)part[nt];
+        const size_t need = 8 * (n + 1) + bytes;
+        if (idb_host_alloc(need, &mem_) == IDB_OK) {
+            off_ = static_cast<int64_t *>(mem_);
+            blob_ = static_cast<char *>(mem_) + 8 * (n + 1);
+        } else {
+            mem_ = nullptr;
+            heap_.resize(need + 8);
+            off_ = reinterpret_cast<int64_t *>((reinterpret_cast<uintptr_t>(heap_.data()) + 7) & ~(uintptr_t)7);
+            blob_ = reinterpret_cast<char *>(off_ + n + 1);
+        }
+        off_[0] = 0;
+        parallel_ranges(nt, [&](size_t lo, size_t hi) {
+            for (size_t t = lo; t < hi; ++t)
+                for (size_t r = n * t / nt; r < n * (t + 1) / nt; ++r) {
+                    off_[r + 1] = off[r + 1] + part[t];
+                    if (!v[r].empty()) std::memcpy(blob_ + off_[r + 1] - v[r].size(), v[r].data(), v[r].size());
+                }
+        }, 1);
+    }
+    const char *blob() const { return blob_; }
+    const int64_t *offsets() const { return off_; }
+};
+
+// ---------------------------------------------------------------------------
 // The column table (cpp/TableHolder.hpp).
 // ---------------------------------------------------------------------------
 class Table {
@@ -205,8 +264,11 @@ class Table {
         bm.stop("Deleting Empty Rows");
         bm.start("Transferring data to device");
         const size_t n = rows();
-        std::string vb, jb, sb, vgb, jgb;
-        std::vector<int64_t> vo, jo, so, vgo, jgo;
+        std::string vgb, jgb;
+        std::vector<int64_t> vgo, jgo;
+        // the three row columns are packed by all host threads into page-locked
+        // blobs (idb_host_alloc), which idb_cluster copies at the link's full rate
+        HostColumn vcolumn, jcolumn, scolumn;
         auto pack = [](const std::vector<std::string> &v, std::string &blob, std::vector<int64_t> &off) {
             off.assign(1, 0);
             size_t total = 0;
@@ -226,22 +288,22 @@ class Table {
         in.n_rows = (uint32_t)n;
         std::vector<std::string> vnames, jnames;
         if (!vcol.empty()) {
-            pack(column(vcol), vb, vo);
+            vcolumn.pack(column(vcol));
             genes(cfg_.opt("gene_columns.first_gene.ref"), vnames);
             pack(vnames, vgb, vgo);
-            in.v_calls = vb.data(); in.v_offsets = vo.data();
+            in.v_calls = vcolumn.blob(); in.v_offsets = vcolumn.offsets();
             in.v_genes = vgb.data(); in.v_gene_offsets = vgo.data(); in.n_v_genes = (uint32_t)vnames.size();
         }
         if (!jcol.empty()) {
-            pack(column(jcol), jb, jo);
+            jcolumn.pack(column(jcol));
             genes(cfg_.opt("gene_columns.second_gene.ref"), jnames);
             pack(jnames, jgb, jgo);
-            in.j_calls = jb.data(); in.j_offsets = jo.data();
+            in.j_calls = jcolumn.blob(); in.j_offsets = jcolumn.offsets();
             in.j_genes = jgb.data(); in.j_gene_offsets = jgo.data(); in.n_j_genes = (uint32_t)jnames.size();
         }
         if (!scol.empty()) {
-            pack(column(scol), sb, so);
-            in.seqs = sb.data(); in.seq_offsets = so.data();
+            scolumn.pack(column(scol));
+            in.seqs = scolumn.blob(); in.seq_offsets = scolumn.offsets();
         }
         bm.stop("Transferring data to device");
         idb_params prm = {};

@@ -226,6 +226,14 @@ idb_status idb_mlp_train(idb_context *ctx, const float *features, const float *t
                          float *final_loss);
 idb_status idb_mlp_load(idb_context *ctx, const float *params /* NULL = unload */);
 
+/* Page-locked host memory for the input columns of idb_cluster (its
+   host->device copies then run at the full rate of the host link; pageable
+   buffers work too, through the driver's staging).  No counterpart in the
+   reference, whose columns are thrust host vectors (cuda/Interlink.hpp:41-43).
+   idb_host_alloc returns IDB_ERR_OUT_OF_MEMORY if the memory cannot be had. */
+idb_status idb_host_alloc(size_t bytes, void **out);
+idb_status idb_host_free(void *p);
+
 /* Thread-local message of the last failing call ("" if none). */
 size_t idb_last_error(char *buf, size_t size);
 const char *idb_status_string(idb_status s);

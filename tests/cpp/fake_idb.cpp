@@ -1,11 +1,11 @@
-// A stand-in for libimmunodbscan_gb300 with the three entry points psdbscan
-// calls, so the host's table flow (read, delete empty rows, append results,
+// A stand-in for libimmunodbscan_gb300 with the entry points psdbscan calls, so the host's table flow (read, delete empty rows, append results,
 // noise removal, write) runs on a machine without a GPU.  Row r gets
 // clone_id = r % 3, core = r % 2 and copies = 1 + r % 4 (copies = 7 when the
 // parameters ask for the buckets-only candidate path, so the tests can see the
 // key arrive); its V call's length is folded into the stats so the tests can
 // see the columns arrived.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "immunodbscan_gb300.h"
@@ -24,6 +24,16 @@ idb_status idb_cluster(idb_context *, const idb_input *in, const idb_params *prm
         std::memset(out->stats, 0, sizeof(idb_stats));
         out->stats->n_clusters = in->n_rows ? 2 : 0;
     }
+    return IDB_OK;
+}
+
+idb_status idb_host_alloc(size_t bytes, void **out) {
+    *out = std::malloc(bytes ? bytes : 1);
+    return *out ? IDB_OK : IDB_ERR_OUT_OF_MEMORY;
+}
+
+idb_status idb_host_free(void *p) {
+    std::free(p);
     return IDB_OK;
 }
 

@@ -91,6 +91,18 @@ def test_host_surface_cpp(tmp_path):
     assert r.returncode == 0, r.stdout + r.stderr
 
 
+def test_parallel_csv_matches_serial(tmp_path):
+    """The multi-threaded CSV reader and writer give the one-thread forms'
+    tables and bytes (up to 200,000-row files, all of the reader's quirks)."""
+    exe = tmp_path / "test_csv_parallel"
+    subprocess.run(["g++", "-std=c++17", "-O2", "-pthread", "-I",
+                    os.path.join(ROOT, "immunodbscan_gb300", "host"),
+                    os.path.join(ROOT, "tests", "cpp", "test_csv_parallel.cpp"), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
 def _cli():
     from immunodbscan_gb300 import build
     return build.CLI

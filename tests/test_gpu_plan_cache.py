@@ -93,3 +93,33 @@ def test_batch_plan_refused_after_other_call():
         clone, core, copies = b.results()
         o = oracle.cluster(w)
         assert np.array_equal(clone, o.clone_id) and np.array_equal(copies, o.copies)
+
+
+def test_replay_learned_schedule_after_batch_plan():
+    """The bench's sequence: a batch plan with the learned schedule on a
+    context, then repeated host calls on the same context (eager, capture,
+    replays), every one the oracle's answer."""
+    from immunodbscan_gb300 import learned
+    w = synth.workload(2, scale=0.01)
+    o = oracle.cluster(w)
+    with Context(0) as ctx:
+        X, T = learned.profile(w, ctx)
+        p, _ = learned.train(X, T, ctx, epochs=50)
+        learned.install(ctx, p)
+        b = DeviceBatch(w, ctx, schedule=1)
+        b.plan()
+        b.run()
+        _same_triple(b.results(), o, "batch")
+        for k in range(5):
+            g = cluster_workload(w, ctx, schedule=1)
+            _same(g, o, f"host call {k} (launches {g.stats.kernel_launches})")
+        for k in range(3):
+            g = cluster_workload(w, ctx, schedule=0)
+            _same(g, o, f"static host call {k} (launches {g.stats.kernel_launches})")
+
+
+def _same_triple(res, o, label):
+    clone, core, copies = res
+    assert np.array_equal(copies, o.copies), label
+    assert np.array_equal(core, o.core), label
+    assert np.array_equal(clone, o.clone_id), label
