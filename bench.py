@@ -427,6 +427,7 @@ def main():
            "phase_ms": {k: float(np.mean([p[i] for p in r["phases"]])) for i, k in
                         enumerate(["front_dedupe", "buckets_schedule", "distance", "graph",
                                    "outputs"])},
+           "ms_outside_phases": step_ms - float(np.mean([sum(p) for p in r["phases"]])),
            "wall_ms_per_step": 1e3 * r["wall"] / args.steps, "gen_seconds": gen_s,
            "clocks": r["clocks"],
            "static_schedule": {"ms_per_step": r_static["step_ms"],
@@ -572,8 +573,7 @@ def main():
     # Zipf(1.8) (bin sizes 1 .. 10^5), Levenshtein eps=2; trained on a profile of
     # a differently seeded copy, timed against the static schedule
     if learn and not args.no_learned_w3 and args.workload == 2:
-        out["learned_schedule_workload3"] = learned_vs_static(3, 0.25, max(3, args.steps // 4),
-                                                              args.warmup, world, local,
+        out["learned_schedule_workload3"] = learned_vs_static(3, 1.0, 3, 2, world, local,
                                                               args.mlp_epochs)
 
     if rank == 0 and not args.no_workloads and args.workload == 2 and args.scale == 1.0:
@@ -674,16 +674,24 @@ def synth_workload(k):
 
 
 def learned_vs_static(k, scale, steps, warmup, world, local, epochs):
-    """Static and learned schedules on workload k at `scale`: step times, the gain,
-    the network's prediction error next to the static cost model's, equality."""
+    """Static and learned schedules on workload k at `scale` (the learned-
+    scheduling workload: 2M rows, V/J usage Zipf(1.8), Levenshtein eps=2): the
+    network is trained on bin-pair logs of runs of workloads 1 and 2 (the
+    nucleotide Levenshtein and the batched amino-acid Hamming workloads), then
+    the step times, the gain, the network's prediction error on this workload
+    next to the static cost model's, and the equality of the partitions."""
     from immunodbscan_gb300 import Context, DeviceBatch, learned, synth, tuning
     w = synth.workload(k, scale=scale)
     ctx_s, ctx_l = Context(local), Context(local)
     try:
         rec = tuning.measure(w, ctx_s)
         shape = (rec["rx"], rec["ty"])
-        wt = synth.workload(k, scale=scale, seed=4242 + k)
-        X, T = learned.profile(wt, ctx_s, tune=shape)
+        Xs, Ts = [], []
+        for kt, st in ((1, 0.25), (2, 0.1)):
+            X, T = learned.profile(synth.workload(kt, scale=st), ctx_s)
+            Xs.append(X)
+            Ts.append(T)
+        X, T = np.concatenate(Xs), np.concatenate(Ts)
         params, loss = learned.train(X, T, ctx_s, epochs=epochs)
         learned.install(ctx_l, params)
         bs = DeviceBatch(w, ctx_s, schedule=0, tune=shape)
@@ -696,41 +704,15 @@ def learned_vs_static(k, scale, steps, warmup, world, local, epochs):
         cl, kl, _ = bl.results()
         q = prediction_quality(w, ctx_s, shape, params)
         return {"workload": workload_name(w), "tile": {"rx": shape[0], "ty": shape[1]},
+                "trained_on": "bin-pair logs of workload 1 (25%) and workload 2 (10%)",
                 "static_ms_per_step": rs["step_ms"], "learned_ms_per_step": rl["step_ms"],
                 "static_distance_ms": rs["ms_dist"], "learned_distance_ms": rl["ms_dist"],
                 "learned_gain": rs["step_ms"] / rl["step_ms"],
                 "identical_partitions": bool(np.array_equal(cs, cl) and np.array_equal(ks, kl)),
-                "train_binpairs": int(len(T)), **q}
+                "train_binpairs": int(len(T)), "train_mse_log2_cycles": loss, **q}
     finally:
         ctx_s.close()
         ctx_l.close()
-
-
-def copy_times(host_inputs, host_outputs, reps: int = 5):
-    """Time (ms) of the host->device copies of the input columns and of the
-    device->host copies of the outputs alone (pinned memory, CUDA events)."""
-    import torch
-    ins = [t for t in host_inputs if isinstance(t, torch.Tensor)]
-    dev_in = [torch.empty_like(t, device="cuda") for t in ins]
-    dev_out = [torch.empty_like(t, device="cuda") for t in host_outputs]
-    host_out = [torch.empty_like(t).pin_memory() for t in host_outputs]   # leave the results
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-
-    def timed(pairs):
-        best = float("inf")
-        for _ in range(reps):
-            torch.cuda.synchronize()
-            e0.record()
-            for dst, src in pairs:
-                dst.copy_(src, non_blocking=True)
-            e1.record()
-            e1.synchronize()
-            best = min(best, e0.elapsed_time(e1))
-        return best
-    up = timed(list(zip(dev_in, ins)))
-    down = timed(list(zip(host_out, dev_out)))
-    del dev_in, dev_out, host_out
-    return up, down
 
 
 def ops_per_pair(w, batch) -> int:

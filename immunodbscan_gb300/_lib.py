@@ -79,6 +79,7 @@ SIGNATURES = {
     "idb_host_alloc": (C.c_int, [C.c_size_t, C.POINTER(C.c_void_p)]),
     "idb_host_free": (C.c_int, [C.c_void_p]),
     "idb_diag_eps": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_float, C.c_int32]),
+    "idb_diag_eps_hops": (C.c_int32, [C.c_uint32, C.c_uint32, C.c_float, C.c_int32, C.c_int32]),
     "idb_status_string": (C.c_char_p, [C.c_int]),
     "idb_abi_version": (C.c_int, []),
     "idb_dedupe_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,

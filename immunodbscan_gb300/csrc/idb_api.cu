@@ -177,6 +177,48 @@ int eps_value(uint32_t lx, uint32_t ly, float threshold, int32_t abs_eps) {
     return (int)e;
 }
 
+// Bounds on the edit distance of two sequences joined through one or two
+// intermediate neighbours (triangle inequality over the per-hop eps), as the
+// reference's epsilonTwoFunctorClass / epsilonThreeFunctorClass define them
+// (cuda/SpecialFunctors.hcu:276-344; unused by its clustering).  Single
+// precision, in the reference's order of operations: an intermediate sequence
+// within eps of a length-L sequence is at most L / (1 - t) long, so
+//   two hops, Levenshtein: b = min(Lx/(1-t), Ly/(1-t));
+//                          trunc((max(Lx, b) + max(b, Ly)) * t)
+//   three hops:            b = min(Lx/(1-t), Ly/(1-t)/(1-t)),
+//                          c = min(Ly/(1-t), Lx/(1-t)/(1-t));
+//                          trunc((max(Lx, b) + max(c, b) + max(Ly, c)) * t)
+//   Hamming (equal lengths): trunc(Lx * t * hops).
+int eps_hops_value(uint32_t lx, uint32_t ly, float threshold, int hops, bool hamming) {
+    volatile float t = threshold;
+    volatile float fx = (float)lx, fy = (float)ly;
+    if (hamming) {
+        volatile float p = fx * t;
+        volatile float q = p * (float)hops;
+        return (int)truncf(q);
+    }
+    volatile float one_t = 1.0f - t;
+    auto mx = [](float a, float b) { return a > b ? a : b; };
+    auto mn = [](float a, float b) { return a < b ? a : b; };
+    if (hops == 2) {
+        volatile float bx = fx / one_t, by = fy / one_t;
+        volatile float b = mn(bx, by);
+        volatile float sum = mx(fx, b) + mx(b, fy);
+        volatile float prod = sum * t;
+        return (int)truncf(prod);
+    }
+    volatile float bx = fx / one_t, byy0 = fy / one_t;
+    volatile float byy = byy0 / one_t;
+    volatile float b = mn(bx, byy);
+    volatile float cy = fy / one_t, cxx0 = fx / one_t;
+    volatile float cxx = cxx0 / one_t;
+    volatile float c = mn(cy, cxx);
+    volatile float s1 = mx(fx, b) + mx(c, b);
+    volatile float sum = s1 + mx(fy, c);
+    volatile float prod = sum * t;
+    return (int)truncf(prod);
+}
+
 idb_status get_ctx(idb_context **pc);
 
 struct HostInputs {
@@ -1302,6 +1344,13 @@ idb_status idb_batch_run(idb_context *c, idb_stats *stats) {
 
 int32_t idb_diag_eps(uint32_t lx, uint32_t ly, float threshold, int32_t abs_eps) {
     return eps_value(lx, ly, threshold, abs_eps);
+}
+
+int32_t idb_diag_eps_hops(uint32_t lx, uint32_t ly, float threshold, int32_t hops,
+                          int32_t use_hamming) {
+    if (hops == 1) return eps_value(lx, ly, threshold, -1);
+    if (hops != 2 && hops != 3) return INT32_MIN;
+    return eps_hops_value(lx, ly, threshold, hops, use_hamming != 0);
 }
 
 idb_status idb_diag_gene_bits(idb_context *c, const char *calls, const int64_t *offsets,

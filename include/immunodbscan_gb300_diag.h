@@ -27,6 +27,17 @@ int idb_diag_int_peak(int device, double *gops_out, double *ms_out);
    capped by abs_eps when abs_eps >= 0.  Host-only; needs no device. */
 int32_t idb_diag_eps(uint32_t lx, uint32_t ly, float threshold, int32_t abs_eps);
 
+/* The reference's multi-hop distance bounds (epsilonTwoFunctorClass and
+   epsilonThreeFunctorClass, cuda/SpecialFunctors.hcu:276-344), which its
+   clustering never calls: the most edits between two sequences that are joined
+   through hops - 1 intermediate sequences, each step within the relative
+   threshold.  hops = 1 is idb_diag_eps without the absolute cap; 2 and 3 follow
+   the reference's single-precision expressions (Levenshtein form, or the
+   equal-length Hamming form with use_hamming).  INT32_MIN for other hops.
+   Host-only. */
+int32_t idb_diag_eps_hops(uint32_t lx, uint32_t ly, float threshold, int32_t hops,
+                          int32_t use_hamming);
+
 /* Number of admissible unique pairs of the input: pairs of uniques (after the
    duplicate collapse) in one repertoire whose V sets and J sets overlap and
    whose length gap is admissible (equal lengths in Hamming mode, |Lx-Ly| <=

@@ -1,7 +1,9 @@
 // ref_eps_harness.cpp -- test infrastructure: prints the reference's own
 // neighbour threshold (epsilonOneFunctorClass, cuda/SpecialFunctors.hcu:245-274)
-// for a grid of thresholds and length pairs, compiled on the host from the
-// reference header where it lies (oracle/build_ref.py).  The output becomes the
+// and its two- and three-hop bounds (epsilonTwoFunctorClass /
+// epsilonThreeFunctorClass, :276-344) for a grid of thresholds and length
+// pairs, compiled on the host from the reference header where it lies
+// (oracle/build_ref.py).  The output becomes the
 // golden table tests/golden/eps_reference.json.
 //
 // The header derives two functors from thrust::unary_function, which the
@@ -42,6 +44,39 @@ int main() {
         std::printf("  [");
         for (unsigned q = 0; q <= 1024; ++q) std::printf("%s%d", q ? "," : "", h(q, q));
         std::printf("]%s\n", k + 1 < sizeof ts / sizeof ts[0] ? "," : "");
+    }
+    // multi-hop bounds (cuda/SpecialFunctors.hcu:276-344): every length pair up to 64
+    std::printf(" ],\n \"two_hop\": [\n");
+    for (size_t k = 0; k < sizeof ts / sizeof ts[0]; ++k) {
+        epsilonTwoFunctorClass<false> f(ts[k]);
+        std::printf("  [");
+        for (unsigned q = 0; q <= 64; ++q) {
+            std::printf("%s[", q ? ",\n   " : "");
+            for (unsigned s = 0; s <= 64; ++s) std::printf("%s%d", s ? "," : "", f(q, s));
+            std::printf("]");
+        }
+        std::printf("]%s\n", k + 1 < sizeof ts / sizeof ts[0] ? "," : "");
+    }
+    std::printf(" ],\n \"three_hop\": [\n");
+    for (size_t k = 0; k < sizeof ts / sizeof ts[0]; ++k) {
+        epsilonThreeFunctorClass<false> f(ts[k]);
+        std::printf("  [");
+        for (unsigned q = 0; q <= 64; ++q) {
+            std::printf("%s[", q ? ",\n   " : "");
+            for (unsigned s = 0; s <= 64; ++s) std::printf("%s%d", s ? "," : "", f(q, s));
+            std::printf("]");
+        }
+        std::printf("]%s\n", k + 1 < sizeof ts / sizeof ts[0] ? "," : "");
+    }
+    std::printf(" ],\n \"hamming_two_three\": [\n");
+    for (size_t k = 0; k < sizeof ts / sizeof ts[0]; ++k) {
+        epsilonTwoFunctorClass<true> f2(ts[k]);
+        epsilonThreeFunctorClass<true> f3(ts[k]);
+        std::printf("  [[");
+        for (unsigned q = 0; q <= 256; ++q) std::printf("%s%d", q ? "," : "", f2(q, q));
+        std::printf("], [");
+        for (unsigned q = 0; q <= 256; ++q) std::printf("%s%d", q ? "," : "", f3(q, q));
+        std::printf("]]%s\n", k + 1 < sizeof ts / sizeof ts[0] ? "," : "");
     }
     std::printf(" ]}\n");
     return 0;

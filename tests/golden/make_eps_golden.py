@@ -1,9 +1,10 @@
 """Writes tests/golden/eps_reference.json.gz: the reference's own neighbour
-threshold for a grid of thresholds and length pairs, printed by
-oracle/_ref/ref_eps (built by oracle/build_ref.py from the reference's
-cuda/SpecialFunctors.hcu).  Run where the reference tree is present:
+threshold and its two- and three-hop bounds for a grid of thresholds and
+length pairs, printed by oracle/_ref/ref_eps (built by oracle/build_ref.py from
+the reference's cuda/SpecialFunctors.hcu).  Run where the reference tree is
+present:
 
-    python oracle/build_ref.py && python tests/golden/make_eps_golden.py
+    IDB_REFERENCE_TREE=<reference checkout> python tests/golden/make_eps_golden.py
 """
 import gzip
 import json
@@ -16,13 +17,14 @@ ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 import build_ref  # noqa: E402
 
-exe = build_ref.build()
-if not exe:
-    sys.exit("the reference tree is not present")
+if not build_ref.build():
+    sys.exit("IDB_REFERENCE_TREE does not name a reference tree")
+exe = build_ref.EPS_EXE
 out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
 table = json.loads(out)
-table["source"] = ("epsilonOneFunctorClass<false> and <true> of cuda/SpecialFunctors.hcu:245-274, "
-                   "compiled on the host by oracle/build_ref.py")
+table["source"] = ("epsilonOneFunctorClass<false> and <true> (cuda/SpecialFunctors.hcu:245-274), "
+                   "epsilonTwoFunctorClass and epsilonThreeFunctorClass <false> and <true> "
+                   "(:276-344), compiled on the host by oracle/build_ref.py")
 path = os.path.join(HERE, "eps_reference.json.gz")
 with gzip.open(path, "wt") as f:
     json.dump(table, f, separators=(",", ":"))

@@ -17,6 +17,7 @@ pytestmark = pytest.mark.gpu
 
 CASES = [
     ("join", lambda: synth.workload(2, scale=0.01)),
+    ("join_large", lambda: synth.workload(2, scale=0.1)),
     ("buckets", lambda: dataclasses.replace(synth.workload(2, scale=0.01), candidates=1)),
     ("levenshtein", lambda: synth.workload(3, scale=0.01)),
     ("levenshtein_minpts4", lambda: synth.workload(4, scale=0.003)),
@@ -32,7 +33,8 @@ def test_streamed_matches_edge_list(gpu_ctx, name, make, budget_mb):
     assert base.stats.streamed == 0
     ws = dataclasses.replace(w, edge_memory_mb=budget_mb)
     got = cluster_workload(ws, gpu_ctx, eval_trees=True)
-    if budget_mb < 0 or base.stats.neighbour_pairs * 16 > (1 << 20):
+    # the list takes 8 bytes a pair: past 1 MiB the first sweep overflows it
+    if budget_mb < 0 or base.stats.neighbour_pairs * 8 > (1 << 20):
         assert got.stats.streamed == 1, name
     assert np.array_equal(got.copies, base.copies), name
     assert np.array_equal(got.core, base.core), name

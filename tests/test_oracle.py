@@ -134,6 +134,68 @@ def test_library_eps_matches_reference_functor():
             assert L.idb_diag_eps(q, q, C.c_float(t), -1) == ham[q], (t, q)
 
 
+def test_library_multi_hop_bounds_match_reference_functors():
+    """The two- and three-hop bounds (idb_diag_eps_hops) against the reference's
+    epsilonTwoFunctorClass / epsilonThreeFunctorClass, entry by entry, in both
+    the Levenshtein and the equal-length Hamming form."""
+    import ctypes as C
+    from immunodbscan_gb300 import _lib
+    L = _lib.lib()
+    g = _eps_golden()
+    n = g["max_len"]
+    for k, t in enumerate(g["thresholds"]):
+        ft = C.c_float(t)
+        for hops, key in ((2, "two_hop"), (3, "three_hop")):
+            tab = g[key][k]
+            for q in range(n + 1):
+                for s in range(n + 1):
+                    assert L.idb_diag_eps_hops(q, s, ft, hops, 0) == tab[q][s], (key, t, q, s)
+        h2, h3 = g["hamming_two_three"][k]
+        for q in range(len(h2)):
+            assert L.idb_diag_eps_hops(q, q, ft, 2, 1) == h2[q], ("hamming two", t, q)
+            assert L.idb_diag_eps_hops(q, q, ft, 3, 1) == h3[q], ("hamming three", t, q)
+
+
+@pytest.mark.parametrize("t", [0.1, 0.15, 0.25])
+def test_multi_hop_bound_holds_on_neighbour_chains(t):
+    """What the bounds promise: sequences joined through one (two) intermediate
+    neighbours under the relative threshold are within the two-hop (three-hop)
+    bound of each other, by the oracle's edit distance."""
+    import ctypes as C
+    from immunodbscan_gb300 import _lib
+    L = _lib.lib()
+    rng = np.random.default_rng(int(t * 1000))
+    alpha = list(b"ACDEFGHIKLMNPQRSTVWY")
+
+    def mutate(x, k):
+        x = bytearray(x)
+        for _ in range(k):
+            op = rng.integers(0, 3)
+            if op == 0 and x:
+                x[int(rng.integers(0, len(x)))] = int(rng.choice(alpha))
+            elif op == 1 and len(x) > 1:
+                del x[int(rng.integers(0, len(x)))]
+            else:
+                x.insert(int(rng.integers(0, len(x) + 1)), int(rng.choice(alpha)))
+        return bytes(x)
+
+    def near(a, b):
+        return oracle.levenshtein(a, b) <= oracle.eps(len(a), len(b), t, -1)
+
+    chains = 0
+    for _ in range(3000):
+        x = bytes(rng.choice(alpha, size=int(rng.integers(8, 30))).astype(np.uint8))
+        b = mutate(x, int(rng.integers(0, 5)))
+        c = mutate(b, int(rng.integers(0, 5)))
+        y = mutate(c, int(rng.integers(0, 5)))
+        if near(x, b) and near(b, c):
+            chains += 1
+            assert oracle.levenshtein(x, c) <= L.idb_diag_eps_hops(len(x), len(c), C.c_float(t), 2, 0)
+            if near(c, y):
+                assert oracle.levenshtein(x, y) <= L.idb_diag_eps_hops(len(x), len(y), C.c_float(t), 3, 0)
+    assert chains > 100
+
+
 def _segments(L, S):
     return [(k * L // S, (k + 1) * L // S) for k in range(S)]
 
