@@ -715,6 +715,33 @@ def learned_vs_static(k, scale, steps, warmup, world, local, epochs):
         ctx_l.close()
 
 
+def copy_times(host_inputs, host_outputs, reps: int = 5):
+    """Time (ms) of the host->device copies of the input columns and of the
+    device->host copies of the outputs alone (pinned memory, CUDA events)."""
+    import torch
+    ins = [t for t in host_inputs if isinstance(t, torch.Tensor)]
+    dev_in = [torch.empty_like(t, device="cuda") for t in ins]
+    dev_out = [torch.empty_like(t, device="cuda") for t in host_outputs]
+    host_out = [torch.empty_like(t).pin_memory() for t in host_outputs]   # leave the results
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed(pairs):
+        best = float("inf")
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            e0.record()
+            for dst, src in pairs:
+                dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+        return best
+    up = timed(list(zip(dev_in, ins)))
+    down = timed(list(zip(host_out, dev_out)))
+    del dev_in, dev_out, host_out
+    return up, down
+
+
 def ops_per_pair(w, batch) -> int:
     """Algorithmic 32-bit integer ops per evaluated pair of the distance kernel.
 

@@ -176,14 +176,18 @@ idb_status idb_batch_run(idb_context *ctx, idb_stats *stats);
    class size at that row and 0 elsewhere -- the copies column idb_cluster
    returns for the same rows.  Inputs and outputs are caller-owned device
    memory; v_bits / j_bits (n_rows x v_words / j_words uint64 words, bit g =
-   reference gene g) may be NULL.  Its hash table lives in a fixed ~5 MB
+   reference gene g, 1 <= words <= 8, i.e. at most 512 genes a column) may be
+   NULL.  Its hash table lives in a fixed ~5 MB
    __device__ array inside the library, which every GPU that loads the library
    holds until the process exits; at most IDB_DEDUPE_NOALLOC_MAX_ROWS rows
    (larger inputs are rejected with IDB_ERR_UNSUPPORTED).  Runs on the calling
    thread's current device and on `stream` (a cudaStream_t, NULL = legacy
-   default stream) and returns when the results are complete.  The first call
-   on a device resolves the array's address (cudaGetSymbolAddress); make that
-   first call before any stream capture.  All calls on a device share the
+   default stream) and returns when the results are complete: it waits on the
+   stream and reads an error word back, so it cannot be called while that
+   stream is being captured.  The first call on a device resolves the array's
+   address (cudaGetSymbolAddress) and keeps it for the life of the process;
+   after cudaDeviceReset that address is stale, so the entry point is not for
+   use across device resets.  All calls on a device share the
    array, which keeps the last call's contents (each call resets it first):
    calls that overlap on the GPU race and must be serialised by the caller.
    Calls no cudaMalloc, cudaFree or allocating library routine. */
