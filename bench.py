@@ -578,6 +578,7 @@ def main():
 
     if rank == 0 and not args.no_workloads and args.workload == 2 and args.scale == 1.0:
         out["workloads"] = workload_table(local)
+        out["csv_to_csv"] = csv_roundtrip()
 
     parity_ok = True
     if rank == 0 and not args.no_cpu:
@@ -666,6 +667,123 @@ def workload_table(local, steps: int = 3, warmup: int = 2):
             ctx_b.close()
             ctx_p.close()
     return rows
+
+
+_CSV_CONF = """input_settings
+{
+    separator "\\t"
+    decimal "."
+    endline "\\n"
+    quotation "\\""
+}
+select_columns_to_read
+{
+    id_column_name "Sequence ID"
+    v_gene_column_name "V-GENE and allele"
+    j_gene_column_name "J-GENE and allele"
+    cdr3_column_name "CDR3-IMGT"
+}
+gene_columns
+{
+    first_gene
+    {
+        name v_gene_column_name
+        ref "@V@"
+    }
+    second_gene
+    {
+        name j_gene_column_name
+        ref "@J@"
+    }
+}
+sequence_columns
+{
+    name cdr3_column_name
+}
+maximum_absolute_edit_distance 1
+minimum_number_of_neighbors 2
+use_hamming true
+output_prefix "output_"
+output_suffix ""
+output_filetype ".csv"
+output_settings
+{
+    separator "\\t"
+    decimal "."
+    endline "\\n"
+    quotation "\\0"
+}
+remove_noise_from_output false
+select_columns_to_write
+{
+    id_column_name "ID.code"
+    v_gene_column_name "V_CALL"
+    cdr3_column_name "CDR3"
+    cores "Cores"
+    copies "Copies"
+    clone_id "Clone"
+}
+benchmark_output_prefix "benchmark_"
+benchmark_output_suffix ""
+benchmark_output_filetype ".csv"
+benchmark_output_settings
+{
+    separator "\\t"
+    decimal "."
+    endline "\\n"
+    quotation "\\""
+}
+"""
+
+
+def csv_roundtrip(scale: float = 0.2):
+    """psdbscan (the command-line host) from a TSV file to a TSV file: the rows of
+    20% of the bench workload (1.0M rows) as one table, Hamming eps=1.  Wall
+    times of its reading, clustering and writing steps (its benchmark log)."""
+    import shutil
+    import tempfile
+    from immunodbscan_gb300 import build, synth
+    w = synth.workload(2, scale=scale)
+    d = tempfile.mkdtemp(prefix="idb_csv_")
+    try:
+        vg, jg = os.path.join(d, "V.txt"), os.path.join(d, "J.txt")
+        with open(vg, "wb") as f:
+            f.write(b"\n".join(w.v_genes) + b"\n")
+        with open(jg, "wb") as f:
+            f.write(b"\n".join(w.j_genes) + b"\n")
+        conf = os.path.join(d, "bench.conf")
+        with open(conf, "w") as f:
+            f.write(_CSV_CONF.replace("@V@", vg).replace("@J@", jg))
+        inp = os.path.join(d, "rows.tsv")
+        with open(inp, "wb") as f:
+            f.write(b"Sequence ID\tV-GENE and allele\tJ-GENE and allele\tCDR3-IMGT\n")
+            chunk = []
+            for i in range(w.n):
+                chunk.append(b"id%d\t%s\t%s\t%s\n" % (i, w.vcall(i), w.jcall(i), w.seq(i)))
+                if len(chunk) == 100000:
+                    f.write(b"".join(chunk))
+                    chunk = []
+            f.write(b"".join(chunk))
+        t0 = time.perf_counter()
+        r = subprocess.run([build.CLI, "--config_file", conf, "--input", inp], capture_output=True,
+                           text=True, cwd=d)
+        wall = time.perf_counter() - t0
+        if r.returncode != 0:
+            return {"error": (r.stdout + r.stderr)[-300:]}
+        timers = {}
+        with open(os.path.join(d, "benchmark_rows.csv")) as f:
+            for line in f:
+                p = line.rstrip("\n").split("\t")
+                if len(p) == 2 and p[1].endswith(" sec"):
+                    timers[p[0]] = float(p[1][:-4])
+        return {"rows": int(w.n), "input_bytes": os.path.getsize(inp),
+                "output_bytes": os.path.getsize(os.path.join(d, "output_rows.csv")),
+                "read_s": timers.get("Reading Files"), "cluster_s": timers.get("Do clustering"),
+                "write_s": timers.get("Writing Output"), "total_s": timers.get("Overall"),
+                "wall_s": wall, "rows_per_s": w.n / wall,
+                "api": "psdbscan --config_file --input (one table, Hamming eps=1, minPts=2)"}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
 
 
 def synth_workload(k):
