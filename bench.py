@@ -526,8 +526,10 @@ def main():
         barrier(world)
         e2e_s = allreduce_max(world, float(np.mean(times)))
         h2d = sum(int(a.numel() * a.element_size()) for a in hkeep if isinstance(a, torch.Tensor))
-        # breakdown: the same host->device copies alone, the device time of the
-        # path (the call's own time stamps), the result copies alone
+        # breakdown: the same host->device copies alone; the span of the path on
+        # the device (the call's own time stamps, from its first kernel to its
+        # last: the columns arrive by row chunks during it, so it includes the
+        # waits for the copies it overlaps); the result copies alone
         up_ms, down_ms = copy_times(hkeep, (clone, core, copies))
         out["e2e"] = {"value": world * admissible / e2e_s / 1e9, "unit": UNIT,
                       "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": 12 * n,
@@ -535,9 +537,10 @@ def main():
                       "api": "idb_cluster (host buffers, %s schedule)" % ("learned" if learn else
                                                                            "static"),
                       "replayed": bool(est.kernel_launches > 0),
-                      "breakdown_ms": {"upload": up_ms, "device": float(np.mean(dev_ms)),
-                                       "download": down_ms,
-                                       "other": e2e_s * 1e3 - up_ms - float(np.mean(dev_ms)) - down_ms}}
+                      "breakdown_ms": {"upload_alone": up_ms, "device_span": float(np.mean(dev_ms)),
+                                       "download_alone": down_ms,
+                                       "batched_device_step": step_ms,
+                                       "serial_sum": up_ms + step_ms + down_ms}}
         diff = ((clone.numpy().view(np.uint32) != clone_b) | (core.numpy() != core_b) |
                 (copies.numpy().view(np.uint32) != copies_b))
         out["e2e"]["identical_partitions_vs_batched"] = bool(not diff.any())

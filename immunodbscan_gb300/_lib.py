@@ -31,7 +31,8 @@ class Params(C.Structure):
     _fields_ = [("threshold", C.c_float), ("abs_eps", C.c_int32), ("min_pts", C.c_uint32),
                 ("use_hamming", C.c_int32), ("eval_trees", C.c_int32), ("schedule", C.c_int32),
                 ("tile_rx", C.c_int32), ("tile_ty", C.c_int32), ("candidates", C.c_int32),
-                ("edge_memory_mb", C.c_int32), ("reserved", C.c_int32 * 2)]
+                ("edge_memory_mb", C.c_int32), ("row_chunks", C.c_int32),
+                ("reserved", C.c_int32 * 1)]
 
 
 class Tuning(C.Structure):

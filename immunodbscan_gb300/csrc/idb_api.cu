@@ -70,7 +70,7 @@ enum BufId {
     bURow, bUCopies, bULen, bURep, bBinHist, bBinCursor, bEntUid, bEntRec, bBpCount, bBp,
     bBpSorted, bBpUnits, bClsHist, bPred, bEdges, bCnt, bUCore,
     bParent, bBMin, bRootFlag, bUidFirst, bDepth, bScanPart, bClone, bCore, bCopies, bUniques,
-    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bBpSmall,
+    bCtr, bVTab, bJTab, bSigAnd, bUClass, bEntMeta, bCallAux, bCallTab, bCallRef, bCallTodo, bBpSmall,
     bJnTab, bJnISlot, bJnStart, bJnCur, bJnBpIdx, bNumBufs
 };
 
@@ -79,8 +79,9 @@ enum BufId {
 struct idb_context {
     int device = 0;
     cudaStream_t stream = nullptr;
-    cudaStream_t copy_stream = nullptr;   // host->device copies of the call columns
-    cudaEvent_t ev_v = nullptr, ev_j = nullptr;   // those copies done
+    cudaStream_t copy_stream = nullptr;   // host->device copies of the columns
+    cudaEvent_t ev_seq = nullptr;         // sequence column copied
+    cudaEvent_t ev_chunk[kMaxRowChunks] = {};   // call columns of row chunk k copied
     DevBuf buf[bNumBufs];
     Counters *h_ctr = nullptr;        // pinned mirror of the counters
     cudaEvent_t ev[16] = {};
@@ -250,6 +251,8 @@ idb_status validate(const idb_input *in, const idb_params *prm, const idb_output
         return fail(IDB_ERR_INVALID_ARG, "neither threshold nor abs_eps is set");
     if (prm->candidates != 0 && prm->candidates != 1)
         return fail(IDB_ERR_INVALID_ARG, "candidates must be 0 (automatic) or 1 (buckets)");
+    if (prm->row_chunks < 0 || prm->row_chunks > kMaxRowChunks)
+        return fail(IDB_ERR_INVALID_ARG, "row_chunks must be 0 (automatic) to %d", kMaxRowChunks);
     if (in->n_repertoires > 0 && in->rep_offsets) {
         if (in->rep_offsets[0] != 0 || in->rep_offsets[in->n_repertoires] != in->n_rows)
             return fail(IDB_ERR_INVALID_ARG, "rep_offsets must start at 0 and end at n_rows");
@@ -311,9 +314,14 @@ struct Pipeline {
     bool trees = false;
     bool timing = false;
     std::vector<int16_t> eps_host;
-    // host inputs: the V / J call columns arrive on the copy stream, overlapped
-    // with the sequence survey and the plan; their gene-bitset kernels wait here
-    cudaEvent_t wait_v = nullptr, wait_j = nullptr;
+    // host inputs arrive on the copy stream: the sequence column first (the
+    // survey waits for it), then the call columns row chunk by row chunk (the
+    // gene-bitset kernels of chunk k wait for its event).  In a graph capture
+    // the waits become external event-wait nodes, so a replay waits for the
+    // copies its own call issued.
+    cudaEvent_t wait_seq = nullptr;
+    cudaEvent_t wait_chunk[kMaxRowChunks] = {};
+    bool external_waits = false;
     bool copies_issued = false;
     bool allow_join = true;   // the segment join finds neighbours, not all admissible pairs
     // every return path (errors included) leaves no copy from the caller's host
@@ -334,8 +342,60 @@ void phase_times(const Counters &h, idb_stats *st) {
     st->ms_distance = st->ms_phase[2];
 }
 
+// Row chunks of the front end.  Host columns of 2^20 rows or more are copied
+// and pre-processed in kMaxRowChunks chunks (or `want`, 1..kMaxRowChunks), so
+// that the gene-bitset and duplicate kernels of a chunk run while the next
+// chunks are being copied; device-resident columns are one chunk.  Inner
+// boundaries are multiples of 32 rows.
+void set_row_chunks(Plan &P, bool host_inputs, int want) {
+    uint32_t k = 1;
+    if (host_inputs) {
+        if (want > 0) k = (uint32_t)std::min(want, kMaxRowChunks);
+        else if (P.N >= (1u << 20)) k = kMaxRowChunks;
+    }
+    P.nchunks = k;
+    P.chunk_row[0] = 0;
+    for (uint32_t i = 1; i < k; ++i)
+        P.chunk_row[i] = (uint32_t)(((uint64_t)P.N * i / k) & ~31ull);
+    P.chunk_row[k] = P.N;
+}
+
+// Host columns onto the copy stream in the order the device needs them: the
+// sequences (for the survey), then the V and J calls of each row chunk, each
+// followed by its event.  Copies of a column go into its staging buffer at the
+// host offsets, so chunk k's bytes and offsets land where the kernels read them.
+idb_status issue_host_copies(idb_context *c, const Plan &P, const idb_input *in) {
+    cudaStream_t cs = c->copy_stream;
+    const size_t N = P.N;
+    if (!P.no_seq) {
+        if (in->seq_offsets[N])
+            CU(cudaMemcpyAsync(c->buf[bSeq].p, in->seqs, (size_t)in->seq_offsets[N],
+                               cudaMemcpyHostToDevice, cs));
+        CU(cudaMemcpyAsync(c->buf[bSeqOff].p, in->seq_offsets, 8 * (N + 1), cudaMemcpyHostToDevice, cs));
+    }
+    CU(cudaEventRecord(c->ev_seq, cs));
+    auto column = [&](const char *src, const int64_t *off, BufId bid, BufId oid, uint32_t r0,
+                      uint32_t r1) -> idb_status {
+        const int64_t b0 = off[r0], b1 = off[r1];
+        if (b1 > b0)
+            CU(cudaMemcpyAsync(static_cast<char *>(c->buf[bid].p) + b0, src + b0, (size_t)(b1 - b0),
+                               cudaMemcpyHostToDevice, cs));
+        CU(cudaMemcpyAsync(static_cast<int64_t *>(c->buf[oid].p) + r0, off + r0,
+                           8 * ((size_t)(r1 - r0) + 1), cudaMemcpyHostToDevice, cs));
+        return IDB_OK;
+    };
+    for (uint32_t k = 0; k < P.nchunks; ++k) {
+        const uint32_t r0 = P.chunk_row[k], r1 = P.chunk_row[k + 1];
+        if (!P.no_v) TRY(column(in->v_calls, in->v_offsets, bV, bVOff, r0, r1));
+        if (!P.no_j) TRY(column(in->j_calls, in->j_offsets, bJ, bJOff, r0, r1));
+        CU(cudaEventRecord(c->ev_chunk[k], cs));
+    }
+    return IDB_OK;
+}
+
 // Stage 0: inputs in place, counters zeroed, survey run and read back.
-idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_inputs) {
+idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_inputs,
+                                   int row_chunks = 0) {
     idb_context *c = pl.c;
     Plan &P = pl.P;
     Buffers &B = pl.B;
@@ -346,23 +406,21 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
     P.no_v = in->v_calls == nullptr;
     P.no_j = in->j_calls == nullptr;
     P.no_seq = in->seqs == nullptr;
+    set_row_chunks(P, host_inputs, row_chunks);
     TRY(ensure(c, bCtr, sizeof(Counters)));
     B.ctr = ptr<Counters>(c, bCtr);
     CU(cudaMemsetAsync(B.ctr, 0, sizeof(Counters), s));
     CU(cudaMemsetAsync(&B.ctr->lmin, 0xFF, sizeof(uint32_t), s));   // min starts at max
-    auto stage = [&](const char *src, const int64_t *off, BufId bid, BufId oid,
-                     const uint8_t **dst, const int64_t **doff, cudaStream_t cs) -> idb_status {
+    // staging buffers of host columns (device columns are read in place)
+    auto place = [&](const char *src, const int64_t *off, BufId bid, BufId oid,
+                     const uint8_t **dst, const int64_t **doff) -> idb_status {
         if (!host_inputs) {
             *dst = reinterpret_cast<const uint8_t *>(src);
             *doff = off;
             return IDB_OK;
         }
-        const size_t nbytes = (size_t)(P.N ? off[P.N] : 0);
-        TRY(ensure(c, bid, nbytes + 16));
+        TRY(ensure(c, bid, (size_t)(P.N ? off[P.N] : 0) + 16));
         TRY(ensure(c, oid, sizeof(int64_t) * ((size_t)P.N + 1)));
-        if (nbytes) CU(cudaMemcpyAsync(c->buf[bid].p, src, nbytes, cudaMemcpyHostToDevice, cs));
-        CU(cudaMemcpyAsync(c->buf[oid].p, off, sizeof(int64_t) * ((size_t)P.N + 1),
-                           cudaMemcpyHostToDevice, cs));
         *dst = ptr<uint8_t>(c, bid);
         *doff = ptr<int64_t>(c, oid);
         return IDB_OK;
@@ -374,19 +432,17 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
         B.seq = ptr<uint8_t>(c, bSeq);
         B.seq_off = ptr<int64_t>(c, bSeqOff);
     } else {
-        TRY(stage(in->seqs, in->seq_offsets, bSeq, bSeqOff, &B.seq, &B.seq_off, s));
+        TRY(place(in->seqs, in->seq_offsets, bSeq, bSeqOff, &B.seq, &B.seq_off));
     }
-    // host inputs: the call columns go on the copy stream, behind nothing, while
-    // the main stream surveys the sequences and the host derives the plan
-    cudaStream_t cs = host_inputs ? c->copy_stream : s;
-    pl.copies_issued = host_inputs;
-    if (!P.no_v) {
-        TRY(stage(in->v_calls, in->v_offsets, bV, bVOff, &B.vcall, &B.v_off, cs));
-        if (host_inputs) { CU(cudaEventRecord(c->ev_v, cs)); pl.wait_v = c->ev_v; }
-    }
-    if (!P.no_j) {
-        TRY(stage(in->j_calls, in->j_offsets, bJ, bJOff, &B.jcall, &B.j_off, cs));
-        if (host_inputs) { CU(cudaEventRecord(c->ev_j, cs)); pl.wait_j = c->ev_j; }
+    if (!P.no_v) TRY(place(in->v_calls, in->v_offsets, bV, bVOff, &B.vcall, &B.v_off));
+    if (!P.no_j) TRY(place(in->j_calls, in->j_offsets, bJ, bJOff, &B.jcall, &B.j_off));
+    if (host_inputs) {
+        // every copy is issued now; the survey waits for the sequences only and
+        // the host derives the plan while the call columns are still arriving
+        pl.copies_issued = true;
+        TRY(issue_host_copies(c, P, in));
+        CU(cudaStreamWaitEvent(s, c->ev_seq, 0));
+        for (uint32_t k = 0; k < P.nchunks; ++k) pl.wait_chunk[k] = c->ev_chunk[k];
     }
     // repertoire offsets
     std::vector<uint32_t> roff(P.R + 1);
@@ -425,11 +481,12 @@ idb_status stage_inputs_and_survey(Pipeline &pl, const idb_input *in, bool host_
 }
 
 // Work-unit shape: rx x-entries per lane (the kernels are compiled for
-// Hamming 4 or 8 with one word, 4 otherwise; Levenshtein 1, or 2 with one word)
-// and ty y-entries, a multiple of 32*rx up to 4096.  Invalid values are ignored.
+// Hamming 4 or 8 with one word, 4 otherwise, and 2 with one word for the
+// segment join; Levenshtein 1, or 2 with one word) and ty y-entries, a multiple
+// of 32*rx up to 4096.  Invalid values are ignored.
 void apply_shape(Plan &P, int rx, int ty) {
     if (rx > 0) {
-        if (P.hamming && (rx == 4 || (rx == 8 && P.W == 1))) P.RX = rx;
+        if (P.hamming && (rx == 4 || ((rx == 8 || rx == 2) && P.W == 1))) P.RX = rx;
         if (!P.hamming && (rx == 1 || (rx == 2 && P.W == 1))) P.RX = rx;
         P.TX = 32 * P.RX;
     }
@@ -515,6 +572,19 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
              P.Gv <= 64 && P.Gj <= 30 && P.R < (1u << 24) - 1 &&
              2ull * (uint64_t)(emax_same + 1) * P.N <= (1ull << 30);
     P.join_smax = P.join ? (uint32_t)std::max(1, emax_same + 1) : 1u;
+    if (P.hamming && P.RX == 2 && !P.join) {   // 2 x-entries per lane: segment join only
+        P.RX = 4;
+        P.TX = 128;
+        if (P.TY % P.TX) P.TY = P.TX * ((P.TY + P.TX - 1) / P.TX);
+    }
+    // segment join without a requested shape: 2 x-entries per lane, 512 y-entries
+    // (its groups are mostly small: narrower x-chunks leave fewer lanes idle)
+    if (P.join && P.W == 1 && prm->tile_rx <= 0) {
+        P.RX = 2;
+        P.TX = 64;
+        if (prm->tile_ty <= 0) P.TY = 512;
+        if (P.TY % P.TX) P.TY = P.TX * ((P.TY + P.TX - 1) / P.TX);
+    }
     P.nbins = (uint64_t)P.R * P.Gv * P.Gj * P.NL * P.K;
     if (P.nbins >= (1ull << 31))
         return fail(IDB_ERR_UNSUPPORTED, "too many buckets (repertoires x V genes x J genes x lengths = %llu)",
@@ -522,16 +592,29 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
     return IDB_OK;
 }
 
-// Workspace for everything sized by N and the plan.
-// The call-string table of the gene-bitset phase lives in the duplicate
-// table's memory (4*tcap bytes, at most 2^20 slots of 8 bytes).
-void set_call_scratch(Buffers &B, uint64_t tcap, uint32_t *aux) {
-    B.call_tab = reinterpret_cast<unsigned long long *>(B.table);
-    B.call_mask = (uint32_t)(std::min<uint64_t>(tcap / 2, 1u << 20) - 1);
-    B.call_ref = B.slot;
-    B.call_todo = B.rep_row;
-    B.call_ntodo = aux;
+// Scratch of the call-string collapse of both gene columns: per column a
+// table of min(N, 2^20) rounded up to a power of two 8-byte slots (at least
+// 512), a slot per row and a list of the rows that compute their own bitset.
+// Its own memory, so that a row chunk's duplicate kernel can run between the
+// call collapses of the next chunk.
+idb_status alloc_call_scratch(idb_context *c, Buffers &B, uint64_t N) {
+    const uint64_t slots = std::min<uint64_t>(next_pow2(std::max<uint64_t>(N, 512)), 1u << 20);
+    TRY(ensure(c, bCallTab, 2 * 8 * slots));
+    TRY(ensure(c, bCallRef, 2 * 4 * N));
+    TRY(ensure(c, bCallTodo, 2 * 4 * N));
+    TRY(ensure(c, bCallAux, 2 * 4 * kMaxRowChunks));
+    for (int k = 0; k < 2; ++k) {
+        CallScratch &cs = B.call[k];
+        cs.tab = ptr<unsigned long long>(c, bCallTab) + k * slots;
+        cs.mask = (uint32_t)(slots - 1);
+        cs.ref = ptr<uint32_t>(c, bCallRef) + k * N;
+        cs.todo = ptr<uint32_t>(c, bCallTodo) + k * N;
+        cs.ntodo = ptr<uint32_t>(c, bCallAux) + k * kMaxRowChunks;
+    }
+    return IDB_OK;
 }
+
+// Workspace for everything sized by N and the plan.
 
 idb_status alloc_fixed(Pipeline &pl) {
     idb_context *c = pl.c;
@@ -598,8 +681,7 @@ idb_status alloc_fixed(Pipeline &pl) {
     B.row2uid = ptr<uint32_t>(c, bRow2Uid);
     B.table = ptr<uint32_t>(c, bTable); B.tcount = ptr<uint32_t>(c, bTCount);
     B.table_mask = tcap - 1;
-    TRY(ensure(c, bCallAux, 16));
-    set_call_scratch(B, tcap, ptr<uint32_t>(c, bCallAux));
+    TRY(alloc_call_scratch(c, B, N));
     B.urow = ptr<uint32_t>(c, bURow); B.ucopies = ptr<uint32_t>(c, bUCopies);
     B.ulen = ptr<uint32_t>(c, bULen); B.urep = ptr<uint32_t>(c, bURep);
     B.bin_hist = ptr<uint32_t>(c, bBinHist); B.bin_cursor = ptr<uint32_t>(c, bBinCursor);
@@ -675,18 +757,35 @@ idb_status device_errors(const Counters &h) {
 
 // Phases after the survey.  With `eager`, sizes are read back and buffers grown
 // between phases; otherwise (graph capture) the capacities in P are used as-is.
+// Gene bitsets and duplicate collapse, row chunk by row chunk: chunk k's
+// kernels wait for its copies (when they are still in flight) and nothing else.
+idb_status launch_front(Pipeline &pl, cudaStream_t s) {
+    const Plan &P = pl.P;
+    const Buffers &B = pl.B;
+    launch_call_init(P, B, true, s);
+    launch_call_init(P, B, false, s);
+    launch_dedupe_init(P, B, s);
+    for (uint32_t k = 0; k < P.nchunks; ++k) {
+        if (pl.wait_chunk[k])
+            CU(cudaStreamWaitEvent(s, pl.wait_chunk[k], pl.external_waits ? cudaEventWaitExternal : 0));
+        launch_gene_bits(P, B, true, k, s);
+        launch_gene_bits(P, B, false, k, s);
+        launch_dedupe_rows(P, B, k, s);
+    }
+    launch_dedupe_final(P, B, s);
+    // a later run of the phases finds the columns in place
+    if (!pl.external_waits)
+        for (auto &e : pl.wait_chunk) e = nullptr;
+    return IDB_OK;
+}
+
 idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false) {
     idb_context *c = pl.c;
     Plan &P = pl.P;
     Buffers &B = pl.B;
     cudaStream_t s = c->stream;
     if (!eager) launch_check_plan(P, B, s);
-    if (pl.wait_v) CU(cudaStreamWaitEvent(s, pl.wait_v, 0));
-    launch_gene_bits(P, B, true, s);
-    if (pl.wait_j) CU(cudaStreamWaitEvent(s, pl.wait_j, 0));
-    launch_gene_bits(P, B, false, s);
-    pl.wait_v = pl.wait_j = nullptr;   // a later run of the phases finds the columns in place
-    launch_dedupe(P, B, s);
+    TRY(launch_front(pl, s));
     launch_uniques(P, B, s);
     TRY(check_launch());
     record(pl, 1);
@@ -804,7 +903,7 @@ bool same_params(const idb_params &a, const idb_params &b) {
     return ta == tb && a.abs_eps == b.abs_eps && a.min_pts == b.min_pts &&
            a.use_hamming == b.use_hamming && a.schedule == b.schedule && a.tile_rx == b.tile_rx &&
            a.tile_ty == b.tile_ty && a.candidates == b.candidates &&
-           a.edge_memory_mb == b.edge_memory_mb;
+           a.edge_memory_mb == b.edge_memory_mb && a.row_chunks == b.row_chunks;
 }
 
 void gene_key(const char *names, const int64_t *off, uint32_t G, std::vector<char> &b,
@@ -899,11 +998,15 @@ idb_status host_plan_capture(Pipeline &pl) {
     CU(cudaStreamSynchronize(s));
     pl.timing = true;
     pl.trees = false;
-    pl.wait_v = pl.wait_j = nullptr;
+    // a replay's copies are issued on the copy stream before the graph is
+    // launched: the graph waits on their events (external event-wait nodes)
+    pl.external_waits = true;
+    for (uint32_t k = 0; k < kMaxRowChunks; ++k) pl.wait_chunk[k] = k < pl.P.nchunks ? c->ev_chunk[k] : nullptr;
     CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(pl.B.ctr, 0, sizeof(Counters), s);
     cudaMemsetAsync(&pl.B.ctr->lmin, 0xFF, sizeof(uint32_t), s);
     record(pl, 0);
+    cudaStreamWaitEvent(s, c->ev_seq, cudaEventWaitExternal);
     launch_survey(pl.P, pl.B, s);
     idb_status st = run_phases(pl, false);
     cudaGraph_t g = nullptr;
@@ -941,26 +1044,9 @@ idb_status host_plan_run(idb_context *c, const idb_input *in, idb_output *out) {
         cudaStream_t cs;
         ~CopyGuard() { cudaStreamSynchronize(cs); }
     } guard{cs};
-    if (!h.no_seq) {
-        if (in->seq_offsets[N])
-            CU(cudaMemcpyAsync(c->buf[bSeq].p, in->seqs, (size_t)in->seq_offsets[N],
-                               cudaMemcpyHostToDevice, s));
-        CU(cudaMemcpyAsync(c->buf[bSeqOff].p, in->seq_offsets, 8 * (N + 1), cudaMemcpyHostToDevice, s));
-    }
-    if (!h.no_v) {
-        if (in->v_offsets[N])
-            CU(cudaMemcpyAsync(c->buf[bV].p, in->v_calls, (size_t)in->v_offsets[N],
-                               cudaMemcpyHostToDevice, cs));
-        CU(cudaMemcpyAsync(c->buf[bVOff].p, in->v_offsets, 8 * (N + 1), cudaMemcpyHostToDevice, cs));
-    }
-    if (!h.no_j) {
-        if (in->j_offsets[N])
-            CU(cudaMemcpyAsync(c->buf[bJ].p, in->j_calls, (size_t)in->j_offsets[N],
-                               cudaMemcpyHostToDevice, cs));
-        CU(cudaMemcpyAsync(c->buf[bJOff].p, in->j_offsets, 8 * (N + 1), cudaMemcpyHostToDevice, cs));
-    }
-    CU(cudaEventRecord(c->ev_v, cs));
-    CU(cudaStreamWaitEvent(s, c->ev_v, 0));
+    // the copies go first on the copy stream; the graph's event-wait nodes hold
+    // each part of the path until the rows it reads have arrived
+    TRY(issue_host_copies(c, h.P, in));
     CU(cudaEventRecord(c->ev[0], s));
     CU(cudaGraphLaunch(h.exec, s));
     CU(cudaEventRecord(c->ev[1], s));
@@ -1022,7 +1108,7 @@ idb_status cluster_impl(idb_context *c, const idb_input *in, const idb_params *p
             host_plan_drop_graph(c);   // the data outgrew the plan: eager, then capture anew
         }
     }
-    TRY(stage_inputs_and_survey(pl, in, host_io));
+    TRY(stage_inputs_and_survey(pl, in, host_io, prm->row_chunks));
     TRY(derive_plan(pl, prm));
     TRY(alloc_fixed(pl));
     Buffers &B = pl.B;
@@ -1190,8 +1276,8 @@ idb_status idb_context_create(int device, idb_context **out) {
     c->device = device;
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CU(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-    CU(cudaEventCreateWithFlags(&c->ev_v, cudaEventDisableTiming));
-    CU(cudaEventCreateWithFlags(&c->ev_j, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&c->ev_seq, cudaEventDisableTiming));
+    for (auto &e : c->ev_chunk) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CU(cudaMallocHost(&c->h_ctr, sizeof(Counters)));
     for (auto &e : c->ev) CU(cudaEventCreate(&e));
     *out = c;
@@ -1210,8 +1296,9 @@ idb_status idb_context_destroy(idb_context *c) {
         if (e) cudaEventDestroy(e);
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
     if (c->mlp_bf16) cudaFree(c->mlp_bf16);
-    if (c->ev_v) cudaEventDestroy(c->ev_v);
-    if (c->ev_j) cudaEventDestroy(c->ev_j);
+    if (c->ev_seq) cudaEventDestroy(c->ev_seq);
+    for (auto e : c->ev_chunk)
+        if (e) cudaEventDestroy(e);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c == t_default_ctx) t_default_ctx = nullptr;
@@ -1385,16 +1472,10 @@ idb_status idb_diag_gene_bits(idb_context *c, const char *calls, const int64_t *
     B.vgenes = ptr<uint8_t>(c, bVGenes); B.vg_off = ptr<int32_t>(c, bVGOff);
     B.vtab = ptr<GeneEntry>(c, bVTab);
     B.vbits = ptr<uint64_t>(c, bVBits);
-    const uint64_t tcap = next_pow2(std::max<uint64_t>(2ull * n_rows, 1024));
-    TRY(ensure(c, bTable, 4 * tcap));
-    TRY(ensure(c, bSlot, 4 * (size_t)n_rows));
-    TRY(ensure(c, bRepRow, 4 * (size_t)n_rows));
-    TRY(ensure(c, bCallAux, 16));
-    B.table = ptr<uint32_t>(c, bTable);
-    B.slot = ptr<uint32_t>(c, bSlot);
-    B.rep_row = ptr<uint32_t>(c, bRepRow);
-    set_call_scratch(B, tcap, ptr<uint32_t>(c, bCallAux));
-    launch_gene_bits(P, B, true, c->stream);
+    TRY(alloc_call_scratch(c, B, n_rows));
+    set_row_chunks(P, false, 1);
+    launch_call_init(P, B, true, c->stream);
+    launch_gene_bits(P, B, true, 0, c->stream);
     TRY(check_launch());
     CU(cudaMemcpyAsync(words_out, B.vbits, sizeof(uint64_t) * n_rows * P.VW, cudaMemcpyDeviceToHost,
                        c->stream));
@@ -1614,9 +1695,7 @@ idb_status idb_autotune(idb_context *c, const idb_input *in, const idb_params *p
     Buffers &B = pl.B;
     cudaStream_t s = c->stream;
     // front and buckets once (independent of the unit shape)
-    launch_gene_bits(P, B, true, s);
-    launch_gene_bits(P, B, false, s);
-    launch_dedupe(P, B, s);
+    TRY(launch_front(pl, s));
     launch_uniques(P, B, s);
     launch_buckets(P, B, s);
     TRY(read_counters(pl));
@@ -1628,9 +1707,10 @@ idb_status idb_autotune(idb_context *c, const idb_input *in, const idb_params *p
     if (!P.fast) {
         cand = {{1, 64}, {1, 256}, {1, 1024}};
     } else if (P.hamming) {
-        const int rxs[2] = {4, 8};
+        const int rxs[3] = {2, 4, 8};
         for (int rx : rxs) {
-            if (rx == 8 && P.W != 1) continue;
+            if (rx != 4 && P.W != 1) continue;
+            if (rx == 2 && !P.join) continue;
             for (int ty : {128, 256, 512, 1024})
                 if (ty >= 32 * rx) cand.push_back({rx, ty});
         }

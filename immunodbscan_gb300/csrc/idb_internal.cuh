@@ -16,6 +16,7 @@ constexpr int kGenericMaxLen = 1024;    // Levenshtein on the generic path
 constexpr int kDepthMax = 50;           // tree-depth histogram cap (cuda/PSDBSCAN.hcu:1029)
 constexpr uint32_t kEdgeChunk = 256;    // edge slots reserved per warp at a time
 constexpr uint32_t kSpinCap = 1u << 22; // bound of every device-side retry loop
+constexpr int kMaxRowChunks = 8;        // host columns uploaded in at most this many row chunks
 // Bin pairs with at most kSmallSide entries on each side (Hamming fast path) are
 // evaluated pair-parallel: lanes take pairs, records travel by shuffles.
 constexpr uint32_t kSmallSide = 32;
@@ -207,10 +208,24 @@ struct Plan {
     bool streamed = false;                        // neighbour pairs not stored: the
                                                   // distance work runs twice
     uint64_t edge_budget = 0;                     // bytes for the edge list (0: no limit)
+    // row chunks of the front end: host columns arrive chunk by chunk and the
+    // gene-bitset and duplicate kernels of chunk k wait only for its rows
+    uint32_t nchunks = 1;
+    uint32_t chunk_row[kMaxRowChunks + 1] = {};   // [nchunks+1] row boundaries
     uint8_t codemap[256];
     int first_byte = -1;                          // byte value with code 0
     // capacities
     uint64_t cap_entries = 0, cap_binpairs = 0, cap_units = 0, cap_edges = 0;
+};
+
+// Scratch of the call-string collapse of one gene column.
+struct CallScratch {
+    unsigned long long *tab = nullptr;              // [mask+1] (hash hi 32 | row)
+    uint32_t mask = 0;
+    uint32_t *ref = nullptr;                        // [N] slot of the row's string or kNone
+    uint32_t *todo = nullptr;                       // [N] rows that compute their own bitset;
+                                                    // row chunk k lists its rows from chunk_row[k]
+    uint32_t *ntodo = nullptr;                      // [kMaxRowChunks] list lengths per chunk
 };
 
 // Device buffers of one call (all carved from the context arena).
@@ -233,13 +248,8 @@ struct Buffers {
     // duplicate table
     uint32_t *table = nullptr, *tcount = nullptr;
     uint64_t table_mask = 0;
-    // call-string collapse of a gene column (scratch, used before the duplicate
-    // table: call_tab aliases table, call_ref slot, call_todo rep_row)
-    unsigned long long *call_tab = nullptr;         // [call_mask+1] (hash hi 32 | row)
-    uint32_t call_mask = 0;
-    uint32_t *call_ref = nullptr;                   // [N] slot of the row's string or kNone
-    uint32_t *call_todo = nullptr;                  // [N] rows that compute their own bitset
-    uint32_t *call_ntodo = nullptr;                 // [1]
+    // call-string collapse, one per gene column (V, J)
+    CallScratch call[2];
     // uniques [N]
     uint32_t *urow = nullptr, *ucopies = nullptr, *ulen = nullptr, *urep = nullptr;
     // bins
@@ -289,8 +299,14 @@ struct Buffers {
 void launch_survey(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_check_plan(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_stamp(unsigned long long *dst, cudaStream_t s);
-void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream_t s);
-void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s);
+// The front end runs by row chunks [chunk_row[k], chunk_row[k+1]): the two
+// init launchers once, then per chunk launch_gene_bits (V, then J) and
+// launch_dedupe_rows, then launch_dedupe_final over all rows.
+void launch_call_init(const Plan &P, const Buffers &B, bool v_column, cudaStream_t s);
+void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, uint32_t chunk, cudaStream_t s);
+void launch_dedupe_init(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_dedupe_rows(const Plan &P, const Buffers &B, uint32_t chunk, cudaStream_t s);
+void launch_dedupe_final(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s);

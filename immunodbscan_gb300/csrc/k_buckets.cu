@@ -567,7 +567,8 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
               const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
               const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
               const uint8_t *__restrict__ codemap, const int16_t *__restrict__ eps_tab,
-              JSlot *tab, uint32_t *__restrict__ islot, uint32_t smax, uint64_t cap_mask) {
+              JSlot *tab, uint32_t *__restrict__ islot, uint32_t *__restrict__ irank, uint32_t smax,
+              uint64_t cap_mask) {
     __shared__ uint8_t cm[256];
     for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
     __syncthreads();
@@ -604,10 +605,16 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
             // the entry that created a key is its head: head index u*smax + k
             islot[(size_t)u * 4 + k] = sl == kNone ? kNone : (sl | (won ? kHeadBit : 0u));
             if (won) tab[sl].head = u * smax + k;
-            // one count increment per key among the lanes here together
+            // one count increment per key among the lanes here together; the
+            // count before it ranks the entry within its key's group (its
+            // place in the group's entries, k_join_fill)
             const uint32_t am = __activemask();
             const uint32_t grp = __match_any_sync(am, sl);
-            if (lane == (uint32_t)__ffs(grp) - 1 && sl != kNone) atomicAdd(&tab[sl].cnt, (uint32_t)__popc(grp));
+            const int leader = __ffs(grp) - 1;
+            uint32_t base = 0;
+            if (lane == (uint32_t)leader && sl != kNone) base = atomicAdd(&tab[sl].cnt, (uint32_t)__popc(grp));
+            base = __shfl_sync(am, base, leader);
+            if (k < S) irank[(size_t)u * smax + k] = base + (uint32_t)__popc(grp & ((1u << lane) - 1u));
         }
     }
 }
@@ -647,8 +654,9 @@ k_join_sizes(Counters *ctr, const uint32_t *__restrict__ islot, const JSlot *__r
     }
 }
 
-// Entries: each unique once per segment whose key forms a group; the side
-// record carries the segment index and the unique id.
+// Entries: each unique once per segment whose key forms a group, at the
+// group's start plus the entry's rank from the insert; the side record carries
+// the segment index and the unique id.
 template <int RSC>
 __global__ void __launch_bounds__(256)
 k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restrict__ urow,
@@ -656,9 +664,8 @@ k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restr
             const int64_t *__restrict__ seq_off, const uint8_t *__restrict__ codemap,
             const int16_t *__restrict__ eps_tab, const uint32_t *__restrict__ islot,
             const uint64_t *__restrict__ vbits, const uint64_t *__restrict__ jbits,
-            const JSlot *__restrict__ tab,
-            const uint32_t *__restrict__ start, uint32_t *__restrict__ cursor,
-            uint32_t *__restrict__ ent_uid, uint4 *__restrict__ ent_rec,
+            const JSlot *__restrict__ tab, const uint32_t *__restrict__ start,
+            const uint32_t *__restrict__ irank, uint32_t smax, uint4 *__restrict__ ent_rec,
             uint4 *__restrict__ ent_meta, int planes, uint32_t W, uint64_t cap_entries,
             uint32_t *err) {
     __shared__ uint8_t cm[256];
@@ -680,10 +687,10 @@ k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restr
             const uint2 ch = *reinterpret_cast<const uint2 *>(&tab[sl].cnt);   // cnt, head
             if (ch.x < 2) continue;
             const uint32_t h = ch.y;
-            const uint64_t pos = (uint64_t)start[h] + atomicAdd(&cursor[h], 1u);
+            const uint64_t pos = (uint64_t)start[h] + irank[(size_t)u * smax + k];
             if (pos >= cap_entries) { atomicOr(err, kErrEntryOverflow); continue; }
-            ent_uid[pos] = u;
-            // side record: V bits, J bits with the segment index in the top two bits
+            // side record (its unique id is the entry's: the join's distance
+            // kernel reads no separate id array): V bits, J bits with the segment index in the top two bits
             const uint64_t vb = vbits[(size_t)row * g.VW];
             const uint32_t jb = (uint32_t)jbits[(size_t)row * g.JW];
             ent_meta[pos] = make_uint4((uint32_t)vb, (uint32_t)(vb >> 32), jb | (k << 30), u);
@@ -744,7 +751,7 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
         cudaMemsetAsync(&B.ctr->n_heads, 0, 2 * sizeof(uint32_t), s);   // n_heads, n_groups
         k_join_insert<<<grid_wave(k_join_insert, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
                                                           B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
-                                                          B.jn_islot,
+                                                          B.jn_islot, B.jn_cur,
                                                           P.join_smax, B.jn_mask);
         k_join_sizes<<<grid_wave(k_join_sizes, heads, kThreads), kThreads, 0, s>>>(
             B.ctr, B.jn_islot, B.jn_tab, P.join_smax, B.jn_start, B.jn_bpidx);
@@ -771,12 +778,11 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
 void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
     if (P.join) {
         BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
-        cudaMemsetAsync(B.jn_cur, 0, sizeof(uint32_t) * (size_t)P.join_smax * P.N, s);
         const int planes = (int)P.B;
         auto go = [&](auto kern) {
             kern<<<grid_wave(kern, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.seq, B.seq_off,
                                                      B.codemap, B.eps_tab, B.jn_islot, B.vbits,
-                                                     B.jbits, B.jn_tab, B.jn_start, B.jn_cur, B.ent_uid,
+                                                     B.jbits, B.jn_tab, B.jn_start, B.jn_cur, P.join_smax,
                                                      B.ent_rec, B.ent_meta, planes, P.W,
                                                      P.cap_entries, &B.ctr->error);
         };

@@ -838,7 +838,7 @@ __device__ __forceinline__ void hamming_unit_y(const DistArgs &a, EdgeWriter &ew
 // EM: 0 = popcount test, 1 = eps == 1 (d & (d-1)) == 0, 2 = eps == 0.
 // ---------------------------------------------------------------------------
 template <int BP, int W, int RX, int EM, bool JN>
-__global__ void __launch_bounds__(kWarps * 32, (W == 1 && RX <= 4 ? 5 : 4))
+__global__ void __launch_bounds__(kWarps * 32, (W == 1 && RX <= 2 ? 6 : (W == 1 && RX <= 4 ? 5 : 4)))
 k_hamming(DistArgs a) {
     constexpr int NW = BP * W;                 // words per record used
     constexpr int R16 = (NW + 3) / 4;          // 16-byte words per record
@@ -1312,14 +1312,22 @@ void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s, 
         const int RX = (int)P.RX;
         if (P.B <= 2) {
             switch (P.W) {
-                case 1: if (RX == 4) run_hamming<2, 1, 4>(P, a, grid, s); else run_hamming<2, 1, 8>(P, a, grid, s); break;
+                case 1:
+                    if (RX == 2 && P.join) run_hamming_jn<2, 1, 2, true>(P, a, grid, s);
+                    else if (RX == 8) run_hamming<2, 1, 8>(P, a, grid, s);
+                    else run_hamming<2, 1, 4>(P, a, grid, s);
+                    break;
                 case 2: run_hamming<2, 2, 4>(P, a, grid, s); break;
                 case 3: run_hamming<2, 3, 4>(P, a, grid, s); break;
                 default: run_hamming<2, 4, 4>(P, a, grid, s); break;
             }
         } else {
             switch (P.W) {
-                case 1: if (RX == 4) run_hamming<5, 1, 4>(P, a, grid, s); else run_hamming<5, 1, 8>(P, a, grid, s); break;
+                case 1:
+                    if (RX == 2 && P.join) run_hamming_jn<5, 1, 2, true>(P, a, grid, s);
+                    else if (RX == 8) run_hamming<5, 1, 8>(P, a, grid, s);
+                    else run_hamming<5, 1, 4>(P, a, grid, s);
+                    break;
                 case 2: run_hamming<5, 2, 4>(P, a, grid, s); break;
                 case 3: run_hamming<5, 3, 4>(P, a, grid, s); break;
                 default: run_hamming<5, 4, 4>(P, a, grid, s); break;

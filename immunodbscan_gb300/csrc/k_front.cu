@@ -144,7 +144,10 @@ __global__ void k_const_strings(uint8_t *blob, int64_t *off, uint32_t N) {
 //   k_call_copy   copies each representative's bitset to the rows that share
 //                 its string.
 // A bitset is a function of the string alone, so the result does not depend
-// on which row wins a slot.
+// on which row wins a slot.  The three kernels run per row chunk (host columns
+// arrive chunk by chunk): a chunk's rows find the slots of earlier chunks'
+// strings, and each chunk lists the rows that compute their own bitset in its
+// own part of the todo array.
 //
 // k_gene_bits: a warp takes up to 32 queued rows, gathers their call bytes into
 // its shared-memory slice, collects the bytes that start some gene name into a
@@ -504,8 +507,8 @@ __device__ __forceinline__ unsigned long long call_hash(const uint32_t *words, u
 // kNone when the row computes its own bitset (it won the slot, or found none);
 // those rows are appended to todo.
 __global__ void __launch_bounds__(kGbWarps * 32)
-k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, uint32_t N,
-             unsigned long long *tab, uint32_t tmask, uint32_t *__restrict__ ref,
+k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off, uint32_t r0,
+             uint32_t r1, unsigned long long *tab, uint32_t tmask, uint32_t *__restrict__ ref,
              uint32_t *__restrict__ todo, uint32_t *n_todo) {
     extern __shared__ __align__(16) uint8_t sm[];
     // rows that compute their own bitset, gathered per warp and appended to
@@ -524,11 +527,11 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
     };
     const GbSlice w = cs_slice(sm, wid);
     const uint8_t *wb = w.bytes();
-    const uint32_t nchunks = (N + kGbRows - 1) / kGbRows;
+    const uint32_t nwin = (r1 - r0 + kGbRows - 1) / kGbRows;
     const uint32_t gwarp = blockIdx.x * kGbWarps + wid, nwarps = gridDim.x * kGbWarps;
-    for (uint32_t ch = gwarp; ch < nchunks; ch += nwarps) {
-        const uint32_t end = min(ch * kGbRows + kGbRows, N);
-        uint32_t r = ch * kGbRows;
+    for (uint32_t ch = gwarp; ch < nwin; ch += nwarps) {
+        const uint32_t end = min(r0 + ch * kGbRows + kGbRows, r1);
+        uint32_t r = r0 + ch * kGbRows;
         while (r < end) {
             uint32_t my_row = 0;
             const uint32_t nr = gb_stage(calls, off, nullptr, r, end, lane, w, &my_row);
@@ -606,11 +609,11 @@ k_call_slots(const uint8_t *__restrict__ calls, const int64_t *__restrict__ off,
 }
 
 // Rows that share a representative's string take its bitset.
-__global__ void k_call_copy(uint32_t N, const uint32_t *__restrict__ ref,
+__global__ void k_call_copy(uint32_t r0, uint32_t r1, uint32_t N, const uint32_t *__restrict__ ref,
                             const unsigned long long *__restrict__ tab, uint32_t tmask, uint32_t GW,
                             uint64_t *__restrict__ bits) {
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    for (uint32_t i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += stride) {
         const uint32_t s = ref[i];
         if (s > tmask) continue;                 // kNone: the row has its own bitset
         const uint32_t src = (uint32_t)tab[s];
@@ -636,7 +639,7 @@ struct DedupArgs {
     const uint8_t *seq; const int64_t *off;
     const uint64_t *vbits, *jbits; uint32_t VW, JW;
     const uint32_t *rep_off; uint32_t R;
-    uint32_t N;
+    uint32_t r0, r1;      // the rows inserted by this launch
     uint2 *dtab;          // slot: {row of the class, ~(class size)}; all ones when empty
     uint32_t *slot;
     uint64_t mask;
@@ -669,7 +672,7 @@ __global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
     __syncthreads();
     const uint32_t *rep_off = rep_smem ? s_rep : a.rep_off;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += stride) {
+    for (uint32_t i = a.r0 + blockIdx.x * blockDim.x + threadIdx.x; i < a.r1; i += stride) {
         const uint32_t r = rep_of_row(rep_off, a.R, i);
         const int64_t o = a.off[i];
         const uint32_t L = (uint32_t)(a.off[i + 1] - o);
@@ -944,13 +947,24 @@ void launch_const_strings(uint8_t *blob, int64_t *off, uint32_t N, cudaStream_t 
     k_const_strings<<<grid_for((uint64_t)N + 1), kThreads, 0, s>>>(blob, off, N);
 }
 
-void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream_t s) {
-    const bool absent = v_column ? P.no_v : P.no_j;
-    uint64_t *bits = v_column ? B.vbits : B.jbits;
-    if (absent) {
+void launch_call_init(const Plan &P, const Buffers &B, bool v_column, cudaStream_t s) {
+    if (v_column ? P.no_v : P.no_j) {
+        uint64_t *bits = v_column ? B.vbits : B.jbits;
         k_gene_bits_const<<<grid_for(P.N), kThreads, 0, s>>>(P.N, bits);
         return;
     }
+    const CallScratch &cs = B.call[v_column ? 0 : 1];
+    cudaMemsetAsync(cs.tab, 0xFF, sizeof(unsigned long long) * ((size_t)cs.mask + 1), s);
+    cudaMemsetAsync(cs.ntodo, 0, sizeof(uint32_t) * kMaxRowChunks, s);
+}
+
+void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, uint32_t chunk, cudaStream_t s) {
+    if (v_column ? P.no_v : P.no_j) return;   // constant bitsets, set by launch_call_init
+    const uint32_t r0 = P.chunk_row[chunk], r1 = P.chunk_row[chunk + 1];
+    if (r1 <= r0) return;
+    const uint32_t nrows = r1 - r0;
+    uint64_t *bits = v_column ? B.vbits : B.jbits;
+    const CallScratch &cs = B.call[v_column ? 0 : 1];
     const uint32_t G = v_column ? P.Gv : P.Gj;
     const uint32_t GW = v_column ? P.VW : P.JW;
     const uint8_t *calls = v_column ? B.vcall : B.jcall;
@@ -960,15 +974,14 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     const GeneEntry *tab = v_column ? B.vtab : B.jtab;
     const GeneMatcher &gm = v_column ? P.vmatch : P.jmatch;
     const uint32_t name_bytes = v_column ? P.gene_bytes_v : P.gene_bytes_j;
-    // 1. collapse the column by string
+    uint32_t *todo = cs.todo + r0, *ntodo = cs.ntodo + chunk;
+    // 1. collapse the chunk's calls by string
     const size_t smem_slots = kGbWarps * ((cs_slice_bytes() + 15) / 16 * 16);
     static_assert(kGbWarps * ((cs_slice_bytes() + 15) / 16 * 16) <= 48 * 1024, "default smem limit");
-    const int grid_rows = grid_wave(k_call_slots, ((uint64_t)P.N + kGbRows - 1) / kGbRows * 32,
+    const int grid_rows = grid_wave(k_call_slots, ((uint64_t)nrows + kGbRows - 1) / kGbRows * 32,
                                     kGbWarps * 32, smem_slots);
-    cudaMemsetAsync(B.call_tab, 0xFF, sizeof(unsigned long long) * ((size_t)B.call_mask + 1), s);
-    cudaMemsetAsync(B.call_ntodo, 0, sizeof(uint32_t), s);
     k_call_slots<<<grid_rows > 0 ? grid_rows : 1, kGbWarps * 32, smem_slots, s>>>(
-        calls, off, P.N, B.call_tab, B.call_mask, B.call_ref, B.call_todo, B.call_ntodo);
+        calls, off, r0, r1, cs.tab, cs.mask, cs.ref, todo, ntodo);
     // 2. bitsets of the representatives
     const size_t smem = gene_bits_smem(G, GW, gm.ts, name_bytes);
     static thread_local size_t attr_set = 0;
@@ -978,25 +991,36 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, cudaStream
     }
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gene_bits, kGbWarps * 32, smem);
-    const uint64_t want = ((uint64_t)P.N + kGbRows * kGbWarps - 1) / (kGbRows * kGbWarps);
+    const uint64_t want = ((uint64_t)nrows + kGbRows * kGbWarps - 1) / (kGbRows * kGbWarps);
     const int grid = (int)std::min<uint64_t>(want, (uint64_t)sm_count() * (per_sm > 0 ? per_sm : 1));
     k_gene_bits<<<grid > 0 ? grid : 1, kGbWarps * 32, smem, s>>>(
-        calls, off, B.call_todo, B.call_ntodo, P.N, genes, goff, G, GW, tab, gm, bits);
-    // 3. everybody else
-    k_call_copy<<<grid_wave(k_call_copy, P.N, kThreads), kThreads, 0, s>>>(P.N, B.call_ref, B.call_tab, B.call_mask, GW,
-                                                    bits);
+        calls, off, todo, ntodo, nrows, genes, goff, G, GW, tab, gm, bits);
+    // 3. everybody else (a representative is a row of this chunk or of an earlier one)
+    k_call_copy<<<grid_wave(k_call_copy, nrows, kThreads), kThreads, 0, s>>>(
+        r0, r1, P.N, cs.ref, cs.tab, cs.mask, GW, bits);
 }
 
-void launch_dedupe(const Plan &P, const Buffers &B, cudaStream_t s) {
+void launch_dedupe_init(const Plan &P, const Buffers &B, cudaStream_t s) {
+    cudaMemsetAsync(B.table, 0xFF, sizeof(uint2) * (B.table_mask + 1), s);
+}
+
+// Rows of one chunk into the duplicate table: their gene bitsets are complete,
+// and so are those of every row already in the table (earlier chunks).
+void launch_dedupe_rows(const Plan &P, const Buffers &B, uint32_t chunk, cudaStream_t s) {
+    const uint32_t r0 = P.chunk_row[chunk], r1 = P.chunk_row[chunk + 1];
+    if (r1 <= r0) return;
     DedupArgs a;
     a.seq = B.seq; a.off = B.seq_off;
     a.vbits = B.vbits; a.jbits = B.jbits; a.VW = P.VW; a.JW = P.JW;
-    a.rep_off = B.rep_off; a.R = P.R; a.N = P.N;
+    a.rep_off = B.rep_off; a.R = P.R; a.r0 = r0; a.r1 = r1;
     a.dtab = reinterpret_cast<uint2 *>(B.table); a.slot = B.slot;
     a.mask = B.table_mask; a.ctr = B.ctr;
-    cudaMemsetAsync(B.table, 0xFF, sizeof(uint2) * (B.table_mask + 1), s);
-    k_dedupe_insert<<<grid_wave(k_dedupe_insert, P.N, kThreads), kThreads, 0, s>>>(a);
-    k_dedupe_final<<<grid_wave(k_dedupe_final, P.N, kThreads), kThreads, 0, s>>>(P.N, B.slot, reinterpret_cast<const uint2 *>(B.table), B.rep_row, B.flag);
+    k_dedupe_insert<<<grid_wave(k_dedupe_insert, r1 - r0, kThreads), kThreads, 0, s>>>(a);
+}
+
+void launch_dedupe_final(const Plan &P, const Buffers &B, cudaStream_t s) {
+    k_dedupe_final<<<grid_wave(k_dedupe_final, P.N, kThreads), kThreads, 0, s>>>(
+        P.N, B.slot, reinterpret_cast<const uint2 *>(B.table), B.rep_row, B.flag);
 }
 
 void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s) {

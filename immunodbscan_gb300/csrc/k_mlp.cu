@@ -91,50 +91,61 @@ __global__ void k_mlp_select(Counters *ctr, const BinPair *__restrict__ bp,
     }
 }
 
-// BF16 forward pass of one sample (weights in shared memory): inputs and
-// hidden activations rounded to BF16, products accumulated in FP32.  Returns
-// the predicted log2 cycles.
-__device__ __forceinline__ float mlp_forward_bf16(const __nv_bfloat16 *w, const float (&f)[kIn]) {
-    __nv_bfloat16 x[kIn];
+// BF16 forward pass of one sample by one warp (weights in shared memory):
+// inputs and hidden activations rounded to BF16, products accumulated in FP32.
+// Lane j computes hidden units j and j+32 of both layers (each a dot product
+// in ascending input order, starting from the bias); the output layer sums the
+// second layer in ascending unit order.  Every lane returns the predicted log2
+// cycles.  A warp per sample keeps the 5k multiply-adds of a sample spread
+// over 32 lanes instead of one long chain.
+__device__ __forceinline__ float mlp_forward_bf16_warp(const __nv_bfloat16 *w, const float (&f)[kIn],
+                                                       float *s_h2, int lane) {
+    const int j0 = lane, j1 = lane + 32;
+    float a0 = __bfloat162float(w[kOffB1 + j0]), a1 = __bfloat162float(w[kOffB1 + j1]);
 #pragma unroll
-    for (int k = 0; k < kIn; ++k) x[k] = __float2bfloat16(f[k]);
-    // fully unrolled so the activations stay in registers
-    float h1[kH];
-#pragma unroll
-    for (int j = 0; j < kH; ++j) {
-        float acc = __bfloat162float(w[kOffB1 + j]);
-#pragma unroll
-        for (int k = 0; k < kIn; ++k)
-            acc = fmaf(__bfloat162float(x[k]), __bfloat162float(w[kOffW1 + k * kH + j]), acc);
-        h1[j] = __bfloat162float(__float2bfloat16(fmaxf(acc, 0.0f)));
+    for (int k = 0; k < kIn; ++k) {
+        const float x = __bfloat162float(__float2bfloat16(f[k]));
+        a0 = fmaf(x, __bfloat162float(w[kOffW1 + k * kH + j0]), a0);
+        a1 = fmaf(x, __bfloat162float(w[kOffW1 + k * kH + j1]), a1);
     }
+    const float h1a = __bfloat162float(__float2bfloat16(fmaxf(a0, 0.0f)));
+    const float h1b = __bfloat162float(__float2bfloat16(fmaxf(a1, 0.0f)));
+    float c0 = __bfloat162float(w[kOffB2 + j0]), c1 = __bfloat162float(w[kOffB2 + j1]);
+#pragma unroll 8
+    for (int k = 0; k < kH; ++k) {
+        const float hk = __shfl_sync(0xFFFFFFFFu, k < 32 ? h1a : h1b, k & 31);
+        c0 = fmaf(hk, __bfloat162float(w[kOffW2 + k * kH + j0]), c0);
+        c1 = fmaf(hk, __bfloat162float(w[kOffW2 + k * kH + j1]), c1);
+    }
+    s_h2[j0] = __bfloat162float(__float2bfloat16(fmaxf(c0, 0.0f)));
+    s_h2[j1] = __bfloat162float(__float2bfloat16(fmaxf(c1, 0.0f)));
+    __syncwarp();
     float y = __bfloat162float(w[kOffB3]);
-    for (int j = 0; j < kH; ++j) {
-        float acc = __bfloat162float(w[kOffB2 + j]);
-#pragma unroll
-        for (int k = 0; k < kH; ++k)
-            acc = fmaf(h1[k], __bfloat162float(w[kOffW2 + k * kH + j]), acc);
-        const float h2 = __bfloat162float(__float2bfloat16(fmaxf(acc, 0.0f)));
-        y = fmaf(h2, __bfloat162float(w[kOffW3 + j]), y);
-    }
+    for (int j = 0; j < kH; ++j) y = fmaf(s_h2[j], __bfloat162float(w[kOffW3 + j]), y);
+    __syncwarp();
     return y;
 }
 
-// BF16 inference over the listed bin pairs: pred[i] = 2^mlp(features)
+// BF16 inference over the listed bin pairs, a warp per bin pair:
+// pred[i] = 2^mlp(features)
 __global__ void __launch_bounds__(kThreads)
 k_mlp_predict_bf16(const Counters *__restrict__ ctr, const BinPair *__restrict__ bp,
                    const uint32_t *__restrict__ heavy, const __nv_bfloat16 *__restrict__ wq,
                    float *__restrict__ pred) {
     __shared__ __nv_bfloat16 w[kMlpParams];
+    __shared__ float s_h2[kThreads / 32][kH];
+    const uint32_t n = ctr->n_heavy;
+    const uint32_t warps = gridDim.x * (kThreads / 32);
+    if (blockIdx.x * (kThreads / 32) >= n) return;   // no sample for this block
     for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) w[k] = wq[k];
     __syncthreads();
-    const uint32_t n = ctr->n_heavy;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t k0 = blockIdx.x * blockDim.x + threadIdx.x; k0 < n; k0 += stride) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (uint32_t k0 = blockIdx.x * (kThreads / 32) + wid; k0 < n; k0 += warps) {
         const uint32_t i = heavy[k0];
         float f[kIn];
         binpair_features(bp[i], f);
-        pred[i] = exp2f(fminf(mlp_forward_bf16(w, f), 60.0f));
+        const float y = mlp_forward_bf16_warp(w, f, s_h2[wid], lane);
+        if (lane == 0) pred[i] = exp2f(fminf(y, 60.0f));
     }
 }
 
@@ -144,14 +155,17 @@ __global__ void __launch_bounds__(kThreads)
 k_mlp_forward_rows(const float *__restrict__ X, uint32_t n, const __nv_bfloat16 *__restrict__ wq,
                    float *__restrict__ y) {
     __shared__ __nv_bfloat16 w[kMlpParams];
+    __shared__ float s_h2[kThreads / 32][kH];
     for (int k = threadIdx.x; k < kMlpParams; k += blockDim.x) w[k] = wq[k];
     __syncthreads();
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t warps = gridDim.x * (kThreads / 32);
+    for (uint32_t i = blockIdx.x * (kThreads / 32) + wid; i < n; i += warps) {
         float f[kIn];
 #pragma unroll
         for (int k = 0; k < kIn; ++k) f[k] = X[(size_t)i * kIn + k];
-        y[i] = mlp_forward_bf16(w, f);
+        const float v = mlp_forward_bf16_warp(w, f, s_h2[wid], lane);
+        if (lane == 0) y[i] = v;
     }
 }
 
@@ -300,7 +314,9 @@ void launch_mlp_predict(const Buffers &B, uint32_t cap, const void *wq_bf16, cud
     cudaMemsetAsync(&B.ctr->n_heavy, 0, sizeof(uint32_t), s);
     const int gsel = (int)std::min<uint64_t>((cap + 255) / 256, (uint64_t)sm_count() * 8);
     k_mlp_select<<<gsel > 0 ? gsel : 1, 256, 0, s>>>(B.ctr, B.bp, B.pred, B.bp_small);
-    const int grid = (int)std::min<uint64_t>((cap + kThreads - 1) / kThreads, (uint64_t)sm_count() * 2);
+    constexpr uint32_t kWarpsPerBlock = kThreads / 32;   // a warp per listed bin pair
+    const int grid = (int)std::min<uint64_t>((cap + kWarpsPerBlock - 1) / kWarpsPerBlock,
+                                             (uint64_t)sm_count() * 8);
     k_mlp_predict_bf16<<<grid > 0 ? grid : 1, kThreads, 0, s>>>(
         B.ctr, B.bp, B.bp_small, static_cast<const __nv_bfloat16 *>(wq_bf16), B.pred);
 }
@@ -325,7 +341,8 @@ void launch_adam(float *p, const float *grad, float *m, float *v, float lr, int 
 
 void launch_mlp_forward_rows(const float *X, uint32_t n, const void *wq_bf16, float *y,
                              cudaStream_t s) {
-    const int grid = (int)std::min<uint64_t>((n + kThreads - 1) / kThreads, (uint64_t)sm_count() * 2);
+    const int grid = (int)std::min<uint64_t>((n + kThreads / 32 - 1) / (kThreads / 32),
+                                             (uint64_t)sm_count() * 8);
     k_mlp_forward_rows<<<grid > 0 ? grid : 1, kThreads, 0, s>>>(
         X, n, static_cast<const __nv_bfloat16 *>(wq_bf16), y);
 }

@@ -74,7 +74,7 @@ class Context:
 
 def make_params(threshold=float("nan"), abs_eps=-1, min_pts=2, use_hamming=False,
                 eval_trees=False, schedule=0, tune=None, candidates=0,
-                edge_memory_mb=0) -> Params:
+                edge_memory_mb=0, row_chunks=0) -> Params:
     p = Params()
     p.threshold = float(threshold) if threshold is not None else math.nan
     p.abs_eps = int(abs_eps)
@@ -87,6 +87,7 @@ def make_params(threshold=float("nan"), abs_eps=-1, min_pts=2, use_hamming=False
         p.tile_ty = int(tune[1])
     p.candidates = int(candidates)
     p.edge_memory_mb = int(edge_memory_mb)
+    p.row_chunks = int(row_chunks)
     return p
 
 
@@ -118,7 +119,7 @@ class Interlink:
                  j_genes_reference, threshold: float, min_pts: int, use_only_hamming: bool,
                  eval_trees: bool = False, *, abs_eps: int = -1, rep_sizes=None,
                  context: Optional[Context] = None, schedule: int = 0, tune=None,
-                 candidates: int = 0, edge_memory_mb: int = 0):
+                 candidates: int = 0, edge_memory_mb: int = 0, row_chunks: int = 0):
         n = int(n_entries)
         keep = []
         inp = Input()
@@ -153,7 +154,7 @@ class Interlink:
             inp.n_repertoires = len(rep_sizes)
             inp.rep_offsets = _p(roff)
         prm = make_params(threshold, abs_eps, min_pts, use_only_hamming, eval_trees, schedule, tune,
-                          candidates, edge_memory_mb)
+                          candidates, edge_memory_mb, row_chunks)
         self._result = _run(inp, prm, n, context, eval_trees)
 
     # getters of cuda/Interlink.hpp:59-63
@@ -200,7 +201,8 @@ def cluster_workload(w, context: Optional[Context] = None, *, schedule: int = 0,
                    w.threshold, w.min_pts, w.use_hamming, eval_trees, abs_eps=w.abs_eps,
                    rep_sizes=np.diff(w.rep_off).tolist() if w.n_rep > 1 else None,
                    context=context, schedule=schedule, tune=tune,
-                   candidates=w.candidates, edge_memory_mb=w.edge_memory_mb)
+                   candidates=w.candidates, edge_memory_mb=w.edge_memory_mb,
+                   row_chunks=w.row_chunks)
     return it.result
 
 

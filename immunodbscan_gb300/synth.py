@@ -54,6 +54,7 @@ class Workload:
     seed: int = 0
     candidates: int = 0           # 0 = automatic candidate pairs, 1 = buckets only
     edge_memory_mb: int = 0       # neighbour-pair list memory (0 no limit, < 0 streamed)
+    row_chunks: int = 0           # host columns copied in this many row chunks (0 automatic)
 
     @property
     def n(self) -> int:

@@ -69,7 +69,12 @@ typedef struct idb_params {
                                   distance work runs twice (counts, then unions
                                   and border minima) and no pair is stored.  Same
                                   answer either way.                              */
-    int32_t  reserved[2];
+    int32_t  row_chunks;       /* idb_cluster (host columns): number of row chunks
+                                  the columns are copied and pre-processed in, so
+                                  that copies overlap the gene-bitset and
+                                  duplicate work; 0 = automatic (8 from 2^20
+                                  rows, else 1), 1..8 = that many.  Same answer. */
+    int32_t  reserved[1];
 } idb_params;
 
 /* Input rows (cuda/Interlink.hpp:54-57: zip(V calls, J calls, sequences)). */
