@@ -466,7 +466,8 @@ def main():
                        "traffic": (profiled_traffic("k_hamming", w.name)
                                    if w.use_hamming and args.scale == 1.0 else None),
                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one "
-                                         "full-size launch (profiles/)",
+                                         "launch at scale 0.2, scaled by the rows to full size "
+                                         "(profiles/k_hamming_workload2_scale0.2.md)",
                        "kernel": "k_hamming" if w.use_hamming else "k_levenshtein",
                        "ops_per_unit": ops_pair,
                        "work_unit": "pair" if w.use_hamming else "pair-column (text residue)",
@@ -476,11 +477,16 @@ def main():
                                         if w.use_hamming and last.pairs_evaluated else None),
                        "peak_source": "measured: idb_diag_int_peak (lop3/add chains, all SMs)"}
 
-    # graph / union-find / border / renumber phases against HBM bandwidth: the
-    # algorithmic bytes 8(n_u+1) CSR offsets + 4 n_u counts + 8 E adjacency + 8 E_cc
-    # parent loads + n_u core flags + 12 n_u parent init/compress + 8 N labels
+    # graph / union-find / border / renumber phases against HBM bandwidth.  The
+    # algorithmic bytes, kernel by kernel: init (copies read, count / parent /
+    # border-minimum written: 16 n_u); count pass (edge 8 B, both ends' copies
+    # 8 B, both ends' count updates 8 B: 24 E); core flags (8 n_u); union pass
+    # (edge 8 B, both ends' core flags 8 B: 16 E, and both ends' parents for a
+    # core-core edge: 8 E_cc); compress (12 n_u); scan of the root flags
+    # (8 n_u); labels (core, parent, border minimum, rank, repertoire, first
+    # unique read, label written: 28 n_u).  Border-minimum updates are left out.
     n_u, E, E_cc = int(last.n_uniques), int(last.neighbour_pairs), int(last.core_edges)
-    graph_bytes = 8 * (n_u + 1) + 4 * n_u + 8 * E + 8 * E_cc + n_u + 12 * n_u + 8 * n
+    graph_bytes = 40 * E + 8 * E_cc + 72 * n_u
     graph_ms = float(np.mean([p[3] for p in r["phases"]]))
     hbm_peak = measured_hbm_peak()
     out["roofline_graph"] = {"bound": "hbm", "achieved": graph_bytes / (graph_ms * 1e-3) / 1e9,
