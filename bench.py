@@ -76,6 +76,8 @@ def parse():
                          "rows: batched and plain device time, identical partitions)")
     ap.add_argument("--no-parity", action="store_true",
                     help="skip the check of every row against the oracle's indexed mode")
+    ap.add_argument("--row-chunks", type=int, default=0,
+                    help="e2e: row chunks the host columns are copied in (0 automatic)")
     return ap.parse_args()
 
 
@@ -511,7 +513,7 @@ def main():
     if not args.no_e2e:
         hin, hkeep = build_host_input(w, pinned=True)
         prm = make_params(w.threshold, w.abs_eps, w.min_pts, w.use_hamming, False, int(learn), shape,
-                          w.candidates)
+                          w.candidates, row_chunks=args.row_chunks)
         clone = torch.empty(n, dtype=torch.int32).pin_memory()
         core = torch.empty(n, dtype=torch.int32).pin_memory()
         copies = torch.empty(n, dtype=torch.int32).pin_memory()
@@ -523,12 +525,13 @@ def main():
         for _ in range(max(3, args.warmup)):
             _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
         barrier(world)
-        times, dev_ms = [], []
+        times, dev_ms, dev_phases = [], [], []
         for _ in range(args.steps):
             t0 = time.perf_counter()
             _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
             times.append(time.perf_counter() - t0)
             dev_ms.append(est.ms_total)
+            dev_phases.append([est.ms_phase[k] for k in range(5)])
         barrier(world)
         e2e_s = allreduce_max(world, float(np.mean(times)))
         h2d = sum(int(a.numel() * a.element_size()) for a in hkeep if isinstance(a, torch.Tensor))
@@ -546,7 +549,11 @@ def main():
                       "breakdown_ms": {"upload_alone": up_ms, "device_span": float(np.mean(dev_ms)),
                                        "download_alone": down_ms,
                                        "batched_device_step": step_ms,
-                                       "serial_sum": up_ms + step_ms + down_ms}}
+                                       "serial_sum": up_ms + step_ms + down_ms,
+                                       "device_span_phases": dict(zip(
+                                           ["front_dedupe (with the copies)", "buckets_schedule",
+                                            "distance", "graph", "outputs"],
+                                           np.mean(dev_phases, axis=0).tolist()))}}
         diff = ((clone.numpy().view(np.uint32) != clone_b) | (core.numpy() != core_b) |
                 (copies.numpy().view(np.uint32) != copies_b))
         out["e2e"]["identical_partitions_vs_batched"] = bool(not diff.any())

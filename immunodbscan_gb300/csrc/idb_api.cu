@@ -733,8 +733,12 @@ idb_status alloc_edges(Pipeline &pl, uint64_t cap) {
     idb_context *c = pl.c;
     cap = std::max<uint64_t>(cap, 4096);
     if (cap > 0xFFFFFFF0ull) return fail(IDB_ERR_UNSUPPORTED, "more than 2^32 neighbour pairs");
-    pl.P.cap_edges = cap;
     TRY(ensure(c, bEdges, sizeof(uint2) * cap, true));
+    // a list kept from an earlier call may hold more pairs: use all of it (up to
+    // the edge-memory budget), so that a call whose pairs fit it sweeps once
+    uint64_t held = std::min<uint64_t>(c->buf[bEdges].cap / sizeof(uint2), 0xFFFFFFF0ull);
+    if (pl.P.edge_budget) held = std::min<uint64_t>(held, pl.P.edge_budget / sizeof(uint2));
+    pl.P.cap_edges = std::max(cap, held);
     pl.B.edges = ptr<uint2>(c, bEdges);
     return IDB_OK;
 }
