@@ -345,8 +345,12 @@ void phase_times(const Counters &h, idb_stats *st) {
 // Row chunks of the front end.  Host columns of 2^20 rows or more are copied
 // and pre-processed in kMaxRowChunks chunks (or `want`, 1..kMaxRowChunks), so
 // that the gene-bitset and duplicate kernels of a chunk run while the next
-// chunks are being copied; device-resident columns are one chunk.  Inner
-// boundaries are multiples of 32 rows.
+// chunks are being copied; device-resident columns are one chunk.  Chunk i of
+// k holds (k - i) / (k (k + 1) / 2) of the rows: the first chunks are the
+// largest and the last one, whose front end runs after the last copy, is the
+// smallest.  (A chunk's front end takes less time than its copy, so every
+// earlier chunk is done before the next one has arrived.)  Inner boundaries
+// are multiples of 32 rows.
 void set_row_chunks(Plan &P, bool host_inputs, int want) {
     uint32_t k = 1;
     if (host_inputs) {
@@ -355,8 +359,12 @@ void set_row_chunks(Plan &P, bool host_inputs, int want) {
     }
     P.nchunks = k;
     P.chunk_row[0] = 0;
-    for (uint32_t i = 1; i < k; ++i)
-        P.chunk_row[i] = (uint32_t)(((uint64_t)P.N * i / k) & ~31ull);
+    const uint64_t total = (uint64_t)k * (k + 1) / 2;
+    uint64_t acc = 0;
+    for (uint32_t i = 1; i < k; ++i) {
+        acc += k - (i - 1);
+        P.chunk_row[i] = (uint32_t)(((uint64_t)P.N * acc / total) & ~31ull);
+    }
     P.chunk_row[k] = P.N;
 }
 
@@ -662,16 +670,16 @@ idb_status alloc_fixed(Pipeline &pl) {
         const uint64_t jcap = next_pow2(std::max<uint64_t>(2 * heads, 1024));
         TRY(ensure(c, bJnTab, sizeof(JSlot) * jcap));
         TRY(ensure(c, bJnISlot, 16 * N1));
-        TRY(ensure(c, bJnStart, 4 * (heads + 1)));
-        TRY(ensure(c, bJnCur, 4 * (heads + 1)));
-        TRY(ensure(c, bJnBpIdx, 4 * (heads + 1)));
+        TRY(ensure(c, bJnStart, 4 * (jcap + 1)));   // group sizes -> starts, per table slot
+        TRY(ensure(c, bJnCur, 4 * (heads + 1)));    // rank of each (unique, segment) in its group
+        TRY(ensure(c, bJnBpIdx, 4 * (jcap + 1)));
         B.jn_tab = ptr<JSlot>(c, bJnTab);
         B.jn_mask = jcap - 1;
         B.jn_islot = ptr<uint32_t>(c, bJnISlot);
         B.jn_start = ptr<uint32_t>(c, bJnStart);
         B.jn_cur = ptr<uint32_t>(c, bJnCur);
         B.jn_bpidx = ptr<uint32_t>(c, bJnBpIdx);
-        scan_n = std::max<uint64_t>(scan_n, heads + 1);
+        scan_n = std::max<uint64_t>(scan_n, jcap + 1);
     }
     B.scan_part_cap = scan_part_needed(std::max<uint64_t>(scan_n, 1u << 20));
     TRY(ensure(c, bScanPart, 4 * (size_t)B.scan_part_cap));

@@ -124,13 +124,13 @@ __device__ __forceinline__ void load_chunk32(const uint8_t *p, uint32_t L, uint3
     }
 }
 
-// One slot of the segment-join table: the segment key, how many (unique,
-// segment) entries hold it, and its head index.  16 bytes: a probe and the
-// updates that follow it touch one sector.
+// One slot of the segment-join table: the segment key and how many (unique,
+// segment) entries hold it.  Padded to 16 bytes, so that a slot never straddles
+// a sector: a probe and the updates that follow it touch one sector.
 struct __align__(16) JSlot {
     unsigned long long key;
     uint32_t cnt;
-    uint32_t head;
+    uint32_t pad;
 };
 
 // Device-resident counters of one clustering call (one struct, zeroed first).
@@ -157,7 +157,8 @@ struct Counters {
     uint32_t small_cursor;       // their work queue head
     uint32_t n_heavy;            // bin pairs the learned predictor evaluates
     uint32_t n_core_edges;       // neighbour pairs with both ends core
-    uint32_t n_heads;            // segment join: distinct segment keys
+    uint32_t n_jslots;           // segment join: table slots in use (the probed prefix)
+    uint32_t n_jslots1;          // n_jslots + 1: the scan of group sizes ends with their total
     uint32_t n_groups;           // segment join: keys held by two or more uniques
     uint32_t n_tiny;             // tiny bin pairs (one lane each), listed from the small list's end
     uint32_t tiny_cursor;        // their work queue head
@@ -268,8 +269,9 @@ struct Buffers {
     JSlot *jn_tab = nullptr;                        // [jn_mask+1] segment-join table
     uint64_t jn_mask = 0;
     uint32_t *jn_islot = nullptr;                   // [4*N] slot of (unique, segment)
-    uint32_t *jn_start = nullptr;                   // [join_smax*N+1] group sizes -> starts
-    uint32_t *jn_cur = nullptr, *jn_bpidx = nullptr;   // [join_smax*N]
+    uint32_t *jn_start = nullptr;                   // [jn_mask+2] group size -> start, per table slot
+    uint32_t *jn_bpidx = nullptr;                   // [jn_mask+2] bin pair of a slot's group
+    uint32_t *jn_cur = nullptr;                     // [join_smax*N] rank of (unique, segment) in its group
     uint32_t *cls_hist = nullptr;                   // [65]
     float *pred = nullptr;                          // learned cost per bin pair
     // graph

@@ -553,9 +553,13 @@ __device__ __forceinline__ uint32_t join_mask(uint32_t nu, uint32_t smax, uint64
     return (uint32_t)min(c - 1, cap_mask);
 }
 
-__global__ void k_join_clear(const Counters *__restrict__ ctr, uint32_t smax, uint64_t cap_mask,
+__global__ void k_join_clear(Counters *ctr, uint32_t smax, uint64_t cap_mask,
                              JSlot *__restrict__ tab) {
     const uint32_t n = join_mask(ctr->n_uniques, smax, cap_mask) + 1u;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        ctr->n_jslots = n;
+        ctr->n_jslots1 = n + 1;
+    }
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
         *reinterpret_cast<uint4 *>(&tab[i]) = make_uint4(~0u, ~0u, 0u, 0u);   // one 16-byte store
@@ -602,9 +606,7 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
                     sl = (sl + 1) & (uint32_t)mask;
                 }
             }
-            // the entry that created a key is its head: head index u*smax + k
             islot[(size_t)u * 4 + k] = sl == kNone ? kNone : (sl | (won ? kHeadBit : 0u));
-            if (won) tab[sl].head = u * smax + k;
             // one count increment per key among the lanes here together; the
             // count before it ranks the entry within its key's group (its
             // place in the group's entries, k_join_fill)
@@ -619,27 +621,24 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
     }
 }
 
-// Size of every key's group (0 for a key held by one unique, and for head
-// indices u*smax + k whose entry did not create its key), and the bin-pair
-// index of the keys that form groups (one counter atomic per block and pass).
+// Size of every key's group, per table slot (0 for an empty slot and for a
+// key held by one unique), and the bin-pair index of the slots that hold
+// groups (one counter atomic per block and pass).  A sequential pass over the
+// probed prefix of the table.
 __global__ void __launch_bounds__(256)
-k_join_sizes(Counters *ctr, const uint32_t *__restrict__ islot, const JSlot *__restrict__ tab,
-             uint32_t smax, uint32_t *__restrict__ sizes, uint32_t *__restrict__ bpidx) {
+k_join_sizes(Counters *ctr, const JSlot *__restrict__ tab, uint32_t *__restrict__ sizes,
+             uint32_t *__restrict__ bpidx) {
     __shared__ uint32_t s_w[8];
     __shared__ uint32_t s_base;
-    const uint32_t nh = ctr->n_uniques * smax;
-    if (blockIdx.x == 0 && threadIdx.x == 0) ctr->n_heads = nh;
+    const uint32_t ns = ctr->n_jslots;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t h0 = blockIdx.x * blockDim.x; h0 < nh; h0 += stride) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) sizes[ns] = 0u;   // the scan's end: the total
+    for (uint32_t h0 = blockIdx.x * blockDim.x; h0 < ns; h0 += stride) {
         const uint32_t h = h0 + threadIdx.x;
-        uint32_t c = 0;
-        if (h < nh) {
-            const uint32_t e = islot[(size_t)(h / smax) * 4 + h % smax];
-            if (e != kNone && (e & kHeadBit)) c = tab[e & ~kHeadBit].cnt;
-        }
+        const uint32_t c = h < ns ? tab[h].cnt : 0u;   // an empty slot counts 0
         const bool grp = c >= 2;
-        if (h < nh) sizes[h] = grp ? c : 0u;
+        if (h < ns) sizes[h] = grp ? c : 0u;
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, grp);
         if (lane == 0) s_w[wid] = (uint32_t)__popc(m);
         __syncthreads();
@@ -684,10 +683,9 @@ k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restr
             const uint32_t e = islot[(size_t)u * 4 + k];
             if (e == kNone) continue;
             const uint32_t sl = e & ~kHeadBit;
-            const uint2 ch = *reinterpret_cast<const uint2 *>(&tab[sl].cnt);   // cnt, head
-            if (ch.x < 2) continue;
-            const uint32_t h = ch.y;
-            const uint64_t pos = (uint64_t)start[h] + irank[(size_t)u * smax + k];
+            const uint32_t s0 = start[sl];
+            if (start[sl + 1] - s0 < 2) continue;              // a key of one unique: no group
+            const uint64_t pos = (uint64_t)s0 + irank[(size_t)u * smax + k];
             if (pos >= cap_entries) { atomicOr(err, kErrEntryOverflow); continue; }
             // side record (its unique id is the entry's: the join's distance
             // kernel reads no separate id array): V bits, J bits with the segment index in the top two bits
@@ -706,27 +704,24 @@ __global__ void k_join_nbp(Counters *ctr) {
     if (threadIdx.x == 0 && blockIdx.x == 0) ctr->n_binpairs = ctr->n_groups;
 }
 
-// One bin pair (a group against itself) per key held by two or more uniques.
+// One bin pair (a group against itself) per key held by two or more uniques:
+// a sequential pass over the probed prefix of the table.
 __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
-                               const uint32_t *__restrict__ islot, uint32_t smax,
                                const JSlot *__restrict__ tab, const uint32_t *__restrict__ start,
-                               const uint32_t *__restrict__ bpidx, const int16_t *__restrict__ eps_tab, uint32_t TX, uint64_t cap_bp,
-                               BinPair *__restrict__ out, uint32_t *err) {
-    const uint32_t nh = ctr->n_heads;
+                               const uint32_t *__restrict__ bpidx, const int16_t *__restrict__ eps_tab,
+                               uint32_t TX, uint64_t cap_bp, BinPair *__restrict__ out, uint32_t *err) {
+    const uint32_t ns = ctr->n_jslots;
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < nh; h += stride) {
-        const uint32_t e = islot[(size_t)(h / smax) * 4 + h % smax];
-        if (e == kNone || !(e & kHeadBit)) continue;
-        const uint32_t sl = e & ~kHeadBit;
-        const uint32_t c = tab[sl].cnt;
+    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < ns; h += stride) {
+        const uint32_t s0 = start[h], c = start[h + 1] - s0;
         if (c < 2) continue;
         const uint32_t k = bpidx[h];
         if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); continue; }
-        const unsigned long long key = tab[sl].key;
+        const unsigned long long key = tab[h].key;
         const uint32_t L = (uint32_t)(key >> 32) & 0xFFu;
         const uint32_t li = L - g.Lmin;
         BinPair P;
-        P.a_start = start[h]; P.a_n = c; P.b_start = start[h]; P.b_n = c;
+        P.a_start = s0; P.a_n = c; P.b_start = s0; P.b_n = c;
         P.unit_base = 0;
         P.ncx = (c + TX - 1) / TX;
         P.la = (uint16_t)L; P.lb = (uint16_t)L;
@@ -745,17 +740,17 @@ __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
 void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
     BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
     if (P.join) {
-        const uint64_t heads = (uint64_t)P.join_smax * P.N;
-        k_join_clear<<<grid_wave(k_join_clear, B.jn_mask + 1, kThreads), kThreads, 0, s>>>(
+        const uint64_t slots = B.jn_mask + 1;   // the allocation; the probed prefix is on the device
+        cudaMemsetAsync(&B.ctr->n_jslots, 0, 2 * sizeof(uint32_t), s);   // n_jslots, n_groups
+        k_join_clear<<<grid_wave(k_join_clear, slots, kThreads), kThreads, 0, s>>>(
             B.ctr, P.join_smax, B.jn_mask, B.jn_tab);
-        cudaMemsetAsync(&B.ctr->n_heads, 0, 2 * sizeof(uint32_t), s);   // n_heads, n_groups
         k_join_insert<<<grid_wave(k_join_insert, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
                                                           B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
                                                           B.jn_islot, B.jn_cur,
                                                           P.join_smax, B.jn_mask);
-        k_join_sizes<<<grid_wave(k_join_sizes, heads, kThreads), kThreads, 0, s>>>(
-            B.ctr, B.jn_islot, B.jn_tab, P.join_smax, B.jn_start, B.jn_bpidx);
-        scan_u32(B.jn_start, B.jn_start, (uint32_t)heads, &B.ctr->n_heads, &B.ctr->n_entries,
+        k_join_sizes<<<grid_wave(k_join_sizes, slots, kThreads), kThreads, 0, s>>>(
+            B.ctr, B.jn_tab, B.jn_start, B.jn_bpidx);
+        scan_u32(B.jn_start, B.jn_start, (uint32_t)slots + 1, &B.ctr->n_jslots1, &B.ctr->n_entries,
                  B.scan_part, B.scan_part_cap, s);
         return;
     }
@@ -838,10 +833,9 @@ void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s) {
 void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
     if (P.join) {
         BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
-        const uint64_t heads = (uint64_t)P.join_smax * P.N;
-        k_join_bp_fill<<<grid_wave(k_join_bp_fill, heads, kThreads), kThreads, 0, s>>>(
-            g, B.ctr, B.jn_islot, P.join_smax, B.jn_tab, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX,
-            P.cap_binpairs, B.bp, &B.ctr->error);
+        k_join_bp_fill<<<grid_wave(k_join_bp_fill, B.jn_mask + 1, kThreads), kThreads, 0, s>>>(
+            g, B.ctr, B.jn_tab, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX, P.cap_binpairs, B.bp,
+            &B.ctr->error);
         return;
     }
     PairGeom pg{P.NL, P.Lmin, P.Gv, P.Gj, P.K, P.dLmax, P.hamming, P.TX, P.TY, P.TY / P.TX};
