@@ -72,8 +72,9 @@ typedef struct idb_params {
     int32_t  row_chunks;       /* idb_cluster (host columns): number of row chunks
                                   the columns are copied and pre-processed in, so
                                   that copies overlap the gene-bitset and
-                                  duplicate work; 0 = automatic (8 from 2^20
-                                  rows, else 1), 1..8 = that many.  Same answer. */
+                                  duplicate work (chunk i of k holds (k-i) parts
+                                  of k(k+1)/2); 0 = automatic (8 from 2^20 rows,
+                                  else 1), 1..8 = that many.  Same answer.       */
     int32_t  reserved[1];
 } idb_params;
 
