@@ -82,6 +82,7 @@ struct idb_context {
     cudaStream_t copy_stream = nullptr;   // host->device copies of the columns
     cudaEvent_t ev_seq = nullptr;         // sequence column copied
     cudaEvent_t ev_chunk[kMaxRowChunks] = {};   // call columns of row chunk k copied
+    cudaEvent_t ev_out[2] = {};           // replays: row copies / core flags written
     DevBuf buf[bNumBufs];
     Counters *h_ctr = nullptr;        // pinned mirror of the counters
     cudaEvent_t ev[16] = {};
@@ -115,6 +116,7 @@ struct idb_context {
         std::vector<uint32_t> roff;
         idb_params prm{};
         bool no_v = false, no_j = false, no_seq = false, uniques = false, model = false;
+        bool early_out = false;   // the graph records ev_out (row copies, row core flags)
         std::vector<char> vgenes, jgenes;
         std::vector<int64_t> vgoff, jgoff;
         Plan P;
@@ -322,6 +324,10 @@ struct Pipeline {
     cudaEvent_t wait_seq = nullptr;
     cudaEvent_t wait_chunk[kMaxRowChunks] = {};
     bool external_waits = false;
+    // a captured call writes the row copies after the uniques and the row core
+    // flags after the core marking, each followed by an event record node, so
+    // that a replay copies them to the host while the rest of the path runs
+    bool early_out = false;
     bool copies_issued = false;
     bool allow_join = true;   // the segment join finds neighbours, not all admissible pairs
     // every return path (errors included) leaves no copy from the caller's host
@@ -799,6 +805,10 @@ idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false
     if (!eager) launch_check_plan(P, B, s);
     TRY(launch_front(pl, s));
     launch_uniques(P, B, s);
+    if (pl.early_out) {
+        launch_outputs(P, B, s, kOutCopies);
+        CU(cudaEventRecordWithFlags(c->ev_out[0], s, cudaEventRecordExternal));
+    }
     TRY(check_launch());
     record(pl, 1);
     launch_buckets(P, B, s);
@@ -863,10 +873,10 @@ idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false
         launch_streamed_labels(P, B, pl.trees, s);
     } else {
         record(pl, 3);
-        launch_graph(P, B, pl.trees, s);
+        launch_graph(P, B, pl.trees, s, pl.early_out ? c->ev_out[1] : nullptr);
     }
     record(pl, 4);
-    launch_outputs(P, B, s);
+    launch_outputs(P, B, s, pl.early_out ? kOutClone : kOutAll);
     TRY(check_launch());
     record(pl, 5);
     return IDB_OK;
@@ -1014,6 +1024,7 @@ idb_status host_plan_capture(Pipeline &pl) {
     // launched: the graph waits on their events (external event-wait nodes)
     pl.external_waits = true;
     for (uint32_t k = 0; k < kMaxRowChunks; ++k) pl.wait_chunk[k] = k < pl.P.nchunks ? c->ev_chunk[k] : nullptr;
+    pl.early_out = !pl.P.streamed;
     CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     cudaMemsetAsync(pl.B.ctr, 0, sizeof(Counters), s);
     cudaMemsetAsync(&pl.B.ctr->lmin, 0xFF, sizeof(uint32_t), s);
@@ -1034,6 +1045,7 @@ idb_status host_plan_capture(Pipeline &pl) {
     h.P = pl.P;
     h.B = pl.B;
     h.model = c->has_model;
+    h.early_out = pl.early_out;
     h.generation = c->generation;
     h.epoch = c->stage_epoch;
     return IDB_OK;
@@ -1063,11 +1075,23 @@ idb_status host_plan_run(idb_context *c, const idb_input *in, idb_output *out) {
     CU(cudaGraphLaunch(h.exec, s));
     CU(cudaEventRecord(c->ev[1], s));
     const Buffers &B = h.B;
+    if (h.early_out) {
+        // the launch records ev_out[0] once the row copies are written and
+        // ev_out[1] once the row core flags are: their copies to the host run
+        // on the copy stream while the graph goes on
+        CU(cudaStreamWaitEvent(cs, c->ev_out[0], 0));
+        CU(cudaMemcpyAsync(out->copies, B.copies, 4 * N, cudaMemcpyDeviceToHost, cs));
+        CU(cudaStreamWaitEvent(cs, c->ev_out[1], 0));
+        CU(cudaMemcpyAsync(out->core, B.core, 4 * N, cudaMemcpyDeviceToHost, cs));
+    }
     CU(cudaMemcpyAsync(c->h_ctr, B.ctr, sizeof(Counters), cudaMemcpyDeviceToHost, s));
     CU(cudaMemcpyAsync(out->clone_id, B.clone_id, 4 * N, cudaMemcpyDeviceToHost, s));
-    CU(cudaMemcpyAsync(out->core, B.core, 4 * N, cudaMemcpyDeviceToHost, s));
-    CU(cudaMemcpyAsync(out->copies, B.copies, 4 * N, cudaMemcpyDeviceToHost, s));
+    if (!h.early_out) {
+        CU(cudaMemcpyAsync(out->core, B.core, 4 * N, cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(out->copies, B.copies, 4 * N, cudaMemcpyDeviceToHost, s));
+    }
     CU(cudaStreamSynchronize(s));
+    CU(cudaStreamSynchronize(cs));
     TRY(device_errors(*c->h_ctr));
     const Counters &hc = *c->h_ctr;
     if (out->uniques) CU(cudaMemcpy(out->uniques, B.uniques, 4 * (size_t)hc.n_uniques, cudaMemcpyDeviceToHost));
@@ -1289,6 +1313,7 @@ idb_status idb_context_create(int device, idb_context **out) {
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CU(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
     CU(cudaEventCreateWithFlags(&c->ev_seq, cudaEventDisableTiming));
+    for (auto &e : c->ev_out) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto &e : c->ev_chunk) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     CU(cudaMallocHost(&c->h_ctr, sizeof(Counters)));
     for (auto &e : c->ev) CU(cudaEventCreate(&e));
@@ -1309,6 +1334,8 @@ idb_status idb_context_destroy(idb_context *c) {
     if (c->h_ctr) cudaFreeHost(c->h_ctr);
     if (c->mlp_bf16) cudaFree(c->mlp_bf16);
     if (c->ev_seq) cudaEventDestroy(c->ev_seq);
+    for (auto e : c->ev_out)
+        if (e) cudaEventDestroy(e);
     for (auto e : c->ev_chunk)
         if (e) cudaEventDestroy(e);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);

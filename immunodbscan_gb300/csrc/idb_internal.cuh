@@ -316,12 +316,17 @@ void launch_schedule(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s,
                      uint32_t sink = kSinkEdges);
 void launch_count_admissible(const Plan &P, const Buffers &B, cudaStream_t s);
-void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s);
+// core_out: when set, the row core flags are written right after the core
+// marking and the event is recorded there (an external record node in a
+// captured graph), so their copy to the host can start before the labels.
+void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s,
+                  cudaEvent_t core_out = nullptr);
 // streamed mode: both distance sweeps (counts, core flags, unions and border
 // minima), then depths, compression and labels
 void launch_streamed_sweeps(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_streamed_labels(const Plan &P, const Buffers &B, bool trees, cudaStream_t s);
-void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s);
+constexpr uint32_t kOutClone = 1, kOutCore = 2, kOutCopies = 4, kOutAll = 7;
+void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s, uint32_t what = kOutAll);
 
 // exclusive scan of n (host) or *n_dev (device, capacity n) uint32 values;
 // out may alias in; *total (device) receives the sum when non-null.

@@ -197,22 +197,27 @@ __global__ void k_labels(const Counters *__restrict__ ctr, const uint32_t *__res
     }
 }
 
+// Row outputs.  `what` selects them (kOutClone / kOutCore / kOutCopies): the
+// copies are final once the uniques exist and the core flags once the counts
+// are, so a call can write (and copy out) those two before the labels.
 __global__ void k_rows_out(uint32_t N, uint32_t min_pts, const uint32_t *__restrict__ row2uid,
                            const uint32_t *__restrict__ urow, const uint32_t *__restrict__ ucopies,
                            const uint32_t *__restrict__ ucore, const uint32_t *__restrict__ ulabel,
                            uint32_t *__restrict__ clone_id, int32_t *__restrict__ core,
-                           uint32_t *__restrict__ copies, Counters *ctr) {
+                           uint32_t *__restrict__ copies, Counters *ctr, uint32_t what) {
     const uint32_t stride = gridDim.x * blockDim.x;
     uint32_t noise = 0;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
         const uint32_t u = row2uid[i];
         const bool rep = urow[u] == i;
-        const uint32_t lab = ulabel[u];
-        clone_id[i] = lab;
-        copies[i] = rep ? ucopies[u] : 0u;
+        if (what & kOutCopies) copies[i] = rep ? ucopies[u] : 0u;
         // a duplicate keeps count 0 and is core only for minPts == 0
-        core[i] = rep ? (int32_t)ucore[u] : (int32_t)(min_pts == 0);
-        noise += lab == 0;
+        if (what & kOutCore) core[i] = rep ? (int32_t)ucore[u] : (int32_t)(min_pts == 0);
+        if (what & kOutClone) {
+            const uint32_t lab = ulabel[u];
+            clone_id[i] = lab;
+            noise += lab == 0;
+        }
     }
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) noise += __shfl_xor_sync(0xFFFFFFFFu, noise, d);
@@ -228,12 +233,16 @@ __global__ void k_uniques_out(const Counters *__restrict__ ctr, const uint32_t *
 
 }  // namespace
 
-void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s) {
+void launch_graph(const Plan &P, const Buffers &B, bool trees, cudaStream_t s, cudaEvent_t core_out) {
     const uint64_t ecap = P.cap_edges;
     const int gu = grid_for(P.N);
     k_graph_init<<<grid_wave(k_graph_init, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ucopies, B.cnt, B.parent, B.bmin);
     k_count<<<grid_wave(k_count, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucopies, B.cnt);
     k_core<<<grid_wave(k_core, P.N, kThreads), kThreads, 0, s>>>(B.ctr, B.ctr, B.cnt, P.min_pts, B.ucore);
+    if (core_out) {   // the row core flags now, and an event for their copy
+        launch_outputs(P, B, s, kOutCore);
+        cudaEventRecordWithFlags(core_out, s, cudaEventRecordExternal);
+    }
     // unions of core-core edges; each non-core unique keeps its minimum core neighbour
     k_union<<<grid_wave(k_union, ecap, kThreads), kThreads, 0, s>>>(B.ctr, ecap, B.edges, B.ucore, B.parent, B.bmin);
     if (trees) {
@@ -278,11 +287,11 @@ void launch_streamed_labels(const Plan &P, const Buffers &B, bool trees, cudaStr
                                       B.uid_first, B.cnt);
 }
 
-void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s) {
+void launch_outputs(const Plan &P, const Buffers &B, cudaStream_t s, uint32_t what) {
     const int gu = grid_for(P.N);
     k_rows_out<<<grid_wave(k_rows_out, P.N, kThreads), kThreads, 0, s>>>(P.N, P.min_pts, B.row2uid, B.urow, B.ucopies, B.ucore,
-                                        B.cnt, B.clone_id, B.core, B.copies, B.ctr);
-    if (B.uniques) k_uniques_out<<<gu, kThreads, 0, s>>>(B.ctr, B.urow, B.uniques);
+                                        B.cnt, B.clone_id, B.core, B.copies, B.ctr, what);
+    if (B.uniques && (what & kOutClone)) k_uniques_out<<<gu, kThreads, 0, s>>>(B.ctr, B.urow, B.uniques);
 }
 
 }  // namespace idb
