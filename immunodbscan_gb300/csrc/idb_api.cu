@@ -589,6 +589,9 @@ idb_status derive_plan(Pipeline &pl, const idb_params *prm) {
              P.Gv <= 64 && P.Gj <= 30 && P.R < (1u << 24) - 1 &&
              2ull * (uint64_t)(emax_same + 1) * P.N <= (1ull << 30);
     P.join_smax = P.join ? (uint32_t)std::max(1, emax_same + 1) : 1u;
+    // with row chunks the uniques are numbered and the join's inserts run chunk
+    // by chunk, while later chunks are still being copied
+    P.front_join = P.join && P.nchunks > 1;
     if (P.hamming && P.RX == 2 && !P.join) {   // 2 x-entries per lane: segment join only
         P.RX = 4;
         P.TX = 128;
@@ -778,22 +781,34 @@ idb_status device_errors(const Counters &h) {
 
 // Phases after the survey.  With `eager`, sizes are read back and buffers grown
 // between phases; otherwise (graph capture) the capacities in P are used as-is.
-// Gene bitsets and duplicate collapse, row chunk by row chunk: chunk k's
-// kernels wait for its copies (when they are still in flight) and nothing else.
+// Gene bitsets, duplicate collapse and unique numbering, row chunk by row
+// chunk: chunk k's kernels wait for its copies (when they are still in flight)
+// and nothing else.  With more than one chunk a chunk's representatives and
+// unique ids are final once its rows are in the duplicate table, so they are
+// numbered (and, for the segment join, inserted into the join table) before
+// the next chunk arrives.
 idb_status launch_front(Pipeline &pl, cudaStream_t s) {
     const Plan &P = pl.P;
     const Buffers &B = pl.B;
     launch_call_init(P, B, true, s);
     launch_call_init(P, B, false, s);
     launch_dedupe_init(P, B, s);
+    if (P.front_join) launch_join_init(P, B, s);
     for (uint32_t k = 0; k < P.nchunks; ++k) {
         if (pl.wait_chunk[k])
             CU(cudaStreamWaitEvent(s, pl.wait_chunk[k], pl.external_waits ? cudaEventWaitExternal : 0));
         launch_gene_bits(P, B, true, k, s);
         launch_gene_bits(P, B, false, k, s);
         launch_dedupe_rows(P, B, k, s);
+        if (P.nchunks > 1) launch_uniques_rows(P, B, k, s);
+        if (P.front_join) launch_join_insert(P, B, (int)k, s);
     }
-    launch_dedupe_final(P, B, s);
+    if (P.nchunks > 1) {
+        launch_uniques_finish(P, B, s);
+    } else {
+        launch_dedupe_final(P, B, s);
+        launch_uniques(P, B, s);
+    }
     // a later run of the phases finds the columns in place
     if (!pl.external_waits)
         for (auto &e : pl.wait_chunk) e = nullptr;
@@ -807,7 +822,6 @@ idb_status run_phases(Pipeline &pl, bool eager, bool stop_after_schedule = false
     cudaStream_t s = c->stream;
     if (!eager) launch_check_plan(P, B, s);
     TRY(launch_front(pl, s));
-    launch_uniques(P, B, s);
     if (pl.early_out) {
         launch_outputs(P, B, s, kOutCopies);
         CU(cudaEventRecordWithFlags(c->ev_out[0], s, cudaEventRecordExternal));
@@ -1738,7 +1752,6 @@ idb_status idb_autotune(idb_context *c, const idb_input *in, const idb_params *p
     cudaStream_t s = c->stream;
     // front and buckets once (independent of the unit shape)
     TRY(launch_front(pl, s));
-    launch_uniques(P, B, s);
     launch_buckets(P, B, s);
     TRY(read_counters(pl));
     TRY(alloc_entries(pl, c->h_ctr->n_entries));

@@ -159,6 +159,7 @@ struct Counters {
     uint32_t n_core_edges;       // neighbour pairs with both ends core
     uint32_t n_jslots;           // segment join: table slots in use (the probed prefix)
     uint32_t n_jslots1;          // n_jslots + 1: the scan of group sizes ends with their total
+    uint32_t chunk_uniques[kMaxRowChunks];   // uniques of each row chunk (numbered by chunk)
     uint32_t n_groups;           // segment join: keys held by two or more uniques
     uint32_t n_tiny;             // tiny bin pairs (one lane each), listed from the small list's end
     uint32_t tiny_cursor;        // their work queue head
@@ -213,6 +214,7 @@ struct Plan {
     // gene-bitset and duplicate kernels of chunk k wait only for its rows
     uint32_t nchunks = 1;
     uint32_t chunk_row[kMaxRowChunks + 1] = {};   // [nchunks+1] row boundaries
+    bool front_join = false;                      // segment-join inserts run by row chunk
     uint8_t codemap[256];
     int first_byte = -1;                          // byte value with code 0
     // capacities
@@ -309,8 +311,18 @@ void launch_gene_bits(const Plan &P, const Buffers &B, bool v_column, uint32_t c
 void launch_dedupe_init(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_dedupe_rows(const Plan &P, const Buffers &B, uint32_t chunk, cudaStream_t s);
 void launch_dedupe_final(const Plan &P, const Buffers &B, cudaStream_t s);
+// more than one row chunk: representatives and unique ids chunk by chunk
+// (launch_uniques_rows after the chunk's launch_dedupe_rows), then the unique
+// count and copies (launch_uniques_finish) in place of launch_dedupe_final +
+// launch_uniques
+void launch_uniques_rows(const Plan &P, const Buffers &B, uint32_t chunk, cudaStream_t s);
+void launch_uniques_finish(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s);
+// segment join: clear the table (sized by the rows when front_join), then the
+// inserts of every unique (chunk < 0) or of one row chunk's uniques
+void launch_join_init(const Plan &P, const Buffers &B, cudaStream_t s);
+void launch_join_insert(const Plan &P, const Buffers &B, int chunk, cudaStream_t s);
 void launch_binpairs(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_schedule(const Plan &P, const Buffers &B, cudaStream_t s);
 void launch_distance(const Plan &P, const Buffers &B, int grid, cudaStream_t s,

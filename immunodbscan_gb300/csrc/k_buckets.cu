@@ -553,9 +553,11 @@ __device__ __forceinline__ uint32_t join_mask(uint32_t nu, uint32_t smax, uint64
     return (uint32_t)min(c - 1, cap_mask);
 }
 
+// The probed prefix is sized by the unique count, or by `rows` (an upper
+// bound) when the inserts run by row chunk, before the count is known.
 __global__ void k_join_clear(Counters *ctr, uint32_t smax, uint64_t cap_mask,
-                             JSlot *__restrict__ tab) {
-    const uint32_t n = join_mask(ctr->n_uniques, smax, cap_mask) + 1u;
+                             JSlot *__restrict__ tab, uint32_t rows) {
+    const uint32_t n = join_mask(rows ? rows : ctr->n_uniques, smax, cap_mask) + 1u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctr->n_jslots = n;
         ctr->n_jslots1 = n + 1;
@@ -572,15 +574,21 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
               const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
               const uint8_t *__restrict__ codemap, const int16_t *__restrict__ eps_tab,
               JSlot *tab, uint32_t *__restrict__ islot, uint32_t *__restrict__ irank, uint32_t smax,
-              uint64_t cap_mask) {
+              int chunk) {
     __shared__ uint8_t cm[256];
     for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
     __syncthreads();
-    const uint32_t nu = ctr->n_uniques;
-    const uint32_t mask = join_mask(nu, smax, cap_mask);
+    // every unique, or (chunk >= 0) the uniques of one row chunk
+    uint32_t u0 = 0, u1 = ctr->n_uniques;
+    if (chunk >= 0) {
+        u0 = 0;
+        for (int m = 0; m < chunk; ++m) u0 += ctr->chunk_uniques[m];
+        u1 = u0 + ctr->chunk_uniques[chunk];
+    }
+    const uint32_t mask = ctr->n_jslots - 1u;   // the prefix k_join_clear prepared
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
-    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+    for (uint32_t u = u0 + blockIdx.x * blockDim.x + threadIdx.x; u < u1; u += stride) {
         const uint32_t row = urow[u], L = ulen[u], r = urep[u];
         const uint32_t S = g.in_range(L) ? seg_count(eps_tab, g.NL, L - g.Lmin) : 0u;
         uint32_t wd[5][4];
@@ -737,17 +745,29 @@ __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
 }
 }  // namespace
 
+void launch_join_init(const Plan &P, const Buffers &B, cudaStream_t s) {
+    cudaMemsetAsync(&B.ctr->n_jslots, 0, 2 * sizeof(uint32_t), s);   // n_jslots, n_groups
+    k_join_clear<<<grid_wave(k_join_clear, B.jn_mask + 1, kThreads), kThreads, 0, s>>>(
+        B.ctr, P.join_smax, B.jn_mask, B.jn_tab, P.front_join ? P.N : 0u);
+}
+
+void launch_join_insert(const Plan &P, const Buffers &B, int chunk, cudaStream_t s) {
+    BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
+    const uint32_t rows = chunk < 0 ? P.N : P.chunk_row[chunk + 1] - P.chunk_row[chunk];
+    if (rows == 0) return;
+    k_join_insert<<<grid_wave(k_join_insert, rows, kThreads), kThreads, 0, s>>>(
+        g, B.ctr, B.urow, B.ulen, B.urep, B.seq, B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
+        B.jn_islot, B.jn_cur, P.join_smax, chunk);
+}
+
 void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
     BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
     if (P.join) {
         const uint64_t slots = B.jn_mask + 1;   // the allocation; the probed prefix is on the device
-        cudaMemsetAsync(&B.ctr->n_jslots, 0, 2 * sizeof(uint32_t), s);   // n_jslots, n_groups
-        k_join_clear<<<grid_wave(k_join_clear, slots, kThreads), kThreads, 0, s>>>(
-            B.ctr, P.join_smax, B.jn_mask, B.jn_tab);
-        k_join_insert<<<grid_wave(k_join_insert, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.urep, B.seq,
-                                                          B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
-                                                          B.jn_islot, B.jn_cur,
-                                                          P.join_smax, B.jn_mask);
+        if (!P.front_join) {                    // else the row chunks did these
+            launch_join_init(P, B, s);
+            launch_join_insert(P, B, -1, s);
+        }
         k_join_sizes<<<grid_wave(k_join_sizes, slots, kThreads), kThreads, 0, s>>>(
             B.ctr, B.jn_tab, B.jn_start, B.jn_bpidx);
         scan_u32(B.jn_start, B.jn_start, (uint32_t)slots + 1, &B.ctr->n_jslots1, &B.ctr->n_entries,

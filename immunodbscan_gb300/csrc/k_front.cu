@@ -713,11 +713,14 @@ __global__ void __launch_bounds__(kThreads) k_dedupe_insert(DedupArgs a) {
     }
 }
 
-__global__ void k_dedupe_final(uint32_t N, const uint32_t *__restrict__ slot,
+// Representative and "is a representative" flag of rows [r0, r1).  Final as
+// soon as every row up to r1 is in the table: later rows have larger indices,
+// so they never lower a class's minimum row.
+__global__ void k_dedupe_final(uint32_t r0, uint32_t r1, const uint32_t *__restrict__ slot,
                                const uint2 *__restrict__ dtab, uint32_t *__restrict__ rep_row,
                                uint32_t *__restrict__ flag) {
     const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += stride) {
+    for (uint32_t i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += stride) {
         const uint32_t s = slot[i];
         const uint32_t r = s == kNone ? i : dtab[s].x;
         rep_row[i] = r;
@@ -749,13 +752,75 @@ __global__ void k_uniques(uint32_t N, const int64_t *__restrict__ off,
     }
 }
 
+// First unique of every repertoire (its first row is a representative: a
+// class never leaves its repertoire), and n_uniques at the end.
 __global__ void k_uid_first(uint32_t N, uint32_t R, const uint32_t *__restrict__ rep_off,
-                            const uint32_t *__restrict__ uid_of_row, const Counters *ctr,
+                            const uint32_t *__restrict__ row2uid, const Counters *ctr,
                             uint32_t *__restrict__ uid_first) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r <= R) {
         const uint32_t row = rep_off[r];
-        uid_first[r] = row < N ? uid_of_row[row] : ctr->n_uniques;
+        uid_first[r] = row < N ? row2uid[row] : ctr->n_uniques;
+    }
+}
+
+// Row chunks: the chunk boundaries and the unique count of every chunk before
+// k give chunk k's first unique id.
+struct ChunkRows {
+    uint32_t n;
+    uint32_t row[kMaxRowChunks + 1];
+};
+
+__device__ __forceinline__ uint32_t chunk_uid_base(const Counters *ctr, uint32_t k) {
+    uint32_t b = 0;
+    for (uint32_t m = 0; m < k; ++m) b += ctr->chunk_uniques[m];
+    return b;
+}
+
+// Unique numbering of row chunk k (rows [r0, r1)), once its representatives
+// are final: uid = chunk k's first uid + the rank among the chunk's
+// representatives (uid_of_row, scanned per chunk), so uids ascend with the row
+// as in the one-pass numbering.  A duplicate takes its representative's uid,
+// which may lie in an earlier chunk.  The copies come later (k_uniques_finish):
+// a class may still grow in later chunks.
+__global__ void k_uniques_rows(uint32_t k, ChunkRows cr, const int64_t *__restrict__ off,
+                               const uint32_t *__restrict__ rep_off, uint32_t R,
+                               const uint32_t *__restrict__ rep_row,
+                               const uint32_t *__restrict__ uid_of_row, const Counters *ctr,
+                               uint32_t *__restrict__ urow, uint32_t *__restrict__ ulen,
+                               uint32_t *__restrict__ urep, uint32_t *__restrict__ row2uid) {
+    const uint32_t r0 = cr.row[k], r1 = cr.row[k + 1];
+    const uint32_t base = chunk_uid_base(ctr, k);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t i = r0 + blockIdx.x * blockDim.x + threadIdx.x; i < r1; i += stride) {
+        const uint32_t r = rep_row[i];
+        uint32_t rb = base;
+        if (r < r0) {                       // the representative is in an earlier chunk
+            uint32_t j = 0;
+            while (j + 1 < k && cr.row[j + 1] <= r) ++j;
+            rb = chunk_uid_base(ctr, j);
+        }
+        const uint32_t u = rb + uid_of_row[r];
+        row2uid[i] = u;
+        if (r == i) {
+            urow[u] = i;
+            ulen[u] = (uint32_t)(off[i + 1] - off[i]);
+            urep[u] = rep_of_row(rep_off, R, i);
+        }
+    }
+}
+
+// After the last chunk: the unique count and every unique's copies (its
+// class size, final now).
+__global__ void k_uniques_finish(uint32_t nchunks, Counters *ctr, const uint32_t *__restrict__ urow,
+                                 const uint32_t *__restrict__ slot, const uint2 *__restrict__ dtab,
+                                 uint32_t *__restrict__ ucopies) {
+    const uint32_t nu = chunk_uid_base(ctr, nchunks);
+    if (blockIdx.x == 0 && threadIdx.x == 0) ctr->n_uniques = nu;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < nu; u += stride) {
+        const uint32_t sl = slot[urow[u]];
+        ucopies[u] = sl == kNone ? 1u : ~dtab[sl].y;
     }
 }
 
@@ -1020,7 +1085,7 @@ void launch_dedupe_rows(const Plan &P, const Buffers &B, uint32_t chunk, cudaStr
 
 void launch_dedupe_final(const Plan &P, const Buffers &B, cudaStream_t s) {
     k_dedupe_final<<<grid_wave(k_dedupe_final, P.N, kThreads), kThreads, 0, s>>>(
-        P.N, B.slot, reinterpret_cast<const uint2 *>(B.table), B.rep_row, B.flag);
+        0, P.N, B.slot, reinterpret_cast<const uint2 *>(B.table), B.rep_row, B.flag);
 }
 
 void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s) {
@@ -1030,7 +1095,29 @@ void launch_uniques(const Plan &P, const Buffers &B, cudaStream_t s) {
                                                    reinterpret_cast<const uint2 *>(B.table),
                                                    B.rep_row, B.uid_of_row, B.urow, B.ucopies,
                                                    B.ulen, B.urep, B.row2uid);
-    k_uid_first<<<(P.R + 1 + 255) / 256, 256, 0, s>>>(P.N, P.R, B.rep_off, B.uid_of_row, B.ctr,
+    k_uid_first<<<(P.R + 1 + 255) / 256, 256, 0, s>>>(P.N, P.R, B.rep_off, B.row2uid, B.ctr,
+                                                     B.uid_first);
+}
+
+void launch_uniques_rows(const Plan &P, const Buffers &B, uint32_t chunk, cudaStream_t s) {
+    const uint32_t r0 = P.chunk_row[chunk], r1 = P.chunk_row[chunk + 1];
+    if (r1 <= r0) return;   // its unique count stays 0
+    k_dedupe_final<<<grid_wave(k_dedupe_final, r1 - r0, kThreads), kThreads, 0, s>>>(
+        r0, r1, B.slot, reinterpret_cast<const uint2 *>(B.table), B.rep_row, B.flag);
+    scan_u32(B.flag + r0, B.uid_of_row + r0, r1 - r0, nullptr, &B.ctr->chunk_uniques[chunk],
+             B.scan_part, B.scan_part_cap, s);
+    ChunkRows cr;
+    cr.n = P.nchunks;
+    for (uint32_t k = 0; k <= kMaxRowChunks; ++k) cr.row[k] = k <= P.nchunks ? P.chunk_row[k] : P.N;
+    k_uniques_rows<<<grid_wave(k_uniques_rows, r1 - r0, kThreads), kThreads, 0, s>>>(
+        chunk, cr, B.seq_off, B.rep_off, P.R, B.rep_row, B.uid_of_row, B.ctr, B.urow, B.ulen,
+        B.urep, B.row2uid);
+}
+
+void launch_uniques_finish(const Plan &P, const Buffers &B, cudaStream_t s) {
+    k_uniques_finish<<<grid_wave(k_uniques_finish, P.N, kThreads), kThreads, 0, s>>>(
+        P.nchunks, B.ctr, B.urow, B.slot, reinterpret_cast<const uint2 *>(B.table), B.ucopies);
+    k_uid_first<<<(P.R + 1 + 255) / 256, 256, 0, s>>>(P.N, P.R, B.rep_off, B.row2uid, B.ctr,
                                                      B.uid_first);
 }
 
