@@ -521,8 +521,9 @@ def main():
         o = _lib.Output(clone.data_ptr(), core.data_ptr(), copies.data_ptr(), None, None, None,
                         C.cast(C.pointer(est), C.c_void_p))
         # the first call runs eagerly, the second also captures the shape, the
-        # rest replay it (idb_cluster's plan cache)
-        for _ in range(max(3, args.warmup)):
+        # rest replay it (idb_cluster's plan cache); a few replays before the
+        # timed ones
+        for _ in range(max(6, args.warmup)):
             _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
         barrier(world)
         times, dev_ms, dev_phases = [], [], []
@@ -546,6 +547,8 @@ def main():
                       "api": "idb_cluster (host buffers, %s schedule)" % ("learned" if learn else
                                                                            "static"),
                       "replayed": bool(est.kernel_launches > 0),
+                      "ms_calls": [round(1e3 * t, 3) for t in times],
+                      "ms_median": float(np.median(times)) * 1e3,
                       "breakdown_ms": {"upload_alone": up_ms, "device_span": float(np.mean(dev_ms)),
                                        "download_alone": down_ms,
                                        "batched_device_step": step_ms,

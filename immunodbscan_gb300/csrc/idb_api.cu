@@ -80,6 +80,8 @@ struct idb_context {
     int device = 0;
     cudaStream_t stream = nullptr;
     cudaStream_t copy_stream = nullptr;   // host->device copies of the columns
+    cudaStream_t side_stream = nullptr;   // the J column's call collapse, beside the V column's
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     cudaEvent_t ev_seq = nullptr;         // sequence column copied
     cudaEvent_t ev_chunk[kMaxRowChunks] = {};   // call columns of row chunk k copied
     cudaEvent_t ev_out[2] = {};           // replays: row copies / core flags written
@@ -797,8 +799,19 @@ idb_status launch_front(Pipeline &pl, cudaStream_t s) {
     for (uint32_t k = 0; k < P.nchunks; ++k) {
         if (pl.wait_chunk[k])
             CU(cudaStreamWaitEvent(s, pl.wait_chunk[k], pl.external_waits ? cudaEventWaitExternal : 0));
+        // the two gene columns are independent: J on the side stream, joined
+        // back before the duplicate collapse (parallel branches in a graph)
+        const bool fork = !P.no_v && !P.no_j;
+        if (fork) {
+            CU(cudaEventRecord(pl.c->ev_fork, s));
+            CU(cudaStreamWaitEvent(pl.c->side_stream, pl.c->ev_fork, 0));
+        }
         launch_gene_bits(P, B, true, k, s);
-        launch_gene_bits(P, B, false, k, s);
+        launch_gene_bits(P, B, false, k, fork ? pl.c->side_stream : s);
+        if (fork) {
+            CU(cudaEventRecord(pl.c->ev_join, pl.c->side_stream));
+            CU(cudaStreamWaitEvent(s, pl.c->ev_join, 0));
+        }
         launch_dedupe_rows(P, B, k, s);
         if (P.nchunks > 1) launch_uniques_rows(P, B, k, s);
         if (P.front_join) launch_join_insert(P, B, (int)k, s);
@@ -1058,6 +1071,8 @@ idb_status host_plan_capture(Pipeline &pl) {
     if (ce != cudaSuccess) return fail(IDB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
     h.graph = g;
     CU(cudaGraphInstantiate(&h.exec, g, 0));
+    CU(cudaGraphUpload(h.exec, s));   // device-side setup now, not in the first replay
+    CU(cudaStreamSynchronize(s));
     h.kernels = graph_kernel_count(g);
     h.P = pl.P;
     h.B = pl.B;
@@ -1329,6 +1344,9 @@ idb_status idb_context_create(int device, idb_context **out) {
     c->device = device;
     CU(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     CU(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    CU(cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
+    CU(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    CU(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
     CU(cudaEventCreateWithFlags(&c->ev_seq, cudaEventDisableTiming));
     for (auto &e : c->ev_out) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     for (auto &e : c->ev_chunk) CU(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1356,6 +1374,9 @@ idb_status idb_context_destroy(idb_context *c) {
     for (auto e : c->ev_chunk)
         if (e) cudaEventDestroy(e);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
     if (c->stream) cudaStreamDestroy(c->stream);
     if (c == t_default_ctx) t_default_ctx = nullptr;
     delete c;
@@ -1426,6 +1447,8 @@ idb_status idb_batch_plan(idb_context *c, const idb_input *in, const idb_params 
     if (ce != cudaSuccess) return fail(IDB_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
     c->graph = g;
     CU(cudaGraphInstantiate(&c->exec, g, 0));
+    CU(cudaGraphUpload(c->exec, s));   // device-side setup now, not in the first replay
+    CU(cudaStreamSynchronize(s));
     {
         size_t nn = 0;
         CU(cudaGraphGetNodes(g, nullptr, &nn));

@@ -293,12 +293,24 @@ __device__ uint32_t gb_stage(const uint8_t *__restrict__ calls, const int64_t *_
             }
         }
     } else {
-        uint8_t *dst = reinterpret_cast<uint8_t *>(w.words);
-        for (uint32_t j = 0; j < nr; ++j) {
-            const int64_t sj = __shfl_sync(0xFFFFFFFFu, st, j);
-            const uint32_t lj = __shfl_sync(0xFFFFFFFFu, len, j);
-            const uint32_t oj = __shfl_sync(0xFFFFFFFFu, excl, j);
-            for (uint32_t t = lane; t < lj; t += 32) dst[oj + t] = calls[sj + t];
+        // gather: every lane copies its own row with aligned 4-byte loads (a
+        // word that holds a row byte never leaves that byte's page), so the
+        // loads of all the window's rows are in flight together
+        if ((uint32_t)lane < nr && len) {
+            uint8_t *dst = reinterpret_cast<uint8_t *>(w.words) + excl;
+            const uintptr_t a = reinterpret_cast<uintptr_t>(calls + st);
+            const uint32_t sh = (uint32_t)(a & 3u);
+            const uint32_t *gw = reinterpret_cast<const uint32_t *>(a - sh);
+            const uint32_t nw = (sh + len + 3) >> 2;
+#pragma unroll 4
+            for (uint32_t t = 0; t < nw; ++t) {
+                const uint32_t v = __ldg(gw + t);
+#pragma unroll
+                for (uint32_t b = 0; b < 4; ++b) {
+                    const int q = (int)(4 * t + b) - (int)sh;
+                    if (q >= 0 && (uint32_t)q < len) dst[q] = (uint8_t)(v >> (8 * b));
+                }
+            }
         }
     }
     __syncwarp();
