@@ -66,3 +66,39 @@ def test_automatic_chunks_above_a_million_rows():
             _same(cluster_workload(w, ctx), o, f"call {k}")
         w1 = dataclasses.replace(w, row_chunks=1)
         _same(cluster_workload(w1, ctx), o, "one chunk")
+
+
+def test_chunks_number_uniques_in_row_order():
+    """Unique ids ascend with the representative row whatever the chunking:
+    the uniques output lists the rows with copies > 0 in order, and the
+    row -> unique map agrees with it."""
+    w = synth.workload(2, scale=0.006)
+    with Context(0) as ctx:
+        ref = None
+        for chunks in (1, 3, 8):
+            w.row_chunks = chunks
+            r = cluster_workload(w, ctx)
+            reps = np.nonzero(r.copies > 0)[0]
+            assert r.n_uniques == reps.size, chunks
+            assert np.array_equal(np.asarray(r.uniques[: r.n_uniques]), reps), chunks
+            if ref is None:
+                ref = r
+            _same(r, ref, f"{chunks} chunks against 1")
+
+
+def test_chunks_with_streamed_mode_and_tree_depths():
+    """Row chunks with no neighbour-pair list (streamed mode), and with the
+    tree-depth histogram (its total and bin 0 do not depend on the order of
+    the unions)."""
+    w = synth.workload(2, scale=0.004)
+    o = oracle.cluster(w)
+    with Context(0) as ctx:
+        w.row_chunks, w.edge_memory_mb = 5, -1
+        g = cluster_workload(w, ctx)
+        assert g.stats.streamed == 1
+        _same(g, o, "streamed, 5 chunks")
+        w.edge_memory_mb = 0
+        h1 = cluster_workload(dataclasses.replace(w, row_chunks=1), ctx, eval_trees=True).tree_depth_hist
+        h5 = cluster_workload(w, ctx, eval_trees=True).tree_depth_hist
+        assert int(np.sum(h1)) == int(np.sum(h5)) == w.n
+        assert int(h1[0]) == int(h5[0])
