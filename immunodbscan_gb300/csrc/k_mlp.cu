@@ -38,6 +38,7 @@ namespace {
 
 constexpr int kThreads = 128;
 constexpr uint32_t kLearnMinPairs = 4096;   // smaller bin pairs skip the network
+constexpr float kLightCyclesPerPair = 32.0f;
 
 // Features of one bin pair (also used by the host to build training sets).
 __device__ void binpair_features(const BinPair &P, float *f) {
@@ -73,8 +74,10 @@ __global__ void k_features(const Counters *__restrict__ ctr, const BinPair *__re
     }
 }
 
-// Bin pairs below kLearnMinPairs are cheap whatever their order: they take the
-// lightest class without running the network; the others are listed for it.
+// Bin pairs below kLearnMinPairs skip the network: their cost is their pair
+// count times kLightCyclesPerPair (a middle value of the logged cycles per
+// pair), which keeps them after the heavy ones and in the static order among
+// themselves; the others are listed for the network.
 __global__ void k_mlp_select(Counters *ctr, const BinPair *__restrict__ bp,
                              float *__restrict__ pred, uint32_t *__restrict__ heavy) {
     const uint32_t n = ctr->n_binpairs;
@@ -82,7 +85,7 @@ __global__ void k_mlp_select(Counters *ctr, const BinPair *__restrict__ bp,
     for (uint32_t i0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); i0 < n; i0 += stride) {
         const uint32_t i = i0 + (threadIdx.x & 31);
         const bool big = i < n && bp[i].cost_lo >= kLearnMinPairs;
-        if (i < n && !big) pred[i] = 1.0f;
+        if (i < n && !big) pred[i] = fmaxf(1.0f, (float)bp[i].cost_lo * kLightCyclesPerPair);
         const uint32_t m = __ballot_sync(0xFFFFFFFFu, big);
         uint32_t b0 = 0;
         if ((threadIdx.x & 31) == 0 && m) b0 = atomicAdd(&ctr->n_heavy, (uint32_t)__popc(m));
