@@ -682,12 +682,13 @@ idb_status alloc_fixed(Pipeline &pl) {
         // keys: at most join_smax per unique; the table at load <= 1/2
         const uint64_t heads = (uint64_t)P.join_smax * N;
         const uint64_t jcap = next_pow2(std::max<uint64_t>(2 * heads, 1024));
-        TRY(ensure(c, bJnTab, sizeof(JSlot) * jcap));
+        TRY(ensure(c, bJnTab, (sizeof(unsigned long long) + sizeof(uint32_t)) * jcap));
         TRY(ensure(c, bJnISlot, 16 * N1));
         TRY(ensure(c, bJnStart, 4 * (jcap + 1)));   // group sizes -> starts, per table slot
         TRY(ensure(c, bJnCur, 4 * (heads + 1)));    // rank of each (unique, segment) in its group
         TRY(ensure(c, bJnBpIdx, 4 * (jcap + 1)));
-        B.jn_tab = ptr<JSlot>(c, bJnTab);
+        B.jn_key = ptr<unsigned long long>(c, bJnTab);
+        B.jn_cnt = reinterpret_cast<uint32_t *>(B.jn_key + jcap);
         B.jn_mask = jcap - 1;
         B.jn_islot = ptr<uint32_t>(c, bJnISlot);
         B.jn_start = ptr<uint32_t>(c, bJnStart);

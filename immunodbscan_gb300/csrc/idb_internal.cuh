@@ -124,14 +124,6 @@ __device__ __forceinline__ void load_chunk32(const uint8_t *p, uint32_t L, uint3
     }
 }
 
-// One slot of the segment-join table: the segment key and how many (unique,
-// segment) entries hold it.  Padded to 16 bytes, so that a slot never straddles
-// a sector: a probe and the updates that follow it touch one sector.
-struct __align__(16) JSlot {
-    unsigned long long key;
-    uint32_t cnt;
-    uint32_t pad;
-};
 
 // Device-resident counters of one clustering call (one struct, zeroed first).
 struct Counters {
@@ -268,7 +260,11 @@ struct Buffers {
     uint32_t *bp_units = nullptr;                   // [cap_binpairs+1]
     uint32_t *bp_small = nullptr;                   // [cap_binpairs] schedule positions of small bin pairs
     // segment join: table of (unique, segment) keys and the groups they form
-    JSlot *jn_tab = nullptr;                        // [jn_mask+1] segment-join table
+    // segment-join table: the keys (all ones = empty slot) and, apart, how
+    // many (unique, segment) entries hold each key, so that the passes over
+    // the slots read 4 bytes per slot
+    unsigned long long *jn_key = nullptr;           // [jn_mask+1]
+    uint32_t *jn_cnt = nullptr;                     // [jn_mask+1]
     uint64_t jn_mask = 0;
     uint32_t *jn_islot = nullptr;                   // [4*N] slot of (unique, segment)
     uint32_t *jn_start = nullptr;                   // [jn_mask+2] group size -> start, per table slot

@@ -556,7 +556,8 @@ __device__ __forceinline__ uint32_t join_mask(uint32_t nu, uint32_t smax, uint64
 // The probed prefix is sized by the unique count, or by `rows` (an upper
 // bound) when the inserts run by row chunk, before the count is known.
 __global__ void k_join_clear(Counters *ctr, uint32_t smax, uint64_t cap_mask,
-                             JSlot *__restrict__ tab, uint32_t rows) {
+                             unsigned long long *__restrict__ key, uint32_t *__restrict__ cnt,
+                             uint32_t rows) {
     const uint32_t n = join_mask(rows ? rows : ctr->n_uniques, smax, cap_mask) + 1u;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         ctr->n_jslots = n;
@@ -564,7 +565,8 @@ __global__ void k_join_clear(Counters *ctr, uint32_t smax, uint64_t cap_mask,
     }
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
-        *reinterpret_cast<uint4 *>(&tab[i]) = make_uint4(~0u, ~0u, 0u, 0u);   // one 16-byte store
+        key[i] = ~0ull;
+        cnt[i] = 0u;
     }
 }
 
@@ -573,7 +575,8 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
               const uint32_t *__restrict__ ulen, const uint32_t *__restrict__ urep,
               const uint8_t *__restrict__ seq, const int64_t *__restrict__ seq_off,
               const uint8_t *__restrict__ codemap, const int16_t *__restrict__ eps_tab,
-              JSlot *tab, uint32_t *__restrict__ islot, uint32_t *__restrict__ irank, uint32_t smax,
+              unsigned long long *tkey, uint32_t *tcnt, uint32_t *__restrict__ islot,
+              uint32_t *__restrict__ irank, uint32_t smax,
               int chunk) {
     __shared__ uint8_t cm[256];
     for (int k = threadIdx.x; k < 256; k += blockDim.x) cm[k] = codemap[k];
@@ -605,9 +608,9 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
                         sl = kNone;
                         break;
                     }
-                    unsigned long long cur = *((volatile unsigned long long *)&tab[sl].key);
+                    unsigned long long cur = *((volatile unsigned long long *)&tkey[sl]);
                     if (cur == ~0ull) {
-                        cur = atomicCAS(&tab[sl].key, ~0ull, key);
+                        cur = atomicCAS(&tkey[sl], ~0ull, key);
                         if (cur == ~0ull) { won = true; break; }
                     }
                     if (cur == key) break;
@@ -622,7 +625,7 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
             const uint32_t grp = __match_any_sync(am, sl);
             const int leader = __ffs(grp) - 1;
             uint32_t base = 0;
-            if (lane == (uint32_t)leader && sl != kNone) base = atomicAdd(&tab[sl].cnt, (uint32_t)__popc(grp));
+            if (lane == (uint32_t)leader && sl != kNone) base = atomicAdd(&tcnt[sl], (uint32_t)__popc(grp));
             base = __shfl_sync(am, base, leader);
             if (k < S) irank[(size_t)u * smax + k] = base + (uint32_t)__popc(grp & ((1u << lane) - 1u));
         }
@@ -631,24 +634,41 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
 
 // Size of every key's group, per table slot (0 for an empty slot and for a
 // key held by one unique), and the bin-pair index of the slots that hold
-// groups (one counter atomic per block and pass).  A sequential pass over the
-// probed prefix of the table.
+// groups.  A sequential pass over the probed prefix of the table, four slots
+// per thread (16-byte loads and stores), with one counter atomic per block and
+// pass of 4 x 256 slots (the counter's atomics bounded the pass at one slot per
+// thread).
 __global__ void __launch_bounds__(256)
-k_join_sizes(Counters *ctr, const JSlot *__restrict__ tab, uint32_t *__restrict__ sizes,
+k_join_sizes(Counters *ctr, const uint32_t *__restrict__ tcnt, uint32_t *__restrict__ sizes,
              uint32_t *__restrict__ bpidx) {
     __shared__ uint32_t s_w[8];
     __shared__ uint32_t s_base;
     const uint32_t ns = ctr->n_jslots;
     const uint32_t lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t stride = 4 * gridDim.x * blockDim.x;
     if (blockIdx.x == 0 && threadIdx.x == 0) sizes[ns] = 0u;   // the scan's end: the total
-    for (uint32_t h0 = blockIdx.x * blockDim.x; h0 < ns; h0 += stride) {
-        const uint32_t h = h0 + threadIdx.x;
-        const uint32_t c = h < ns ? tab[h].cnt : 0u;   // an empty slot counts 0
-        const bool grp = c >= 2;
-        if (h < ns) sizes[h] = grp ? c : 0u;
-        const uint32_t m = __ballot_sync(0xFFFFFFFFu, grp);
-        if (lane == 0) s_w[wid] = (uint32_t)__popc(m);
+    for (uint32_t h0 = 4 * blockIdx.x * blockDim.x; h0 < ns; h0 += stride) {
+        const uint32_t h = h0 + 4 * threadIdx.x;
+        uint32_t c[4] = {0u, 0u, 0u, 0u};
+        if (h + 4 <= ns) {   // the probed prefix is a power of two >= 1024: whole quads
+            const uint4 v = *reinterpret_cast<const uint4 *>(tcnt + h);
+            c[0] = v.x; c[1] = v.y; c[2] = v.z; c[3] = v.w;
+        }
+        uint32_t mine = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (c[k] < 2) c[k] = 0;
+            mine += c[k] != 0;
+        }
+        if (h + 4 <= ns) *reinterpret_cast<uint4 *>(sizes + h) = make_uint4(c[0], c[1], c[2], c[3]);
+        // rank of this thread's groups in the block: warp scan, then warp sums
+        uint32_t incl = mine;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
+            if (lane >= (uint32_t)d) incl += t;
+        }
+        if (lane == 31) s_w[wid] = incl;
         __syncthreads();
         if (threadIdx.x == 0) {
             uint32_t t = 0;
@@ -656,7 +676,10 @@ k_join_sizes(Counters *ctr, const JSlot *__restrict__ tab, uint32_t *__restrict_
             s_base = t ? atomicAdd(&ctr->n_groups, t) : 0u;
         }
         __syncthreads();
-        if (grp) bpidx[h] = s_base + s_w[wid] + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        uint32_t idx = s_base + s_w[wid] + incl - mine;
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (c[k]) bpidx[h + k] = idx++;
         __syncthreads();
     }
 }
@@ -671,7 +694,7 @@ k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restr
             const int64_t *__restrict__ seq_off, const uint8_t *__restrict__ codemap,
             const int16_t *__restrict__ eps_tab, const uint32_t *__restrict__ islot,
             const uint64_t *__restrict__ vbits, const uint64_t *__restrict__ jbits,
-            const JSlot *__restrict__ tab, const uint32_t *__restrict__ start,
+            const uint32_t *__restrict__ start,
             const uint32_t *__restrict__ irank, uint32_t smax, uint4 *__restrict__ ent_rec,
             uint4 *__restrict__ ent_meta, int planes, uint32_t W, uint64_t cap_entries,
             uint32_t *err) {
@@ -715,7 +738,7 @@ __global__ void k_join_nbp(Counters *ctr) {
 // One bin pair (a group against itself) per key held by two or more uniques:
 // a sequential pass over the probed prefix of the table.
 __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
-                               const JSlot *__restrict__ tab, const uint32_t *__restrict__ start,
+                               const unsigned long long *__restrict__ tkey, const uint32_t *__restrict__ start,
                                const uint32_t *__restrict__ bpidx, const int16_t *__restrict__ eps_tab,
                                uint32_t TX, uint64_t cap_bp, BinPair *__restrict__ out, uint32_t *err) {
     const uint32_t ns = ctr->n_jslots;
@@ -725,7 +748,7 @@ __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
         if (c < 2) continue;
         const uint32_t k = bpidx[h];
         if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); continue; }
-        const unsigned long long key = tab[h].key;
+        const unsigned long long key = tkey[h];
         const uint32_t L = (uint32_t)(key >> 32) & 0xFFu;
         const uint32_t li = L - g.Lmin;
         BinPair P;
@@ -748,7 +771,7 @@ __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
 void launch_join_init(const Plan &P, const Buffers &B, cudaStream_t s) {
     cudaMemsetAsync(&B.ctr->n_jslots, 0, 2 * sizeof(uint32_t), s);   // n_jslots, n_groups
     k_join_clear<<<grid_wave(k_join_clear, B.jn_mask + 1, kThreads), kThreads, 0, s>>>(
-        B.ctr, P.join_smax, B.jn_mask, B.jn_tab, P.front_join ? P.N : 0u);
+        B.ctr, P.join_smax, B.jn_mask, B.jn_key, B.jn_cnt, P.front_join ? P.N : 0u);
 }
 
 void launch_join_insert(const Plan &P, const Buffers &B, int chunk, cudaStream_t s) {
@@ -756,7 +779,7 @@ void launch_join_insert(const Plan &P, const Buffers &B, int chunk, cudaStream_t
     const uint32_t rows = chunk < 0 ? P.N : P.chunk_row[chunk + 1] - P.chunk_row[chunk];
     if (rows == 0) return;
     k_join_insert<<<grid_wave(k_join_insert, rows, kThreads), kThreads, 0, s>>>(
-        g, B.ctr, B.urow, B.ulen, B.urep, B.seq, B.seq_off, B.codemap, B.eps_tab, B.jn_tab,
+        g, B.ctr, B.urow, B.ulen, B.urep, B.seq, B.seq_off, B.codemap, B.eps_tab, B.jn_key, B.jn_cnt,
         B.jn_islot, B.jn_cur, P.join_smax, chunk);
 }
 
@@ -769,7 +792,7 @@ void launch_buckets(const Plan &P, const Buffers &B, cudaStream_t s) {
             launch_join_insert(P, B, -1, s);
         }
         k_join_sizes<<<grid_wave(k_join_sizes, slots, kThreads), kThreads, 0, s>>>(
-            B.ctr, B.jn_tab, B.jn_start, B.jn_bpidx);
+            B.ctr, B.jn_cnt, B.jn_start, B.jn_bpidx);
         scan_u32(B.jn_start, B.jn_start, (uint32_t)slots + 1, &B.ctr->n_jslots1, &B.ctr->n_entries,
                  B.scan_part, B.scan_part_cap, s);
         return;
@@ -797,7 +820,7 @@ void launch_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
         auto go = [&](auto kern) {
             kern<<<grid_wave(kern, P.N, kThreads), kThreads, 0, s>>>(g, B.ctr, B.urow, B.ulen, B.seq, B.seq_off,
                                                      B.codemap, B.eps_tab, B.jn_islot, B.vbits,
-                                                     B.jbits, B.jn_tab, B.jn_start, B.jn_cur, P.join_smax,
+                                                     B.jbits, B.jn_start, B.jn_cur, P.join_smax,
                                                      B.ent_rec, B.ent_meta, planes, P.W,
                                                      P.cap_entries, &B.ctr->error);
         };
@@ -854,7 +877,7 @@ void launch_binpairs_fill(const Plan &P, const Buffers &B, cudaStream_t s) {
     if (P.join) {
         BinGeom g{P.Gv, P.Gj, P.NL, P.Lmin, P.VW, P.JW, P.K};
         k_join_bp_fill<<<grid_wave(k_join_bp_fill, B.jn_mask + 1, kThreads), kThreads, 0, s>>>(
-            g, B.ctr, B.jn_tab, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX, P.cap_binpairs, B.bp,
+            g, B.ctr, B.jn_key, B.jn_start, B.jn_bpidx, B.eps_tab, P.TX, P.cap_binpairs, B.bp,
             &B.ctr->error);
         return;
     }
