@@ -29,9 +29,6 @@ constexpr uint32_t kTinySide = 8;
 // buckets evaluate their pairs faster (64 repertoires, 1M rows: 2.92 against
 // 3.09 ms per call; eps 1: 1.25 against 0.99 ms for the join).
 constexpr int kJoinMaxEps = 2;
-// Segment join: flag in a (unique, segment) entry's slot index for the entry
-// that created the key (slot indices stay below 2^31).
-constexpr uint32_t kHeadBit = 0x80000000u;
 constexpr int kMlpIn = 16;              // learned scheduler: features per bin pair
 constexpr int kMlpHidden = 64;          // two hidden layers of 64
 constexpr int kMlpParams = kMlpIn * kMlpHidden + kMlpHidden + kMlpHidden * kMlpHidden + kMlpHidden +

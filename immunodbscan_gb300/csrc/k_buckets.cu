@@ -598,7 +598,6 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
         build_planes(seq + seq_off[row], S ? L : 0u, cm, wd);
         for (uint32_t k = 0; k < 4; ++k) {
             uint32_t sl = kNone;
-            bool won = false;
             if (k < S) {
                 const unsigned long long key = seg_key(wd, r, L, k, k * L / S, (k + 1) * L / S);
                 sl = (uint32_t)(mix64(key, 0x51ull) & mask);
@@ -611,13 +610,13 @@ k_join_insert(BinGeom g, Counters *ctr, const uint32_t *__restrict__ urow,
                     unsigned long long cur = *((volatile unsigned long long *)&tkey[sl]);
                     if (cur == ~0ull) {
                         cur = atomicCAS(&tkey[sl], ~0ull, key);
-                        if (cur == ~0ull) { won = true; break; }
+                        if (cur == ~0ull) break;   // this entry created the key
                     }
                     if (cur == key) break;
                     sl = (sl + 1) & (uint32_t)mask;
                 }
             }
-            islot[(size_t)u * 4 + k] = sl == kNone ? kNone : (sl | (won ? kHeadBit : 0u));
+            islot[(size_t)u * 4 + k] = sl;
             // one count increment per key among the lanes here together; the
             // count before it ranks the entry within its key's group (its
             // place in the group's entries, k_join_fill)
@@ -711,9 +710,8 @@ k_join_fill(BinGeom g, const Counters *__restrict__ ctr, const uint32_t *__restr
         uint4 rec[RSC];
         build_small_record<RSC>(seq + seq_off[row], L, cm, planes, W, rec);
         for (uint32_t k = 0; k < S; ++k) {
-            const uint32_t e = islot[(size_t)u * 4 + k];
-            if (e == kNone) continue;
-            const uint32_t sl = e & ~kHeadBit;
+            const uint32_t sl = islot[(size_t)u * 4 + k];
+            if (sl == kNone) continue;
             const uint32_t s0 = start[sl];
             if (start[sl + 1] - s0 < 2) continue;              // a key of one unique: no group
             const uint64_t pos = (uint64_t)s0 + irank[(size_t)u * smax + k];
