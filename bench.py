@@ -31,6 +31,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes as C
+import gc
 import json
 import math
 import os
@@ -523,16 +524,25 @@ def main():
         # the first call runs eagerly, the second also captures the shape, the
         # rest replay it (idb_cluster's plan cache); a few replays before the
         # timed ones
+        call_args = (ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o))
         for _ in range(max(6, args.warmup)):
-            _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
+            _lib.check(L.idb_cluster(*call_args))
         barrier(world)
         times, dev_ms, dev_phases = [], [], []
-        for _ in range(args.steps):
-            t0 = time.perf_counter()
-            _lib.check(L.idb_cluster(ctx_learned.handle, C.byref(hin), C.byref(prm), C.byref(o)))
-            times.append(time.perf_counter() - t0)
-            dev_ms.append(est.ms_total)
-            dev_phases.append([est.ms_phase[k] for k in range(5)])
+        # the interpreter's cyclic garbage collector runs outside the timed
+        # calls (a collection in this process can take tens of ms)
+        gc.collect()
+        gc.disable()
+        try:
+            for _ in range(args.steps):
+                t0 = time.perf_counter()
+                rc = L.idb_cluster(*call_args)
+                times.append(time.perf_counter() - t0)
+                _lib.check(rc)
+                dev_ms.append(est.ms_total)
+                dev_phases.append([est.ms_phase[k] for k in range(5)])
+        finally:
+            gc.enable()
         barrier(world)
         e2e_s = allreduce_max(world, float(np.mean(times)))
         h2d = sum(int(a.numel() * a.element_size()) for a in hkeep if isinstance(a, torch.Tensor))

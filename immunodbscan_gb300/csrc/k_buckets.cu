@@ -739,29 +739,36 @@ __global__ void k_join_bp_fill(BinGeom g, const Counters *__restrict__ ctr,
                                const unsigned long long *__restrict__ tkey, const uint32_t *__restrict__ start,
                                const uint32_t *__restrict__ bpidx, const int16_t *__restrict__ eps_tab,
                                uint32_t TX, uint64_t cap_bp, BinPair *__restrict__ out, uint32_t *err) {
-    const uint32_t ns = ctr->n_jslots;
-    const uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t h = blockIdx.x * blockDim.x + threadIdx.x; h < ns; h += stride) {
-        const uint32_t s0 = start[h], c = start[h + 1] - s0;
-        if (c < 2) continue;
-        const uint32_t k = bpidx[h];
-        if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); continue; }
-        const unsigned long long key = tkey[h];
-        const uint32_t L = (uint32_t)(key >> 32) & 0xFFu;
-        const uint32_t li = L - g.Lmin;
-        BinPair P;
-        P.a_start = s0; P.a_n = c; P.b_start = s0; P.b_n = c;
-        P.unit_base = 0;
-        P.ncx = (c + TX - 1) / TX;
-        P.la = (uint16_t)L; P.lb = (uint16_t)L;
-        P.v = (uint16_t)((key >> 30) & 3u);                   // segment of the group
-        P.j = (uint16_t)seg_count(eps_tab, g.NL, li);         // segments of length L
-        P.eps = eps_tab[(size_t)li * g.NL + li];
-        P.same = 1;
-        const uint64_t cost = (uint64_t)c * (c - 1) / 2;
-        P.cls = (uint8_t)(cost ? 63 - __clzll((long long)cost) : 0);
-        P.cost_lo = (uint32_t)min(cost, (uint64_t)0xFFFFFFFFu);
-        out[k] = P;
+    const uint32_t ns = ctr->n_jslots;   // a power of two >= 1024: whole quads of slots
+    const uint32_t stride = 4 * gridDim.x * blockDim.x;
+    for (uint32_t h0 = 4 * (blockIdx.x * blockDim.x + threadIdx.x); h0 < ns; h0 += stride) {
+        // four slots a thread: their starts in one 16-byte load, and the next
+        // quad's first start (start has ns + 1 entries)
+        const uint4 v = *reinterpret_cast<const uint4 *>(start + h0);
+        const uint32_t sv[5] = {v.x, v.y, v.z, v.w, start[h0 + 4]};
+#pragma unroll
+        for (uint32_t q = 0; q < 4; ++q) {
+            const uint32_t h = h0 + q, s0 = sv[q], c = sv[q + 1] - s0;
+            if (c < 2) continue;
+            const uint32_t k = bpidx[h];
+            if (k >= cap_bp) { atomicOr(err, kErrBinPairOverflow); continue; }
+            const unsigned long long key = tkey[h];
+            const uint32_t L = (uint32_t)(key >> 32) & 0xFFu;
+            const uint32_t li = L - g.Lmin;
+            BinPair P;
+            P.a_start = s0; P.a_n = c; P.b_start = s0; P.b_n = c;
+            P.unit_base = 0;
+            P.ncx = (c + TX - 1) / TX;
+            P.la = (uint16_t)L; P.lb = (uint16_t)L;
+            P.v = (uint16_t)((key >> 30) & 3u);                   // segment of the group
+            P.j = (uint16_t)seg_count(eps_tab, g.NL, li);         // segments of length L
+            P.eps = eps_tab[(size_t)li * g.NL + li];
+            P.same = 1;
+            const uint64_t cost = (uint64_t)c * (c - 1) / 2;
+            P.cls = (uint8_t)(cost ? 63 - __clzll((long long)cost) : 0);
+            P.cost_lo = (uint32_t)min(cost, (uint64_t)0xFFFFFFFFu);
+            out[k] = P;
+        }
     }
 }
 }  // namespace
