@@ -38,7 +38,8 @@ class Params(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("tile_rx", C.c_int32), ("tile_ty", C.c_int32), ("ms_distance", C.c_double),
                 ("n_tried", C.c_int32), ("tried_rx", C.c_int32 * 16), ("tried_ty", C.c_int32 * 16),
-                ("tried_ms", C.c_double * 16)]
+                ("tried_ms", C.c_double * 16), ("schedule", C.c_int32),
+                ("schedule_ms", C.c_double * 2)]
 
 
 class Input(C.Structure):

@@ -1801,16 +1801,9 @@ idb_status idb_autotune(idb_context *c, const idb_input *in, const idb_params *p
     }
     if (cand.size() > 16) cand.resize(16);
     if (P.cap_edges == 0) TRY(alloc_edges(pl, std::max<uint64_t>(4ull * P.N, 1ull << 16)));
-    double best_ms = 1e30;
-    for (auto &cd : cand) {
-        Plan Q = P;
-        if (P.fast) {
-            Q.RX = cd.first;
-            Q.TX = 32 * Q.RX;
-            Q.TY = cd.second;
-        } else {
-            Q.TY = cd.second;
-        }
+    // one shape and schedule order: bin pairs, the order, then the distance
+    // kernel three times (best of the three)
+    auto time_shape = [&](Plan Q, float *ms_out) -> idb_status {
         CU(cudaMemsetAsync(&B.ctr->n_binpairs, 0, 4, s));
         launch_binpairs(Q, B, s);
         TRY(read_counters(pl));
@@ -1818,6 +1811,7 @@ idb_status idb_autotune(idb_context *c, const idb_input *in, const idb_params *p
         TRY(alloc_binpairs(pl, c->h_ctr->n_binpairs));
         Q.cap_binpairs = pl.P.cap_binpairs;
         launch_binpairs_fill(Q, B, s);
+        if (Q.schedule == 1) launch_mlp_predict(B, (uint32_t)Q.cap_binpairs, c->mlp_bf16, s);
         launch_schedule(Q, B, s);
         float ms_best = 1e30f;
         for (int rep = 0; rep < 3; ++rep) {
@@ -1843,16 +1837,46 @@ idb_status idb_autotune(idb_context *c, const idb_input *in, const idb_params *p
                 ms_best = 1e30f;
             }
         }
+        *ms_out = ms_best;
+        return IDB_OK;
+    };
+    double best_ms = 1e30;
+    Plan best_plan = P;
+    for (auto &cd : cand) {
+        Plan Q = P;
+        Q.schedule = 0;
+        if (P.fast) {
+            Q.RX = cd.first;
+            Q.TX = 32 * Q.RX;
+            Q.TY = cd.second;
+        } else {
+            Q.TY = cd.second;
+        }
+        float ms_best = 0;
+        TRY(time_shape(Q, &ms_best));
         const int k = best->n_tried++;
         best->tried_rx[k] = Q.RX;
         best->tried_ty[k] = (int)Q.TY;
         best->tried_ms[k] = ms_best;
         if (ms_best < best_ms) {
             best_ms = ms_best;
+            best_plan = Q;
             best->tile_rx = Q.RX;
             best->tile_ty = (int)Q.TY;
             best->ms_distance = ms_best;
         }
+    }
+    // the schedule order for the fastest shape: static heavy-first, or the
+    // learned cost when the context holds a model
+    best->schedule = 0;
+    best->schedule_ms[0] = best_ms;
+    if (c->has_model) {
+        Plan Q = best_plan;
+        Q.schedule = 1;
+        float ms_learned = 0;
+        TRY(time_shape(Q, &ms_learned));
+        best->schedule_ms[1] = ms_learned;
+        if (ms_learned < best_ms) best->schedule = 1;
     }
     TRY(device_errors(*c->h_ctr));
     return IDB_OK;

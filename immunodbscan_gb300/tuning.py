@@ -68,7 +68,8 @@ def measure(w, ctx: Optional[Context] = None) -> dict:
     _lib.check(_lib.lib().idb_autotune(ctx.handle if ctx else None, C.byref(inp), C.byref(prm),
                                        C.byref(t)))
     tried = [{"rx": t.tried_rx[k], "ty": t.tried_ty[k], "ms": t.tried_ms[k]} for k in range(t.n_tried)]
-    return {"rx": t.tile_rx, "ty": t.tile_ty, "ms": t.ms_distance, "tried": tried}
+    return {"rx": t.tile_rx, "ty": t.tile_ty, "ms": t.ms_distance, "tried": tried,
+            "schedule": t.schedule, "schedule_ms": [t.schedule_ms[0], t.schedule_ms[1]]}
 
 
 def shape_for(w, ctx: Optional[Context] = None, cache_path: str = DEFAULT_CACHE,

@@ -206,7 +206,11 @@ idb_status idb_dedupe_noalloc(const char *seqs, const int64_t *seq_offsets,
 /* Autotuner: builds the buckets of the input once, then times the distance
    kernel for every candidate work-unit shape (x-entries per lane, y-chunk
    length) on this data and returns the fastest in best->tile_rx/tile_ty
-   (pass them in idb_params for the real runs).  Host inputs as idb_cluster. */
+   (pass them in idb_params for the real runs).  For that shape it then times
+   the bucket-pair schedule orders: the static heavy-first order and, when the
+   context holds a model (idb_mlp_load), the learned one; the faster goes in
+   best->schedule (pass it as idb_params.schedule).  Host inputs as
+   idb_cluster. */
 typedef struct idb_tuning {
     int32_t tile_rx, tile_ty;   /* the fastest shape                              */
     double  ms_distance;        /* its distance-kernel time (best of the repeats)  */
@@ -214,6 +218,9 @@ typedef struct idb_tuning {
     int32_t tried_rx[16];
     int32_t tried_ty[16];
     double  tried_ms[16];
+    int32_t schedule;           /* the faster order for that shape: 0 static,
+                                   1 learned                                       */
+    double  schedule_ms[2];     /* distance-kernel time per order (0: not timed)   */
 } idb_tuning;
 idb_status idb_autotune(idb_context *ctx, const idb_input *in, const idb_params *prm,
                         idb_tuning *best);

@@ -91,3 +91,25 @@ def test_bf16_inference_matches_cpu_forward(gpu_ctx):
     assert np.max(np.abs(y_dev - y_bf16)) <= 1e-3 * span + 1e-3
     assert np.max(np.abs(y_dev - y_f64)) <= 2e-2 * span
     assert np.corrcoef(y_dev, y_f64)[0, 1] > 0.999
+
+
+def test_autotune_picks_a_schedule_order():
+    """With a model loaded the autotuner also times the learned order for the
+    fastest shape and reports the faster order; both orders give the same
+    partition."""
+    from immunodbscan_gb300 import Context
+    w = synth.workload(2, scale=0.01)
+    with Context(0) as ctx:
+        rec0 = tuning.measure(w, ctx)
+        assert rec0["schedule"] == 0 and rec0["schedule_ms"][0] > 0 and rec0["schedule_ms"][1] == 0
+        X, T = learned.profile(w, ctx)
+        p, _ = learned.train(X, T, ctx, epochs=50)
+        learned.install(ctx, p)
+        rec = tuning.measure(w, ctx)
+        assert rec["schedule"] in (0, 1)
+        assert rec["schedule_ms"][0] > 0 and rec["schedule_ms"][1] > 0
+        assert rec["schedule_ms"][rec["schedule"]] == min(rec["schedule_ms"])
+        tune = (rec["rx"], rec["ty"])
+        a = cluster_workload(w, ctx, schedule=0, tune=tune)
+        b = cluster_workload(w, ctx, schedule=1, tune=tune)
+        assert np.array_equal(a.clone_id, b.clone_id) and np.array_equal(a.core, b.core)
