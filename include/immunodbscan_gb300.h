@@ -117,8 +117,10 @@ typedef struct idb_stats {
     double   ms_distance;      /* device time of the distance kernel               */
     double   ms_phase[8];      /* front+dedupe, buckets+schedule, distance, graph,
                                   outputs (device time; eager calls include waits
-                                  on host read-backs)                              */
-    uint32_t kernel_launches;  /* kernels launched (graph replays)                 */
+                                  on host read-backs, and with host columns the
+                                  first phase includes the copies it overlaps)     */
+    uint32_t kernel_launches;  /* kernels in the replayed graph; 0 for an eager
+                                  call                                             */
     uint32_t core_edges;       /* neighbour pairs with both ends core              */
     uint64_t lev_columns;      /* text columns consumed by live Levenshtein pairs  */
     uint32_t candidates;       /* 0: every admissible pair of the buckets scored;
