@@ -44,6 +44,11 @@ import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# More hardware work queues than CUDA's default 8, set before CUDA starts in
+# this process: with torch's streams and several library contexts (three
+# streams each) a shared queue serialised unrelated streams and stalled single
+# idb_cluster calls by 20-30 ms.  A value set by the caller wins.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 METRIC = ("Gpair-distances/s and sequences clustered/s, batched+learned vs plain "
           "(identical partitions)")

@@ -5,6 +5,7 @@
 // defaults data/psdbscan.conf and data/ExampleData.csv.  Reads the input
 // table(s), clusters through the C ABI (idb_cluster), writes the output table
 // and the benchmark log named by the configuration.
+#include <cstdlib>
 #include <iostream>
 #include <string>
 #include <vector>
@@ -26,6 +27,11 @@ void usage() {
 }  // namespace
 
 int main(int argc, char **argv) {
+    // more hardware work queues than CUDA's default 8, before the first CUDA
+    // call: the library's copy, side and main streams then never share a
+    // queue with one another (a shared queue serialises unrelated streams and
+    // stalled single calls by tens of milliseconds); a value the user set wins
+    setenv("CUDA_DEVICE_MAX_CONNECTIONS", "32", 0);
     using psdb::Benchmark;
     Benchmark &bm = Benchmark::instance();
     bm.start("Overall");
